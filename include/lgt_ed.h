@@ -1,0 +1,221 @@
+/*
+ * lgt_ed.h -- C ABI of the GB300 exact-diagonalisation library (liblgted.so).
+ *
+ * Drop-in boundary for the exact-diagonalisation path of NoaFeldman/LGT
+ * (finite_ed.jl with the local-operator conventions of u1_lgt_hamiltonian.jl
+ * and, for the plaquette + Jordan-Wigner model, the term list of
+ * matter_gauge_entanglement_pjw.jl).  Each entry point names the reference
+ * function it replaces.  A Julia `ccall` shim binds these symbols one to one
+ * (lgt_gb300/julia/LGTED.jl).
+ *
+ * Conventions
+ *  - Every function returns an lgt_status; 0 is success.  lgt_last_error()
+ *    gives a message for the calling thread's last failure.  Nothing aborts
+ *    the process: the reference's @assert failures become status codes.
+ *  - The library owns all device memory behind opaque handles.  Host buffers
+ *    are caller-owned.  Arrays that mirror Julia matrices are column-major.
+ *  - Basis indices returned to the caller are 1-based where they replace a
+ *    reference index (key_dict values), 0-based elsewhere, as documented.
+ *  - Amplitude panels are "K-interleaved": element (row, k, comp) of K
+ *    vectors of length N lives at ((row * K) + k) * ncomp + comp, ncomp = 1
+ *    for real and 2 for complex (re, im).  For K = 1, ncomp = 2 this is
+ *    exactly a Julia Vector{ComplexF64}.
+ *  - A handle is used by one host thread at a time.  Each basis handle owns
+ *    a CUDA stream; calls return when results are in the caller's buffers.
+ *  - Flags LGT_DEVICE_PTRS: the amplitude pointers given to lgt_matvec,
+ *    lgt_observe, lgt_ground_state and lgt_expm_steps are device pointers on
+ *    the basis's device (no host<->device copies are made).
+ */
+#ifndef LGT_ED_H
+#define LGT_ED_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define LGT_API __attribute__((visibility("default")))
+#else
+#define LGT_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t lgt_status;
+
+enum {
+  LGT_OK = 0,
+  LGT_ERR_ARG = 1,        /* invalid argument (sizes, pointers, flags)          */
+  LGT_ERR_SECTOR = 2,     /* inconsistent charge sector (finite_ed.jl:127)      */
+  LGT_ERR_KEYWIDTH = 3,   /* lattice/dg beyond the key width                    */
+  LGT_ERR_MEMORY = 4,     /* device allocation failed                           */
+  LGT_ERR_CUDA = 5,       /* a CUDA call failed                                 */
+  LGT_ERR_NOCONV = 6,     /* Krylov solver did not converge (finite_ed.jl:339)  */
+  LGT_ERR_DEVICE = 7,     /* a kernel self-check failed (rank/bounds/NaN)       */
+  LGT_ERR_NOTFOUND = 8,   /* state not in the basis (finite_ed.jl:530)          */
+  LGT_ERR_UNSUPPORTED = 9 /* feature not available for these arguments          */
+};
+
+/* Model flags (bit set) for lgt_ham_create. */
+enum {
+  LGT_MODEL_REF = 0,   /* finite_ed.jl:252-322: on-site + bare hopping          */
+  LGT_MODEL_JW = 1,    /* Jordan-Wigner strings on the column snake             */
+  LGT_MODEL_PLAQ = 2,  /* magnetic plaquette -(1/2g^2)(W + W^dag)              */
+  LGT_MODEL_PJW = 3    /* matter_gauge_entanglement_pjw.jl:82-147               */
+};
+
+/* Arithmetic of the amplitude panels. */
+enum {
+  LGT_FP64 = 0,        /* FP64 amplitudes, coefficients and accumulation       */
+  LGT_FP32 = 1,        /* FP32 amplitudes, coefficients and accumulation       */
+  LGT_FP32_MIXED = 2   /* Krylov drivers: FP32 H*psi and storage, FP64 dots,
+                          reorthogonalisation, tridiagonal solve, residual and
+                          refinement                                           */
+};
+
+enum { LGT_DEVICE_PTRS = 1 };
+
+typedef struct lgt_basis lgt_basis;
+typedef struct lgt_ham lgt_ham;
+
+/* Krylov solver options.  lgt_krylov_defaults() fills the reference's values
+   (finite_ed.jl:336-338 for eigsolve, :417-419 for exponentiate). */
+typedef struct lgt_krylov_opts {
+  int32_t krylovdim;     /* Krylov dimension (eigsolve: 50, exponentiate: 30) */
+  int32_t maxiter;       /* restarts (eigsolve: 300, exponentiate: 100)        */
+  double tol;            /* absolute residual / error tolerance (1e-10)        */
+  int32_t precision;     /* LGT_FP64 or LGT_FP32_MIXED                         */
+  int32_t reorth_passes; /* Gram-Schmidt passes against the whole basis (2)    */
+  int32_t check_every;   /* steps between convergence checks                   */
+  int32_t refine_steps;  /* FP64 correction steps after an FP32 solve          */
+  uint64_t seed;         /* start vector of point k: normal(seed, k)           */
+  int32_t use_graph;     /* replay the step sequence as a CUDA graph           */
+  int32_t start_given;   /* ground state: 1 = psi holds the start vectors      */
+} lgt_krylov_opts;
+
+/* Per-call solver report. */
+typedef struct lgt_info {
+  int64_t matvecs;       /* H*psi panel applications                           */
+  int32_t restarts;      /* Krylov restarts                                    */
+  int32_t converged;     /* points that met tol                                */
+  double max_residual;   /* largest final residual / error estimate            */
+  double seconds;        /* device time of the call (CUDA events)              */
+} lgt_info;
+
+/* Observables of one state (one coupling point), measure_ED
+   (finite_ed.jl:369-393) plus the plaquette.  Grids are column-major. */
+typedef struct lgt_obs {
+  double t;              /* time stamp passed by the caller                    */
+  double nf_mean, nf_even, nf_odd, E2_mean;
+  double plaq_mean;      /* (1/N_P) sum_p <W_p + W_p^dag>                       */
+  double n_stag;         /* (1/N_s) sum (-1)^(ix+iy) <n_f>                     */
+  double norm2;          /* <psi|psi>                                          */
+} lgt_obs;
+
+LGT_API void lgt_krylov_defaults(lgt_krylov_opts* o, int for_exponentiate);
+LGT_API const char* lgt_last_error(void);
+LGT_API const char* lgt_version(void);
+
+/* ---- basis -------------------------------------------------------------- */
+
+/* build_basis (finite_ed.jl:125-162).  g_charges: nx*ny, column-major
+   (g[ix,iy] at (ix-1) + (iy-1)*nx).  Enumerates the Gauss-law sector on the
+   GPU as sorted order keys.  device < 0 uses the current device. */
+LGT_API lgt_status lgt_basis_create(int32_t nx, int32_t ny, int32_t dg, const int32_t* g_charges,
+                            int32_t device, lgt_basis** out);
+
+/* length(states) (finite_ed.jl:133,227-231). */
+LGT_API lgt_status lgt_basis_dim(const lgt_basis* b, int64_t* dim);
+
+/* Keys of states [first, first+count): the order key (mask << w*N_U | e_U
+   digits, strictly increasing in reference index order) and/or the
+   reference _encode key (finite_ed.jl:80-97, dg == 1 only; bit pattern of
+   the Int64).  Either pointer may be NULL. */
+LGT_API lgt_status lgt_basis_keys(const lgt_basis* b, int64_t first, int64_t count, uint64_t* order_keys,
+                          int64_t* ref_keys);
+
+/* Contents of `states` (finite_ed.jl:229) for [first, first+count): per
+   state the column-major n_f (nx*ny), e_R ((nx-1)*ny), e_U (nx*(ny-1))
+   blocks, states one after the other.  Any pointer may be NULL. */
+LGT_API lgt_status lgt_basis_states(const lgt_basis* b, int64_t first, int64_t count, int8_t* n_f,
+                            int8_t* e_R, int8_t* e_U);
+
+/* key_dict lookup (finite_ed.jl:291-292,527-531): for each reference
+   _encode key, its 1-based index, or 0 when the configuration is not in the
+   basis.  dg == 1 only. */
+LGT_API lgt_status lgt_basis_lookup(const lgt_basis* b, const int64_t* ref_keys, int64_t n,
+                            int64_t* index1);
+
+/* Same for order keys: 0-based index or -1. */
+LGT_API lgt_status lgt_basis_rank(const lgt_basis* b, const uint64_t* order_keys, int64_t n,
+                          int64_t* index0);
+
+LGT_API void lgt_basis_destroy(lgt_basis* b);
+
+/* ---- Hamiltonian -------------------------------------------------------- */
+
+/* build_hamiltonian (finite_ed.jl:252-322) for K coupling points that share
+   the basis: point k has couplings g[k], t[k], m[k].  Matrix-free: nothing
+   of size nnz is stored.  model: LGT_MODEL_* flags. */
+LGT_API lgt_status lgt_ham_create(const lgt_basis* b, int32_t K, const double* g, const double* t,
+                          const double* m, uint32_t model, lgt_ham** out);
+
+/* Replace the couplings of all K points (quench: build_hamiltonian at the
+   final couplings, finite_ed.jl:582,632). */
+LGT_API lgt_status lgt_ham_set_couplings(lgt_ham* h, const double* g, const double* t, const double* m);
+
+/* nnz(H) as SparseArrays counts it (finite_ed.jl:355): stored diagonal
+   entries plus the off-diagonal entries. */
+LGT_API lgt_status lgt_ham_nnz(const lgt_ham* h, int64_t* nnz);
+
+/* The sparse matrix of point k as CSR (host buffers; rowptr has N+1 entries,
+   colidx/values nnz).  H is symmetric, so these are also the colptr/rowval/
+   nzval arrays of the reference's SparseMatrixCSC.  Indices are 0-based.
+   Values are computed in the reference's own summation order. */
+LGT_API lgt_status lgt_ham_export_csr(const lgt_ham* h, int32_t k, int64_t* rowptr, int32_t* colidx,
+                              double* values);
+
+/* y = H x for all K points (the SparseMatrixCSC * Vector product inside
+   KrylovKit).  x, y: K-interleaved panels of N rows; ncomp 1 or 2;
+   precision LGT_FP64 (double) or LGT_FP32 (float). */
+LGT_API lgt_status lgt_matvec(const lgt_ham* h, const void* x, void* y, int32_t ncomp, int32_t precision,
+                      uint32_t flags);
+
+/* find_ground_state (finite_ed.jl:333-341) for all K points: lowest
+   eigenpair by Lanczos with full reorthogonalisation.  E0: K doubles.  psi:
+   real panel [N][K] (double; float for LGT_FP32_MIXED with device pointers
+   is not accepted -- the output is always double), may be NULL.  residual:
+   K doubles (final FP64 residual norm ||H psi - E0 psi||), may be NULL. */
+LGT_API lgt_status lgt_ground_state(lgt_ham* h, const lgt_krylov_opts* opts, double* E0, void* psi,
+                            double* residual, uint32_t flags, lgt_info* info);
+
+/* evolve_ED! (finite_ed.jl:405-431): n_steps Krylov steps
+   psi <- exp(-i H dt) psi, each followed by renormalisation, for all K
+   points.  psi: complex double panel [N][K][2], updated in place.  obs:
+   (n_steps + 1) * K records (t = step * dt), filled every step, or NULL.
+   norm_drift: K doubles (max |1 - ||psi||| before renormalisation), may be
+   NULL. */
+LGT_API lgt_status lgt_expm_steps(lgt_ham* h, const lgt_krylov_opts* opts, double dt, int32_t n_steps,
+                          void* psi, lgt_obs* obs, double* norm_drift, uint32_t flags,
+                          lgt_info* info);
+
+/* measure_ED (finite_ed.jl:369-393) of K states: per point the nx*ny grids
+   <n_f> and <E^2> (column-major, point after point) and the (nx-1)*(ny-1)
+   plaquette grid <W + W^dag>; any grid pointer may be NULL.  summary: K
+   records, may be NULL.  psi: panel [N][K][ncomp] in `precision`. */
+LGT_API lgt_status lgt_observe(const lgt_ham* h, const void* psi, int32_t ncomp, int32_t precision,
+                       uint32_t flags, double t_now, double* nf_grid, double* E2_grid,
+                       double* plaq_grid, lgt_obs* summary);
+
+/* Energy <psi|H|psi> / <psi|psi> per point, FP64 (finite_ed.jl has no
+   counterpart; used for energy-drift reports of evolve_ED!). */
+LGT_API lgt_status lgt_energy(const lgt_ham* h, const void* psi, int32_t ncomp, uint32_t flags,
+                      double* energy);
+
+LGT_API void lgt_ham_destroy(lgt_ham* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LGT_ED_H */

@@ -1,0 +1,704 @@
+// capi.cu -- the extern "C" boundary (include/lgt_ed.h): handles, argument
+// checks, host<->device staging and error reporting around the kernels.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/lgt_ed.h"
+#include "lgt_hpsi.h"
+#include "lgt_internal.h"
+#include "lgt_krylov.h"
+#include "lgt_observe.h"
+
+using namespace lgt;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+lgt_status fail(lgt_status code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+lgt_status cuda_fail(cudaError_t e, const char* where) {
+  return fail(e == cudaErrorMemoryAllocation ? LGT_ERR_MEMORY : LGT_ERR_CUDA,
+              std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+lgt_status from_msg(const std::string& m) {
+  if (m.empty()) return LGT_OK;
+  if (m.rfind("NOCONV", 0) == 0) return fail(LGT_ERR_NOCONV, m);
+  if (m.find("out of memory") != std::string::npos) return fail(LGT_ERR_MEMORY, m);
+  return fail(LGT_ERR_CUDA, m);
+}
+
+#define CUDA_OR_FAIL(call)                            \
+  do {                                                \
+    cudaError_t e_ = (call);                          \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+// Device buffer owned by a handle, grown on demand.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t need(size_t b) {
+    if (b <= bytes) return cudaSuccess;
+    cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e == cudaSuccess) bytes = b;
+    return e;
+  }
+  void release() {
+    cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+}  // namespace
+
+struct lgt_basis {
+  BasisDev B;
+  int device = 0;
+};
+
+struct lgt_ham {
+  const lgt_basis* b = nullptr;
+  int K = 0;
+  uint32_t model = 0;
+  std::vector<double> g, t, m;
+  double* coef_d = nullptr;  // [4][K]: g^2/2, m, -t, -1/(2g^2)
+  float* coef_f = nullptr;
+  int seg_smem = 0;
+  KrylovCache* cache = nullptr;
+  DevBuf x, y, part, out;
+  OpDev op() const {
+    OpDev o;
+    o.G = b->B.G;
+    o.R = b->B.view();
+    o.err = b->B.err;
+    o.model = model;
+    o.K = K;
+    o.seg_smem = seg_smem;
+    o.cE_d = coef_d;
+    o.cm_d = coef_d + K;
+    o.ch_d = coef_d + 2 * K;
+    o.cp_d = coef_d + 3 * K;
+    o.cE_f = coef_f;
+    o.cm_f = coef_f + K;
+    o.ch_f = coef_f + 2 * K;
+    o.cp_f = coef_f + 3 * K;
+    return o;
+  }
+};
+
+namespace {
+
+lgt_status set_device(const lgt_basis* b) {
+  CUDA_OR_FAIL(cudaSetDevice(b->device));
+  return LGT_OK;
+}
+
+// Reads and clears the basis' device error word.
+lgt_status check_device_errors(const lgt_basis* b) {
+  int err = 0;
+  CUDA_OR_FAIL(cudaMemcpyAsync(&err, b->B.err, sizeof(int), cudaMemcpyDeviceToHost, b->B.stream));
+  CUDA_OR_FAIL(cudaStreamSynchronize(b->B.stream));
+  if (err) {
+    cudaMemsetAsync(b->B.err, 0, sizeof(int), b->B.stream);
+    std::string m = "device self-check failed:";
+    if (err & kDevErrRank) m += " neighbour key not in basis;";
+    if (err & kDevErrBounds) m += " index out of bounds;";
+    if (err & kDevErrNaN) m += " non-finite value;";
+    if (err & kDevErrSpin) m += " bounded wait expired;";
+    return fail(LGT_ERR_DEVICE, m);
+  }
+  return LGT_OK;
+}
+
+lgt_status upload_couplings(lgt_ham* h) {
+  const int K = h->K;
+  std::vector<double> cd(4 * size_t(K));
+  std::vector<float> cf(4 * size_t(K));
+  for (int k = 0; k < K; ++k) {
+    const double g = h->g[k], t = h->t[k], m = h->m[k];
+    if (!std::isfinite(g) || !std::isfinite(t) || !std::isfinite(m) || g == 0.0)
+      return fail(LGT_ERR_ARG, "couplings must be finite and g != 0");
+    cd[k] = (g * g) / 2;             // finite_ed.jl:268,271
+    cd[K + k] = m;                   // finite_ed.jl:274
+    cd[2 * K + k] = -t;              // finite_ed.jl:293-294,312-313
+    cd[3 * K + k] = -(1.0 / (2.0 * (g * g)));  // matter_gauge_entanglement_pjw.jl:131,142-143
+  }
+  for (size_t i = 0; i < cd.size(); ++i) cf[i] = float(cd[i]);
+  CUDA_OR_FAIL(cudaMemcpyAsync(h->coef_d, cd.data(), sizeof(double) * cd.size(),
+                               cudaMemcpyHostToDevice, h->b->B.stream));
+  CUDA_OR_FAIL(cudaMemcpyAsync(h->coef_f, cf.data(), sizeof(float) * cf.size(),
+                               cudaMemcpyHostToDevice, h->b->B.stream));
+  CUDA_OR_FAIL(cudaStreamSynchronize(h->b->B.stream));
+  return LGT_OK;
+}
+
+bool on_device(uint32_t flags) { return (flags & LGT_DEVICE_PTRS) != 0; }
+
+}  // namespace
+
+extern "C" {
+
+void lgt_krylov_defaults(lgt_krylov_opts* o, int for_exponentiate) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->krylovdim = for_exponentiate ? 30 : 50;   // finite_ed.jl:337,418
+  o->maxiter = for_exponentiate ? 100 : 300;   // finite_ed.jl:338,418
+  o->tol = 1e-10;                              // finite_ed.jl:338,419
+  o->precision = LGT_FP64;
+  o->reorth_passes = 2;
+  o->check_every = 5;
+  o->refine_steps = 0;
+  o->seed = 0;
+  o->use_graph = 1;
+  o->start_given = 0;
+}
+
+const char* lgt_last_error(void) { return g_last_error.c_str(); }
+
+const char* lgt_version(void) { return "lgted 0.1 (sm_103a)"; }
+
+lgt_status lgt_basis_create(int32_t nx, int32_t ny, int32_t dg, const int32_t* g_charges,
+                            int32_t device, lgt_basis** out) {
+  if (!out || !g_charges) return fail(LGT_ERR_ARG, "null argument");
+  *out = nullptr;
+  Geom G;
+  std::string m = make_geom(nx, ny, dg, g_charges, &G);
+  if (!m.empty()) {
+    if (m.rfind("Inconsistent sector", 0) == 0) return fail(LGT_ERR_SECTOR, m);
+    if (m.find("bits") != std::string::npos || m.find("31 sites") != std::string::npos)
+      return fail(LGT_ERR_KEYWIDTH, m);
+    return fail(LGT_ERR_ARG, m);
+  }
+  lgt_basis* b = new (std::nothrow) lgt_basis();
+  if (!b) return fail(LGT_ERR_MEMORY, "host allocation failed");
+  if (device < 0) {
+    if (cudaGetDevice(&b->device) != cudaSuccess) b->device = 0;
+  } else {
+    b->device = device;
+  }
+  cudaError_t e = cudaSetDevice(b->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->B.stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete b;
+    return cuda_fail(e, "lgt_basis_create");
+  }
+  b->B.G = G;
+  m = build_basis_device(&b->B);
+  if (!m.empty()) {
+    free_basis_device(&b->B);
+    cudaStreamDestroy(b->B.stream);
+    delete b;
+    if (m.find("memory") != std::string::npos) return fail(LGT_ERR_MEMORY, m);
+    return fail(LGT_ERR_CUDA, m);
+  }
+  *out = b;
+  return LGT_OK;
+}
+
+lgt_status lgt_basis_dim(const lgt_basis* b, int64_t* dim) {
+  if (!b || !dim) return fail(LGT_ERR_ARG, "null argument");
+  *dim = b->B.dim;
+  return LGT_OK;
+}
+
+lgt_status lgt_basis_keys(const lgt_basis* b, int64_t first, int64_t count, uint64_t* order_keys,
+                          int64_t* ref_keys) {
+  if (!b) return fail(LGT_ERR_ARG, "null basis");
+  if (first < 0 || count < 0 || first + count > b->B.dim) return fail(LGT_ERR_ARG, "range");
+  if (ref_keys && b->B.G.dg != 1)
+    return fail(LGT_ERR_UNSUPPORTED, "_encode keys exist only for dg == 1 (finite_ed.jl:89,93)");
+  lgt_status st = set_device(b);
+  if (st) return st;
+  if (count == 0) return LGT_OK;
+  cudaStream_t s = b->B.stream;
+  if (order_keys)
+    CUDA_OR_FAIL(cudaMemcpyAsync(order_keys, b->B.keys + first, sizeof(uint64_t) * count,
+                                 cudaMemcpyDeviceToHost, s));
+  if (ref_keys) {
+    uint64_t* d = nullptr;
+    CUDA_OR_FAIL(cudaMallocAsync(&d, sizeof(uint64_t) * count, s));
+    launch_ref_keys(b->B, first, count, d, s);
+    CUDA_OR_FAIL(cudaGetLastError());
+    CUDA_OR_FAIL(cudaMemcpyAsync(ref_keys, d, sizeof(uint64_t) * count, cudaMemcpyDeviceToHost, s));
+    CUDA_OR_FAIL(cudaFreeAsync(d, s));
+  }
+  CUDA_OR_FAIL(cudaStreamSynchronize(s));
+  return LGT_OK;
+}
+
+lgt_status lgt_basis_states(const lgt_basis* b, int64_t first, int64_t count, int8_t* n_f,
+                            int8_t* e_R, int8_t* e_U) {
+  if (!b) return fail(LGT_ERR_ARG, "null basis");
+  if (first < 0 || count < 0 || first + count > b->B.dim) return fail(LGT_ERR_ARG, "range");
+  lgt_status st = set_device(b);
+  if (st) return st;
+  if (count == 0) return LGT_OK;
+  const Geom& G = b->B.G;
+  cudaStream_t s = b->B.stream;
+  const size_t a = size_t(count) * G.ns, r = size_t(count) * G.nR, u = size_t(count) * G.nU;
+  int8_t* d = nullptr;
+  CUDA_OR_FAIL(cudaMallocAsync(&d, a + r + u + 3, s));
+  launch_decode_states(b->B, first, count, d, d + a, d + a + r, s);
+  CUDA_OR_FAIL(cudaGetLastError());
+  if (n_f) CUDA_OR_FAIL(cudaMemcpyAsync(n_f, d, a, cudaMemcpyDeviceToHost, s));
+  if (e_R && r) CUDA_OR_FAIL(cudaMemcpyAsync(e_R, d + a, r, cudaMemcpyDeviceToHost, s));
+  if (e_U && u) CUDA_OR_FAIL(cudaMemcpyAsync(e_U, d + a + r, u, cudaMemcpyDeviceToHost, s));
+  CUDA_OR_FAIL(cudaFreeAsync(d, s));
+  CUDA_OR_FAIL(cudaStreamSynchronize(s));
+  return LGT_OK;
+}
+
+static lgt_status rank_common(const lgt_basis* b, const void* keys, int64_t n, int64_t* out,
+                              bool ref) {
+  if (!b || (n > 0 && (!keys || !out))) return fail(LGT_ERR_ARG, "null argument");
+  if (n < 0) return fail(LGT_ERR_ARG, "negative count");
+  if (ref && b->B.G.dg != 1)
+    return fail(LGT_ERR_UNSUPPORTED, "_encode keys exist only for dg == 1");
+  lgt_status st = set_device(b);
+  if (st) return st;
+  if (n == 0) return LGT_OK;
+  cudaStream_t s = b->B.stream;
+  uint64_t* din = nullptr;
+  int64_t* dout = nullptr;
+  CUDA_OR_FAIL(cudaMallocAsync(&din, sizeof(uint64_t) * n, s));
+  CUDA_OR_FAIL(cudaMallocAsync(&dout, sizeof(int64_t) * n, s));
+  CUDA_OR_FAIL(cudaMemcpyAsync(din, keys, sizeof(uint64_t) * n, cudaMemcpyHostToDevice, s));
+  if (ref) launch_rank_ref_keys(b->B, din, n, dout, s);
+  else launch_rank_order_keys(b->B, din, n, dout, s);
+  CUDA_OR_FAIL(cudaGetLastError());
+  CUDA_OR_FAIL(cudaMemcpyAsync(out, dout, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, s));
+  CUDA_OR_FAIL(cudaFreeAsync(din, s));
+  CUDA_OR_FAIL(cudaFreeAsync(dout, s));
+  CUDA_OR_FAIL(cudaStreamSynchronize(s));
+  return LGT_OK;
+}
+
+lgt_status lgt_basis_lookup(const lgt_basis* b, const int64_t* ref_keys, int64_t n,
+                            int64_t* index1) {
+  return rank_common(b, ref_keys, n, index1, true);
+}
+
+lgt_status lgt_basis_rank(const lgt_basis* b, const uint64_t* order_keys, int64_t n,
+                          int64_t* index0) {
+  return rank_common(b, order_keys, n, index0, false);
+}
+
+void lgt_basis_destroy(lgt_basis* b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  cudaStreamSynchronize(b->B.stream);
+  free_basis_device(&b->B);
+  cudaStreamDestroy(b->B.stream);
+  delete b;
+}
+
+lgt_status lgt_ham_create(const lgt_basis* b, int32_t K, const double* g, const double* t,
+                          const double* m, uint32_t model, lgt_ham** out) {
+  if (!b || !g || !t || !m || !out) return fail(LGT_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (K < 1 || K > 256) return fail(LGT_ERR_ARG, "K must be in 1..256");
+  if (model > LGT_MODEL_PJW) return fail(LGT_ERR_ARG, "unknown model flags");
+  if (b->B.dim >= (int64_t(1) << 30))
+    return fail(LGT_ERR_UNSUPPORTED, "sector dimension must be below 2^30");
+  lgt_status st = set_device(b);
+  if (st) return st;
+  lgt_ham* h = new (std::nothrow) lgt_ham();
+  if (!h) return fail(LGT_ERR_MEMORY, "host allocation failed");
+  h->b = b;
+  h->K = K;
+  h->model = model;
+  h->g.assign(g, g + K);
+  h->t.assign(t, t + K);
+  h->m.assign(m, m + K);
+  h->seg_smem = hpsi_seg_smem_default(b->B.nmasks);
+  cudaError_t e = cudaMalloc(&h->coef_d, sizeof(double) * 4 * K);
+  if (e == cudaSuccess) e = cudaMalloc(&h->coef_f, sizeof(float) * 4 * K);
+  if (e != cudaSuccess) {
+    lgt_ham_destroy(h);
+    return cuda_fail(e, "lgt_ham_create");
+  }
+  st = upload_couplings(h);
+  if (st) {
+    lgt_ham_destroy(h);
+    return st;
+  }
+  h->cache = krylov_cache_new();
+  *out = h;
+  return LGT_OK;
+}
+
+lgt_status lgt_ham_set_couplings(lgt_ham* h, const double* g, const double* t, const double* m) {
+  if (!h || !g || !t || !m) return fail(LGT_ERR_ARG, "null argument");
+  lgt_status st = set_device(h->b);
+  if (st) return st;
+  std::vector<double> og = h->g, ot = h->t, om = h->m;
+  h->g.assign(g, g + h->K);
+  h->t.assign(t, t + h->K);
+  h->m.assign(m, m + h->K);
+  st = upload_couplings(h);
+  if (st) {
+    h->g = og;
+    h->t = ot;
+    h->m = om;
+  }
+  return st;
+}
+
+lgt_status lgt_ham_nnz(const lgt_ham* h, int64_t* nnz) {
+  if (!h || !nnz) return fail(LGT_ERR_ARG, "null argument");
+  lgt_status st = set_device(h->b);
+  if (st) return st;
+  const int64_t N = h->b->B.dim;
+  cudaStream_t s = h->b->B.stream;
+  int64_t* d = nullptr;
+  CUDA_OR_FAIL(cudaMallocAsync(&d, sizeof(int64_t) * (N + 1), s));
+  CUDA_OR_FAIL(launch_row_nnz(h->b->B.G, h->b->B.view(), h->model, d, s));
+  std::vector<int64_t> c(N);
+  if (N) CUDA_OR_FAIL(cudaMemcpyAsync(c.data(), d, sizeof(int64_t) * N, cudaMemcpyDeviceToHost, s));
+  CUDA_OR_FAIL(cudaFreeAsync(d, s));
+  CUDA_OR_FAIL(cudaStreamSynchronize(s));
+  int64_t tot = 0;
+  for (int64_t v : c) tot += v;
+  *nnz = tot;
+  return LGT_OK;
+}
+
+lgt_status lgt_ham_export_csr(const lgt_ham* h, int32_t k, int64_t* rowptr, int32_t* colidx,
+                              double* values) {
+  if (!h || !rowptr || !colidx || !values) return fail(LGT_ERR_ARG, "null argument");
+  if (k < 0 || k >= h->K) return fail(LGT_ERR_ARG, "point index out of range");
+  lgt_status st = set_device(h->b);
+  if (st) return st;
+  const int64_t N = h->b->B.dim;
+  cudaStream_t s = h->b->B.stream;
+  int64_t* dcnt = nullptr;
+  CUDA_OR_FAIL(cudaMallocAsync(&dcnt, sizeof(int64_t) * (N + 1), s));
+  CUDA_OR_FAIL(launch_row_nnz(h->b->B.G, h->b->B.view(), h->model, dcnt, s));
+  std::vector<int64_t> c(N + 1, 0);
+  if (N) CUDA_OR_FAIL(cudaMemcpyAsync(c.data(), dcnt, sizeof(int64_t) * N, cudaMemcpyDeviceToHost, s));
+  CUDA_OR_FAIL(cudaStreamSynchronize(s));
+  rowptr[0] = 0;
+  for (int64_t i = 0; i < N; ++i) rowptr[i + 1] = rowptr[i] + c[i];
+  const int64_t nnz = rowptr[N];
+  int32_t* dcol = nullptr;
+  double* dval = nullptr;
+  CUDA_OR_FAIL(cudaMemcpyAsync(dcnt, rowptr, sizeof(int64_t) * (N + 1), cudaMemcpyHostToDevice, s));
+  CUDA_OR_FAIL(cudaMallocAsync(&dcol, sizeof(int32_t) * (nnz + 1), s));
+  CUDA_OR_FAIL(cudaMallocAsync(&dval, sizeof(double) * (nnz + 1), s));
+  CUDA_OR_FAIL(launch_row_fill(h->b->B.G, h->b->B.view(), h->model, dcnt, h->g[k], h->t[k],
+                               h->m[k], dcol, dval, h->b->B.err, s));
+  if (nnz) {
+    CUDA_OR_FAIL(cudaMemcpyAsync(colidx, dcol, sizeof(int32_t) * nnz, cudaMemcpyDeviceToHost, s));
+    CUDA_OR_FAIL(cudaMemcpyAsync(values, dval, sizeof(double) * nnz, cudaMemcpyDeviceToHost, s));
+  }
+  CUDA_OR_FAIL(cudaFreeAsync(dcnt, s));
+  CUDA_OR_FAIL(cudaFreeAsync(dcol, s));
+  CUDA_OR_FAIL(cudaFreeAsync(dval, s));
+  CUDA_OR_FAIL(cudaStreamSynchronize(s));
+  return check_device_errors(h->b);
+}
+
+lgt_status lgt_matvec(const lgt_ham* hc, const void* x, void* y, int32_t ncomp, int32_t precision,
+                      uint32_t flags) {
+  lgt_ham* h = const_cast<lgt_ham*>(hc);
+  if (!h || !x || !y) return fail(LGT_ERR_ARG, "null argument");
+  if (ncomp != 1 && ncomp != 2) return fail(LGT_ERR_ARG, "ncomp must be 1 or 2");
+  if (precision != LGT_FP64 && precision != LGT_FP32)
+    return fail(LGT_ERR_ARG, "matvec precision must be LGT_FP64 or LGT_FP32");
+  lgt_status st = set_device(h->b);
+  if (st) return st;
+  const int64_t N = h->b->B.dim;
+  const size_t es = precision == LGT_FP64 ? 8 : 4;
+  const size_t bytes = size_t(N) * h->K * ncomp * es;
+  cudaStream_t s = h->b->B.stream;
+  const void* dx = x;
+  void* dy = y;
+  if (!on_device(flags)) {
+    CUDA_OR_FAIL(h->x.need(bytes));
+    CUDA_OR_FAIL(h->y.need(bytes));
+    CUDA_OR_FAIL(cudaMemcpyAsync(h->x.p, x, bytes, cudaMemcpyHostToDevice, s));
+    dx = h->x.p;
+    dy = h->y.p;
+  }
+  const OpDev op = h->op();
+  cudaError_t e = (precision == LGT_FP64)
+                      ? apply_h_d(op, static_cast<const double*>(dx), static_cast<double*>(dy), ncomp, s)
+                      : apply_h_f(op, static_cast<const float*>(dx), static_cast<float*>(dy), ncomp, s);
+  if (e != cudaSuccess) return cuda_fail(e, "lgt_matvec");
+  if (!on_device(flags)) CUDA_OR_FAIL(cudaMemcpyAsync(y, dy, bytes, cudaMemcpyDeviceToHost, s));
+  CUDA_OR_FAIL(cudaStreamSynchronize(s));
+  return check_device_errors(h->b);
+}
+
+static KrylovParams to_params(const lgt_krylov_opts* o, int for_exp) {
+  lgt_krylov_opts d;
+  lgt_krylov_defaults(&d, for_exp);
+  if (!o) o = &d;
+  KrylovParams p;
+  p.krylovdim = o->krylovdim > 0 ? o->krylovdim : d.krylovdim;
+  p.maxiter = o->maxiter >= 0 ? o->maxiter : d.maxiter;
+  p.tol = o->tol > 0 ? o->tol : d.tol;
+  p.mixed = (o->precision == LGT_FP32_MIXED || o->precision == LGT_FP32) ? 1 : 0;
+  p.reorth = o->reorth_passes > 0 ? o->reorth_passes : d.reorth_passes;
+  p.check_every = o->check_every > 0 ? o->check_every : d.check_every;
+  p.refine = o->refine_steps > 0 ? o->refine_steps : 0;
+  p.seed = o->seed;
+  p.use_graph = o->use_graph;
+  p.start_given = o->start_given;
+  return p;
+}
+
+lgt_status lgt_ground_state(lgt_ham* h, const lgt_krylov_opts* opts, double* E0, void* psi,
+                            double* residual, uint32_t flags, lgt_info* info) {
+  if (!h || !E0) return fail(LGT_ERR_ARG, "null argument");
+  KrylovParams p = to_params(opts, 0);
+  if (p.check_every > p.krylovdim) p.check_every = p.krylovdim;
+  if (p.start_given && !psi) return fail(LGT_ERR_ARG, "start_given needs psi");
+  lgt_status st = set_device(h->b);
+  if (st) return st;
+  const int64_t N = h->b->B.dim;
+  if (N == 0) return fail(LGT_ERR_ARG, "empty basis");
+  const size_t bytes = size_t(N) * h->K * sizeof(double);
+  cudaStream_t s = h->b->B.stream;
+  double* X = nullptr;
+  if (psi && on_device(flags)) {
+    X = static_cast<double*>(psi);
+  } else {
+    CUDA_OR_FAIL(h->x.need(bytes));
+    X = static_cast<double*>(h->x.p);
+    if (p.start_given) CUDA_OR_FAIL(cudaMemcpyAsync(X, psi, bytes, cudaMemcpyHostToDevice, s));
+  }
+  std::vector<double> res(h->K);
+  KrylovReport rep;
+  std::string m = lanczos_ground_state(h->op(), p, h->cache, X, E0, res.data(), s, &rep);
+  if (residual) std::memcpy(residual, res.data(), sizeof(double) * h->K);
+  if (info) {
+    info->matvecs = rep.matvecs;
+    info->restarts = rep.restarts;
+    info->converged = rep.converged;
+    info->max_residual = rep.max_residual;
+    info->seconds = rep.seconds;
+  }
+  lgt_status rc = from_msg(m);
+  if (rc != LGT_OK && rc != LGT_ERR_NOCONV) return rc;
+  if (psi && !on_device(flags))
+    CUDA_OR_FAIL(cudaMemcpyAsync(psi, X, bytes, cudaMemcpyDeviceToHost, s));
+  CUDA_OR_FAIL(cudaStreamSynchronize(s));
+  lgt_status de = check_device_errors(h->b);
+  if (de) return de;
+  if (rc == LGT_ERR_NOCONV) return fail(LGT_ERR_NOCONV, m);
+  return LGT_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+void summarize(const Geom& G, const double* feat, double t_now, lgt_obs* o) {
+  // measure_ED's means (finite_ed.jl:387-390) plus plaquette / staggered density
+  const int ns = G.ns;
+  double nf = 0, e2 = 0, ne = 0, no = 0, st = 0, pl = 0;
+  int cnt_e = 0, cnt_o = 0;
+  for (int iy = 0; iy < G.ny; ++iy)
+    for (int ix = 0; ix < G.nx; ++ix) {
+      const int s = iy * G.nx + ix;
+      nf += feat[s];
+      e2 += feat[ns + s];
+      if ((ix + iy) % 2 == 0) {
+        ne += feat[s];
+        st += feat[s];
+        ++cnt_e;
+      } else {
+        no += feat[s];
+        st -= feat[s];
+        ++cnt_o;
+      }
+    }
+  for (int q = 0; q < G.nP; ++q) pl += feat[2 * ns + q];
+  o->t = t_now;
+  o->nf_mean = nf / ns;
+  o->nf_even = cnt_e ? ne / cnt_e : NAN;
+  o->nf_odd = cnt_o ? no / cnt_o : NAN;
+  o->E2_mean = e2 / ns;
+  o->plaq_mean = G.nP ? pl / G.nP : 0.0;
+  o->n_stag = st / ns;
+  o->norm2 = feat[2 * ns + G.nP];
+}
+
+template <typename T>
+lgt_status observe_dev(lgt_ham* h, const T* x, int ncomp, std::vector<double>* feat) {
+  const Geom& G = h->b->B.G;
+  const int nf = observe_nfeat(G);
+  int nblk;
+  int64_t rpb;
+  observe_plan(h->b->B.dim, &nblk, &rpb);
+  CUDA_OR_FAIL(h->part.need(sizeof(double) * size_t(nblk) * h->K * nf));
+  CUDA_OR_FAIL(h->out.need(sizeof(double) * size_t(h->K) * nf));
+  cudaStream_t s = h->b->B.stream;
+  cudaError_t e = launch_observe<T>(G, h->b->B.view(), x, h->K, ncomp,
+                                    static_cast<double*>(h->part.p), static_cast<double*>(h->out.p),
+                                    h->b->B.err, s);
+  if (e != cudaSuccess) return cuda_fail(e, "observe");
+  feat->resize(size_t(h->K) * nf);
+  CUDA_OR_FAIL(cudaMemcpyAsync(feat->data(), h->out.p, sizeof(double) * feat->size(),
+                               cudaMemcpyDeviceToHost, s));
+  CUDA_OR_FAIL(cudaStreamSynchronize(s));
+  return LGT_OK;
+}
+
+struct ObsRecorder : StepObserver {
+  lgt_ham* h;
+  lgt_obs* obs;
+  double dt;
+  std::string on_step(int step, const double* X) override {
+    if (!obs) return std::string();
+    std::vector<double> feat;
+    if (observe_dev<double>(h, X, 2, &feat) != LGT_OK) return std::string(lgt_last_error());
+    const int nf = observe_nfeat(h->b->B.G);
+    for (int k = 0; k < h->K; ++k)
+      summarize(h->b->B.G, feat.data() + size_t(k) * nf, step * dt, obs + size_t(step) * h->K + k);
+    return std::string();
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+lgt_status lgt_expm_steps(lgt_ham* h, const lgt_krylov_opts* opts, double dt, int32_t n_steps,
+                          void* psi, lgt_obs* obs, double* norm_drift, uint32_t flags,
+                          lgt_info* info) {
+  if (!h || !psi) return fail(LGT_ERR_ARG, "null argument");
+  if (n_steps < 0 || !std::isfinite(dt)) return fail(LGT_ERR_ARG, "bad dt or n_steps");
+  KrylovParams p = to_params(opts, 1);
+  if (p.check_every > p.krylovdim) p.check_every = p.krylovdim;
+  lgt_status st = set_device(h->b);
+  if (st) return st;
+  const int64_t N = h->b->B.dim;
+  const size_t bytes = size_t(N) * h->K * 2 * sizeof(double);
+  cudaStream_t s = h->b->B.stream;
+  double* X = nullptr;
+  if (on_device(flags)) {
+    X = static_cast<double*>(psi);
+  } else {
+    CUDA_OR_FAIL(h->y.need(bytes));
+    X = static_cast<double*>(h->y.p);
+    CUDA_OR_FAIL(cudaMemcpyAsync(X, psi, bytes, cudaMemcpyHostToDevice, s));
+  }
+  ObsRecorder rec;
+  rec.h = h;
+  rec.obs = obs;
+  rec.dt = dt;
+  KrylovReport rep;
+  std::string m = krylov_expm(h->op(), p, h->cache, dt, n_steps, X, norm_drift, obs ? &rec : nullptr,
+                              s, &rep);
+  if (info) {
+    info->matvecs = rep.matvecs;
+    info->restarts = rep.restarts;
+    info->converged = rep.converged;
+    info->max_residual = rep.max_residual;
+    info->seconds = rep.seconds;
+  }
+  lgt_status rc = from_msg(m);
+  if (rc) return rc;
+  if (!on_device(flags)) CUDA_OR_FAIL(cudaMemcpyAsync(psi, X, bytes, cudaMemcpyDeviceToHost, s));
+  CUDA_OR_FAIL(cudaStreamSynchronize(s));
+  return check_device_errors(h->b);
+}
+
+lgt_status lgt_observe(const lgt_ham* hc, const void* psi, int32_t ncomp, int32_t precision,
+                       uint32_t flags, double t_now, double* nf_grid, double* E2_grid,
+                       double* plaq_grid, lgt_obs* summary) {
+  lgt_ham* h = const_cast<lgt_ham*>(hc);
+  if (!h || !psi) return fail(LGT_ERR_ARG, "null argument");
+  if (ncomp != 1 && ncomp != 2) return fail(LGT_ERR_ARG, "ncomp must be 1 or 2");
+  if (precision != LGT_FP64 && precision != LGT_FP32)
+    return fail(LGT_ERR_ARG, "precision must be LGT_FP64 or LGT_FP32");
+  lgt_status st = set_device(h->b);
+  if (st) return st;
+  const Geom& G = h->b->B.G;
+  const int64_t N = h->b->B.dim;
+  const size_t es = precision == LGT_FP64 ? 8 : 4;
+  const size_t bytes = size_t(N) * h->K * ncomp * es;
+  cudaStream_t s = h->b->B.stream;
+  const void* dx = psi;
+  if (!on_device(flags)) {
+    CUDA_OR_FAIL(h->x.need(bytes));
+    CUDA_OR_FAIL(cudaMemcpyAsync(h->x.p, psi, bytes, cudaMemcpyHostToDevice, s));
+    dx = h->x.p;
+  }
+  std::vector<double> feat;
+  st = (precision == LGT_FP64) ? observe_dev<double>(h, static_cast<const double*>(dx), ncomp, &feat)
+                               : observe_dev<float>(h, static_cast<const float*>(dx), ncomp, &feat);
+  if (st) return st;
+  const int nf = observe_nfeat(G);
+  for (int k = 0; k < h->K; ++k) {
+    const double* f = feat.data() + size_t(k) * nf;
+    if (nf_grid) std::memcpy(nf_grid + size_t(k) * G.ns, f, sizeof(double) * G.ns);
+    if (E2_grid) std::memcpy(E2_grid + size_t(k) * G.ns, f + G.ns, sizeof(double) * G.ns);
+    if (plaq_grid && G.nP)
+      std::memcpy(plaq_grid + size_t(k) * G.nP, f + 2 * G.ns, sizeof(double) * G.nP);
+    if (summary) summarize(G, f, t_now, summary + k);
+  }
+  return check_device_errors(h->b);
+}
+
+lgt_status lgt_energy(const lgt_ham* hc, const void* psi, int32_t ncomp, uint32_t flags,
+                      double* energy) {
+  lgt_ham* h = const_cast<lgt_ham*>(hc);
+  if (!h || !psi || !energy) return fail(LGT_ERR_ARG, "null argument");
+  if (ncomp != 1 && ncomp != 2) return fail(LGT_ERR_ARG, "ncomp must be 1 or 2");
+  lgt_status st = set_device(h->b);
+  if (st) return st;
+  const int64_t N = h->b->B.dim;
+  const size_t bytes = size_t(N) * h->K * ncomp * sizeof(double);
+  cudaStream_t s = h->b->B.stream;
+  CUDA_OR_FAIL(h->y.need(bytes));
+  const double* dx = static_cast<const double*>(psi);
+  DevBuf tmp;
+  if (!on_device(flags)) {
+    CUDA_OR_FAIL(h->x.need(bytes));
+    CUDA_OR_FAIL(cudaMemcpyAsync(h->x.p, psi, bytes, cudaMemcpyHostToDevice, s));
+    dx = static_cast<const double*>(h->x.p);
+  }
+  double* dy = static_cast<double*>(h->y.p);
+  cudaError_t e = apply_h_d(h->op(), dx, dy, ncomp, s);
+  if (e != cudaSuccess) return cuda_fail(e, "lgt_energy");
+  std::vector<double> num(h->K), den(h->K);
+  std::string m = panel_dots(h->cache, dx, dy, N, h->K, ncomp, num.data(), s);
+  if (m.empty()) m = panel_dots(h->cache, dx, dx, N, h->K, ncomp, den.data(), s);
+  if (!m.empty()) return from_msg(m);
+  for (int k = 0; k < h->K; ++k) energy[k] = num[k] / den[k];
+  return check_device_errors(h->b);
+}
+
+void lgt_ham_destroy(lgt_ham* h) {
+  if (!h) return;
+  if (h->b) {
+    cudaSetDevice(h->b->device);
+    cudaStreamSynchronize(h->b->B.stream);
+  }
+  krylov_cache_free(h->cache);
+  h->x.release();
+  h->y.release();
+  h->part.release();
+  h->out.release();
+  cudaFree(h->coef_d);
+  cudaFree(h->coef_f);
+  delete h;
+}
+
+}  // extern "C"

@@ -1,0 +1,332 @@
+// hpsi.cu -- matrix-free, row-pull, atomic-free y = H x on K-interleaved
+// panels (replaces build_hamiltonian's sparse matrix, finite_ed.jl:252-322,
+// and the SparseMatrixCSC * Vector product inside KrylovKit).
+//
+// Panel layout: x[row][col], col = k * ncomp + comp, C = K * ncomp columns
+// per row, rows contiguous (C * sizeof(T) bytes).  Column k of the panel uses
+// the couplings (g_k, t_k, m_k) of coupling point k; comp is 0 (real) or
+// 0/1 (real/imaginary part).  H is real, so a complex vector is simply two
+// columns that share coefficients.
+//
+// One warp owns 32 consecutive rows and works in two phases:
+//  1. lane = row: decode the row's key, derive e_R, enumerate its moves and
+//     rank each neighbour key ONCE (shared by all C columns) into a
+//     shared-memory neighbour list (index << 2 | kind);
+//  2. lane = (row, column chunk): gather V-wide vectors (double2 / float4)
+//     of x from each neighbour row, accumulate in registers, write y once.
+// Every output element is written by exactly one thread: no atomics, and the
+// result is bitwise reproducible run to run.
+#include <cstdio>
+
+#include "lgt_hpsi.h"
+#include "lgt_moves.cuh"
+#include "lgt_rank.cuh"
+
+namespace lgt {
+
+namespace {
+
+constexpr int kWarps = 8;
+constexpr int kThreads = kWarps * 32;
+
+template <typename T, int V>
+struct Vec;
+template <>
+struct Vec<double, 1> {
+  using type = double;
+};
+template <>
+struct Vec<double, 2> {
+  using type = double2;
+};
+template <>
+struct Vec<float, 1> {
+  using type = float;
+};
+template <>
+struct Vec<float, 4> {
+  using type = float4;
+};
+
+template <typename T, int V>
+__device__ __forceinline__ void vload(const T* p, T (&r)[V]) {
+  using VT = typename Vec<T, V>::type;
+  VT v = __ldg(reinterpret_cast<const VT*>(p));
+  const T* s = reinterpret_cast<const T*>(&v);
+#pragma unroll
+  for (int e = 0; e < V; ++e) r[e] = s[e];
+}
+
+template <typename T, int V>
+__device__ __forceinline__ void vstore(T* p, const T (&r)[V]) {
+  using VT = typename Vec<T, V>::type;
+  VT v;
+  T* s = reinterpret_cast<T*>(&v);
+#pragma unroll
+  for (int e = 0; e < V; ++e) s[e] = r[e];
+  *reinterpret_cast<VT*>(p) = v;
+}
+
+struct SmemLayout {
+  int binom_off, segc_off, coef_off, nbr_off, meta_off, total;
+};
+
+template <typename T>
+__host__ __device__ inline SmemLayout smem_layout(int nmasks, int seg_smem, int K, int max_moves) {
+  SmemLayout L;
+  int o = 0;
+  L.binom_off = o;
+  o += 32 * 33 * 4;
+  L.segc_off = o;
+  if (seg_smem) o += ((nmasks + 1) * 4 + 15) / 16 * 16;
+  L.coef_off = o;
+  o += (4 * K * int(sizeof(T)) + 15) / 16 * 16;
+  L.meta_off = o;  // per row: cnt (int16), e2 (int16), stag (int16), pad
+  o += kWarps * 32 * 8;
+  L.nbr_off = o;
+  o += kWarps * 32 * max_moves * 4;
+  L.total = o;
+  return L;
+}
+
+template <typename T, int V, bool PLAQ, bool JW>
+__global__ void __launch_bounds__(kThreads) k_hpsi(HpsiArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const Geom& G = a.G;
+  const SmemLayout L = smem_layout<T>(a.R.nmasks, a.seg_smem, a.K, G.max_moves);
+  uint32_t* s_binom = reinterpret_cast<uint32_t*>(smem + L.binom_off);
+  uint32_t* s_segc = reinterpret_cast<uint32_t*>(smem + L.segc_off);
+  T* s_coef = reinterpret_cast<T*>(smem + L.coef_off);  // [4][K]: cE, cm, ch, cp
+  int16_t* s_meta = reinterpret_cast<int16_t*>(smem + L.meta_off);
+  uint32_t* s_nbr = reinterpret_cast<uint32_t*>(smem + L.nbr_off);
+
+  for (int i = threadIdx.x; i < 32 * 33; i += kThreads) s_binom[i] = a.R.binom[i];
+  if (a.seg_smem)
+    for (int i = threadIdx.x; i <= a.R.nmasks; i += kThreads) s_segc[i] = a.R.segc[i];
+  for (int i = threadIdx.x; i < a.K; i += kThreads) {
+    s_coef[i] = a.cE[i];
+    s_coef[a.K + i] = a.cm[i];
+    s_coef[2 * a.K + i] = a.ch[i];
+    s_coef[3 * a.K + i] = a.cp[i];
+  }
+  __syncthreads();
+  const uint32_t* segc = a.seg_smem ? s_segc : a.R.segc;
+
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t warp_row0 = (int64_t(blockIdx.x) * kWarps + wid) * 32;
+  if (warp_row0 >= a.N) return;
+  int16_t* meta = s_meta + (wid * 32) * 4;
+  uint32_t* nbr = s_nbr + size_t(wid * 32) * G.max_moves;
+
+  // ---- phase 1: one lane per row: moves + ranks -------------------------
+  {
+    const int64_t row = warp_row0 + lane;
+    int cnt = 0, e2 = 0, stag = 0;
+    if (row < a.N) {
+      const Config c = decode(G, __ldg(a.R.keys + row));
+      diag_parts(G, c, &e2, &stag);
+      uint32_t* my = nbr + lane * G.max_moves;
+      for_each_move<PLAQ, JW>(G, c, [&](uint64_t nkey, uint32_t kind) {
+        const int64_t j = rank_key(a.R, segc, s_binom, nkey);
+        if (j < 0) {
+          raise_err(a.err, kDevErrRank);
+          return;
+        }
+        if (cnt < G.max_moves) my[cnt++] = (uint32_t(j) << 2) | kind;
+      });
+    }
+    meta[lane * 4 + 0] = int16_t(cnt);
+    meta[lane * 4 + 1] = int16_t(e2);
+    meta[lane * 4 + 2] = int16_t(stag);
+  }
+  __syncwarp();
+
+  // ---- phase 2: lanes over (row, column chunk) ---------------------------
+  const int C = a.C;
+  const int chunks = C / V;
+  const int items = 32 * chunks;
+  const T* __restrict__ x = a.xsel ? a.x + size_t(*a.xsel) * a.xstride : a.x;
+  T* __restrict__ y = a.y;
+  const int ncomp = a.ncomp;
+  for (int it = lane; it < items; it += 32) {
+    const int rl = it / chunks;
+    const int ch = it - rl * chunks;
+    const int64_t row = warp_row0 + rl;
+    if (row >= a.N) continue;
+    const int col0 = ch * V;
+    const int cnt = meta[rl * 4 + 0];
+    const T e2 = T(meta[rl * 4 + 1]);
+    const T stag = T(meta[rl * 4 + 2]);
+    T cd[V], chp[V], cpl[V], acc[V], xv[V];
+#pragma unroll
+    for (int e = 0; e < V; ++e) {
+      const int k = (col0 + e) / ncomp;
+      cd[e] = s_coef[k] * e2 + s_coef[a.K + k] * stag;  // (g^2/2) sum e^2 + m sum stag n_f
+      chp[e] = s_coef[2 * a.K + k];                     // -t
+      cpl[e] = s_coef[3 * a.K + k];                     // -1/(2 g^2)
+    }
+    vload<T, V>(x + size_t(row) * C + col0, xv);
+#pragma unroll
+    for (int e = 0; e < V; ++e) acc[e] = cd[e] * xv[e];
+    const uint32_t* lst = nbr + rl * G.max_moves;
+    for (int n = 0; n < cnt; ++n) {
+      const uint32_t ent = lst[n];
+      const size_t j = ent >> 2;
+      const uint32_t kind = ent & 3u;
+      vload<T, V>(x + j * C + col0, xv);
+#pragma unroll
+      for (int e = 0; e < V; ++e) {
+        const T cf = (kind == kPlaq) ? cpl[e] : ((kind == kHopNeg) ? -chp[e] : chp[e]);
+        acc[e] = fma(cf, xv[e], acc[e]);
+      }
+    }
+    vstore<T, V>(y + size_t(row) * C + col0, acc);
+  }
+}
+
+template <typename T, int V, bool PLAQ, bool JW>
+cudaError_t launch_t(const HpsiArgs<T>& a, cudaStream_t s) {
+  const SmemLayout L = smem_layout<T>(a.R.nmasks, a.seg_smem, a.K, a.G.max_moves);
+  auto kern = k_hpsi<T, V, PLAQ, JW>;
+  // raise the dynamic shared-memory limit once per kernel (outside any graph
+  // capture: the first launch of a configuration is always eager)
+  static int attr_bytes = 48 * 1024;
+  if (L.total > attr_bytes) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total);
+    if (e != cudaSuccess) return e;
+    attr_bytes = L.total;
+  }
+  const int64_t blocks = (a.N + kThreads - 1) / kThreads;
+  if (blocks <= 0) return cudaSuccess;
+  kern<<<unsigned(blocks), kThreads, L.total, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename T, int V>
+cudaError_t launch_v(const HpsiArgs<T>& a, uint32_t model, cudaStream_t s) {
+  const bool plaq = model & kModelPlaq, jw = model & kModelJW;
+  if (plaq && jw) return launch_t<T, V, true, true>(a, s);
+  if (plaq) return launch_t<T, V, true, false>(a, s);
+  if (jw) return launch_t<T, V, false, true>(a, s);
+  return launch_t<T, V, false, false>(a, s);
+}
+
+}  // namespace
+
+int hpsi_seg_smem_default(int nmasks) { return (nmasks + 1) * 4 <= 16 * 1024 ? 1 : 0; }
+
+template <typename T>
+cudaError_t launch_hpsi(HpsiArgs<T> a, uint32_t model, cudaStream_t s) {
+  constexpr int VW = 16 / int(sizeof(T));
+  const bool vec_ok = (a.C % VW == 0) && ((reinterpret_cast<uintptr_t>(a.x) & 15) == 0) &&
+                      ((reinterpret_cast<uintptr_t>(a.y) & 15) == 0);
+  if (vec_ok) return launch_v<T, VW>(a, model, s);
+  return launch_v<T, 1>(a, model, s);
+}
+
+template cudaError_t launch_hpsi<double>(HpsiArgs<double>, uint32_t, cudaStream_t);
+template cudaError_t launch_hpsi<float>(HpsiArgs<float>, uint32_t, cudaStream_t);
+
+// ----------------------------------------------------------------------------
+// CSR export (parity checks and the reference's nnz(H), finite_ed.jl:355)
+// ----------------------------------------------------------------------------
+namespace {
+
+template <bool PLAQ, bool JW>
+__global__ void k_row_nnz(Geom G, RankView R, int64_t N, int64_t* counts) {
+  int64_t row = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (row >= N) return;
+  const Config c = decode(G, R.keys[row]);
+  int64_t n = 1;  // the diagonal is always stored (finite_ed.jl:276)
+  for_each_move<PLAQ, JW>(G, c, [&](uint64_t, uint32_t) { ++n; });
+  counts[row] = n;
+}
+
+// Diagonal in the reference's own summation order (finite_ed.jl:265-276), so
+// exported values are bitwise those of build_hamiltonian.
+__device__ double ref_diag(const Geom& G, const Config& c, double g, double m) {
+  double E = 0.0;
+  const double cE = __dmul_rn(g, g) / 2.0;
+  for (int iy = 0; iy < G.ny; ++iy)
+    for (int ix = 0; ix < G.nx; ++ix) {
+      if (ix < G.nx - 1) {
+        double e = double(get_eR(G, c.rpack, iy * (G.nx - 1) + ix));
+        E = __dadd_rn(E, __dmul_rn(cE, __dmul_rn(e, e)));
+      }
+      if (iy < G.ny - 1) {
+        double e = double(get_eU(G, c.digits, iy * G.nx + ix));
+        E = __dadd_rn(E, __dmul_rn(cE, __dmul_rn(e, e)));
+      }
+      const double stag = ((ix + iy) % 2 == 0) ? 1.0 : -1.0;
+      E = __dadd_rn(E, __dmul_rn(__dmul_rn(m, stag), double((c.mask >> (iy * G.nx + ix)) & 1u)));
+    }
+  return E;
+}
+
+template <bool PLAQ, bool JW>
+__global__ void k_row_fill(Geom G, RankView R, int64_t N, const int64_t* rowptr, double g,
+                           double t, double m, int32_t* cols, double* vals, int* err) {
+  int64_t row = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (row >= N) return;
+  const Config c = decode(G, R.keys[row]);
+  int64_t p = rowptr[row];
+  const int64_t end = rowptr[row + 1];
+  const double invg2 = 1.0 / (2.0 * __dmul_rn(g, g));
+  // insertion into a column-sorted row
+  auto put = [&](int64_t col, double v) {
+    int64_t q = p;
+    while (q > rowptr[row] && cols[q - 1] > col) {
+      cols[q] = cols[q - 1];
+      vals[q] = vals[q - 1];
+      --q;
+    }
+    cols[q] = int32_t(col);
+    vals[q] = v;
+    ++p;
+  };
+  put(row, ref_diag(G, c, g, m));
+  for_each_move<PLAQ, JW>(G, c, [&](uint64_t nkey, uint32_t kind) {
+    const int64_t j = rank_key(R, R.segc, R.binom, nkey);
+    if (j < 0 || p >= end) {
+      raise_err(err, j < 0 ? kDevErrRank : kDevErrBounds);
+      return;
+    }
+    const double v = (kind == kPlaq) ? -invg2 : ((kind == kHopNeg) ? t : -t);
+    put(j, v);
+  });
+}
+
+}  // namespace
+
+cudaError_t launch_row_nnz(const Geom& G, const RankView& R, uint32_t model, int64_t* counts,
+                           cudaStream_t s) {
+  const int64_t N = R.dim;
+  if (N == 0) return cudaSuccess;
+  const unsigned blocks = unsigned((N + 255) / 256);
+  const bool plaq = model & kModelPlaq, jw = model & kModelJW;
+  if (plaq && jw) k_row_nnz<true, true><<<blocks, 256, 0, s>>>(G, R, N, counts);
+  else if (plaq) k_row_nnz<true, false><<<blocks, 256, 0, s>>>(G, R, N, counts);
+  else if (jw) k_row_nnz<false, true><<<blocks, 256, 0, s>>>(G, R, N, counts);
+  else k_row_nnz<false, false><<<blocks, 256, 0, s>>>(G, R, N, counts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_row_fill(const Geom& G, const RankView& R, uint32_t model,
+                            const int64_t* rowptr, double g, double t, double m, int32_t* cols,
+                            double* vals, int* err, cudaStream_t s) {
+  const int64_t N = R.dim;
+  if (N == 0) return cudaSuccess;
+  const unsigned blocks = unsigned((N + 255) / 256);
+  const bool plaq = model & kModelPlaq, jw = model & kModelJW;
+  if (plaq && jw)
+    k_row_fill<true, true><<<blocks, 256, 0, s>>>(G, R, N, rowptr, g, t, m, cols, vals, err);
+  else if (plaq)
+    k_row_fill<true, false><<<blocks, 256, 0, s>>>(G, R, N, rowptr, g, t, m, cols, vals, err);
+  else if (jw)
+    k_row_fill<false, true><<<blocks, 256, 0, s>>>(G, R, N, rowptr, g, t, m, cols, vals, err);
+  else
+    k_row_fill<false, false><<<blocks, 256, 0, s>>>(G, R, N, rowptr, g, t, m, cols, vals, err);
+  return cudaGetLastError();
+}
+
+}  // namespace lgt

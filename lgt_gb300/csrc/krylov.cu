@@ -1,0 +1,1164 @@
+// krylov.cu -- batched Lanczos ground states and Krylov exp(-iHt) steps on the
+// GPU (replaces KrylovKit.eigsolve in find_ground_state, finite_ed.jl:333-341,
+// and KrylovKit.exponentiate in evolve_ED!, finite_ed.jl:405-431).
+//
+// K independent coupling points advance in lockstep on K-interleaved panels;
+// each point has its own tridiagonal matrix, convergence state and restart.
+// A Lanczos step is
+//     W = H V_j                          (hpsi, storage precision)
+//     repeat reorth times:               (classical Gram-Schmidt against the
+//        h = V_{0..j}^H W                 whole basis, FP64 accumulation)
+//        W -= V_{0..j} h,  alpha_j += Re h_j
+//     beta_j = ||W||,  V_{j+1} = W / beta_j
+// Every reduction is two-stage (per-block partials, then a fixed-order sum),
+// so results are bitwise reproducible.  All kernels read the step index j
+// from device memory, so the step sequence is captured once as a CUDA graph
+// and replayed.  The tridiagonal problems are solved on the device: lowest
+// eigenpair by Sturm bisection + inverse iteration (ground state), full
+// eigendecomposition by implicit QL (exponential).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "lgt_krylov.h"
+
+namespace lgt {
+
+namespace {
+
+constexpr int kT = 256;   // threads of the panel kernels
+constexpr int kIC = 8;    // Krylov vectors per multidot pass
+constexpr int kMaxDim = 64;
+
+#define KCK(call)                                                                  \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess) return std::string(#call ": ") + cudaGetErrorString(e_); \
+  } while (0)
+
+// status codes per point
+enum : int { kActive = 0, kExhausted = 1, kConverged = 2, kWritten = 3 };
+
+__device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+// Standard normal samples from a counter-based hash (Box-Muller).  Point k
+// of seed s draws the same vector whatever K is.
+template <typename S>
+__global__ void k_randn(S* out, int64_t N, int C, int ncomp, uint64_t seed) {
+  const int64_t n = N * C;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t row = i / C;
+    const int c = int(i - row * C);
+    const int k = c / ncomp, comp = c - k * ncomp;
+    uint64_t h = splitmix64(splitmix64(seed) ^ splitmix64(uint64_t(k) + 0x5851F42D4C957F2Dull));
+    h = splitmix64(h ^ (uint64_t(row) * uint64_t(ncomp) + uint64_t(comp)));
+    const uint64_t h2 = splitmix64(h);
+    const double u1 = (double((h >> 11) + 1)) * 0x1.0p-53;  // (0, 1]
+    const double u2 = double(h2 >> 11) * 0x1.0p-53;
+    out[i] = S(sqrt(-2.0 * log(u1)) * cospi(2.0 * u2));
+  }
+}
+
+// Per-block partial dot products of W against V_0..V_{J-1}:
+// part[blk][i][0][c] = sum_rows V_i[row][c] W[row][c]
+// part[blk][i][1][c] = sum_rows V_i[row][c] W[row][c^1]   (complex only)
+template <typename S, int NC>
+__global__ void __launch_bounds__(kT) k_multidot(const S* __restrict__ V, size_t vstride,
+                                                 const int* jstate, int jfixed,
+                                                 const S* __restrict__ W, int64_t N, int C,
+                                                 int64_t rpb, double* part, int Jmax) {
+  extern __shared__ double red[];  // [RG][kIC][2][C]
+  const int J = jstate ? (*jstate + 1) : jfixed;
+  const int RG = kT / C;
+  const int c = threadIdx.x % C, rg = threadIdx.x / C;
+  const bool act = rg < RG;
+  const int64_t r0 = int64_t(blockIdx.x) * rpb;
+  const int64_t r1 = (r0 + rpb < N) ? r0 + rpb : N;
+  for (int i0 = 0; i0 < J; i0 += kIC) {
+    double a[kIC], b[kIC];
+#pragma unroll
+    for (int q = 0; q < kIC; ++q) a[q] = b[q] = 0.0;
+    if (act) {
+      for (int64_t row = r0 + rg; row < r1; row += RG) {
+        const size_t off = size_t(row) * C;
+        const double w = double(W[off + c]);
+        const double wx = (NC == 2) ? double(W[off + (c ^ 1)]) : 0.0;
+#pragma unroll
+        for (int q = 0; q < kIC; ++q) {
+          if (i0 + q < J) {
+            const double v = double(V[size_t(i0 + q) * vstride + off + c]);
+            a[q] = fma(v, w, a[q]);
+            if (NC == 2) b[q] = fma(v, wx, b[q]);
+          }
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < kIC; ++q) {
+        red[((rg * kIC + q) * 2 + 0) * C + c] = a[q];
+        red[((rg * kIC + q) * 2 + 1) * C + c] = b[q];
+      }
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < kIC * 2 * C; q += kT) {
+      double s = 0.0;
+      for (int g = 0; g < RG; ++g) s += red[g * kIC * 2 * C + q];
+      const int ii = q / (2 * C);
+      if (i0 + ii < J) part[(size_t(blockIdx.x) * Jmax + i0) * 2 * C + q] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// h[i][k] = <V_i, W>_k (complex for NC = 2), summed over blocks in order.
+// alpha_j of active points accumulates Re h_j (first pass sets it).
+__global__ void k_finish_dots(const double* part, int nblk, int Jmax, const int* jstate,
+                              int jfixed, int K, int C, int ncomp, double* h, double* alpha,
+                              int ldT, int first_pass, const int* status) {
+  const int J = jstate ? (*jstate + 1) : jfixed;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= J * K) return;
+  const int i = t / K, k = t - i * K;
+  double re = 0.0, im = 0.0;
+  for (int b = 0; b < nblk; ++b) {
+    const double* p = part + (size_t(b) * Jmax + i) * 2 * C;
+    if (ncomp == 1) {
+      re += p[k];
+    } else {
+      re += p[2 * k] + p[2 * k + 1];
+      im += p[C + 2 * k] - p[C + 2 * k + 1];
+    }
+  }
+  h[(size_t(i) * K + k) * 2 + 0] = re;
+  h[(size_t(i) * K + k) * 2 + 1] = im;
+  if (alpha && i == J - 1 && status[k] == kActive) {
+    double* a = alpha + size_t(k) * ldT + (J - 1);
+    *a = first_pass ? re : (*a + re);
+  }
+}
+
+// W -= sum_{i<J} h_i V_i (complex product for NC = 2) for active points, and
+// per-block partial sums of |W|^2 per column.
+template <typename S, int NC>
+__global__ void __launch_bounds__(kT) k_update(const S* __restrict__ V, size_t vstride,
+                                               const int* jstate, int jfixed, S* W, int64_t N,
+                                               int C, int ncomp, const double* h, int K,
+                                               const int* status, int64_t rpb, double* npart) {
+  __shared__ double red[kT];
+  const int J = jstate ? (*jstate + 1) : jfixed;
+  const int RG = kT / C;
+  const int c = threadIdx.x % C, rg = threadIdx.x / C;
+  const int k = c / ncomp;
+  const bool act = rg < RG && (!status || status[k] == kActive);
+  const int64_t r0 = int64_t(blockIdx.x) * rpb;
+  const int64_t r1 = (r0 + rpb < N) ? r0 + rpb : N;
+  double nrm = 0.0;
+  if (act) {
+    for (int64_t row = r0 + rg; row < r1; row += RG) {
+      const size_t off = size_t(row) * C;
+      double w = double(W[off + c]);
+      for (int i = 0; i < J; ++i) {
+        const double hr = h[(size_t(i) * K + k) * 2 + 0];
+        const double v = double(V[size_t(i) * vstride + off + c]);
+        if (NC == 1) {
+          w = fma(-hr, v, w);
+        } else {
+          const double hi = h[(size_t(i) * K + k) * 2 + 1];
+          const double vp = double(V[size_t(i) * vstride + off + (c ^ 1)]);
+          // (hr + i hi)(v_re + i v_im): re = hr v_re - hi v_im, im = hr v_im + hi v_re
+          w = (c & 1) ? (w - (hr * v + hi * vp)) : (w - (hr * v - hi * vp));
+        }
+      }
+      if (J > 0) W[off + c] = S(w);
+      const double ws = double(S(w));
+      nrm = fma(ws, ws, nrm);
+    }
+  }
+  red[threadIdx.x] = (rg < RG) ? nrm : 0.0;
+  __syncthreads();
+  if (threadIdx.x < C) {
+    double s = 0.0;
+    for (int g = 0; g < RG; ++g) s += red[g * C + threadIdx.x];
+    npart[size_t(blockIdx.x) * C + threadIdx.x] = s;
+  }
+}
+
+// beta_j = ||W|| per point.  A Krylov space that has become invariant
+// (beta below the relative threshold) marks the point exhausted: its Ritz
+// pair on the current basis is exact.
+__global__ void k_finish_norm(const double* npart, int nblk, int K, int C, int ncomp,
+                              const int* jstate, double* beta, const double* alpha, int ldT,
+                              int* status, int* len, double* bnorm, double tiny_rel, int write_beta) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K) return;
+  double s = 0.0;
+  for (int b = 0; b < nblk; ++b)
+    for (int q = 0; q < ncomp; ++q) s += npart[size_t(b) * C + k * ncomp + q];
+  const double nb = sqrt(s);
+  bnorm[k] = nb;
+  if (!write_beta || status[k] != kActive) return;
+  const int j = *jstate;
+  beta[size_t(k) * ldT + j] = nb;
+  len[k] = j + 1;
+  double scale = fabs(alpha[size_t(k) * ldT + j]);
+  if (j > 0) scale = fmax(scale, beta[size_t(k) * ldT + j - 1]);
+  scale = fmax(scale, 1.0);
+  if (!(nb > tiny_rel * scale)) status[k] = kExhausted;
+}
+
+// dst = src / bnorm per column for points with status == sel.  dst is panel
+// (*jstate + dst_off) of `dstbase` when jstate is given.
+template <typename SI, typename SO>
+__global__ void k_scale(const SI* src, SO* dstbase, size_t vstride, const int* jstate, int dst_off,
+                        int64_t N, int C, int ncomp, const double* bnorm, const int* status,
+                        int sel) {
+  SO* dst = dstbase + size_t((jstate ? *jstate : 0) + dst_off) * vstride;
+  const int64_t n = N * C;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const int c = int(i % C);
+    const int k = c / ncomp;
+    if (status && status[k] != sel) continue;
+    const double b = bnorm[k];
+    dst[i] = SO(b > 0.0 ? double(src[i]) / b : 0.0);
+  }
+}
+
+__global__ void k_advance(int* jstate) { jstate[0] += 1; }
+
+__global__ void k_set_int(int* p, int n, int v, const int* status, int only_status) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && (!status || status[i] == only_status)) p[i] = v;
+}
+
+// ---- tridiagonal solvers -----------------------------------------------------
+
+// Number of eigenvalues of T (diag a, off-diag b) below x (Sturm sequence).
+__device__ int sturm_count(const double* a, const double* b, int n, double x) {
+  int cnt = 0;
+  double q = 1.0;
+  for (int i = 0; i < n; ++i) {
+    const double bb = (i > 0) ? b[i - 1] * b[i - 1] : 0.0;
+    q = (a[i] - x) - ((i > 0) ? bb / q : 0.0);
+    if (q == 0.0) q = -1e-300;
+    if (q < 0.0) ++cnt;
+  }
+  return cnt;
+}
+
+// Lowest eigenpair of the n x n tridiagonal T: bisection on the Sturm count,
+// then inverse iteration on the positive-definite T - (theta - delta) I
+// (LDL^T without pivoting is stable there).  z normalised, z[0] >= 0.
+__device__ double lowest_eigpair(const double* a, const double* b, int n, double* z,
+                                 double* work) {
+  double lo = a[0], hi = a[0];
+  for (int i = 0; i < n; ++i) {
+    const double r = ((i > 0) ? fabs(b[i - 1]) : 0.0) + ((i < n - 1) ? fabs(b[i]) : 0.0);
+    lo = fmin(lo, a[i] - r);
+    hi = fmax(hi, a[i] + r);
+  }
+  const double scale = fmax(fmax(fabs(lo), fabs(hi)), 1e-300);
+  for (int it = 0; it < 200; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (mid <= lo || mid >= hi) break;
+    if (sturm_count(a, b, n, mid) >= 1) hi = mid; else lo = mid;
+    if (hi - lo <= 2.2e-16 * scale) break;
+  }
+  const double theta = 0.5 * (lo + hi);
+  const double shift = theta - 4.0 * 2.2e-16 * scale;
+  for (int i = 0; i < n; ++i) z[i] = 1.0;
+  for (int rep = 0; rep < 3; ++rep) {
+    // LDL^T of T - shift I: d (work), l (work + n)
+    double* d = work;
+    double* l = work + kMaxDim;
+    d[0] = a[0] - shift;
+    if (d[0] <= 0.0) d[0] = 1e-300;
+    for (int i = 1; i < n; ++i) {
+      l[i - 1] = b[i - 1] / d[i - 1];
+      d[i] = (a[i] - shift) - l[i - 1] * b[i - 1];
+      if (d[i] <= 0.0) d[i] = 1e-300;
+    }
+    // solve L y = z, D w = y, L^T x = w
+    for (int i = 1; i < n; ++i) z[i] -= l[i - 1] * z[i - 1];
+    for (int i = 0; i < n; ++i) z[i] /= d[i];
+    for (int i = n - 2; i >= 0; --i) z[i] -= l[i] * z[i + 1];
+    double nn = 0.0, mx = 0.0;
+    for (int i = 0; i < n; ++i) mx = fmax(mx, fabs(z[i]));
+    for (int i = 0; i < n; ++i) {
+      z[i] /= mx;
+      nn += z[i] * z[i];
+    }
+    nn = sqrt(nn);
+    for (int i = 0; i < n; ++i) z[i] /= nn;
+  }
+  if (z[0] < 0.0)
+    for (int i = 0; i < n; ++i) z[i] = -z[i];
+  return theta;
+}
+
+// Ground-state convergence check, one block (thread 0) per point:
+// Ritz value theta, residual beta_{n-1} |z_{n-1}|, coefficients z.
+__global__ void k_check_lowest(const double* alpha, const double* beta, int ldT, int* status,
+                               const int* len, double* theta, double* resid, double* coef,
+                               double tol) {
+  const int k = blockIdx.x;
+  if (threadIdx.x != 0) return;
+  const int st = status[k];
+  if (st >= kConverged) return;
+  const int n = len[k];
+  double z[kMaxDim], work[2 * kMaxDim];
+  if (n <= 0) return;
+  const double th = lowest_eigpair(alpha + size_t(k) * ldT, beta + size_t(k) * ldT, n, z, work);
+  const double r = fabs(beta[size_t(k) * ldT + n - 1] * z[n - 1]);
+  theta[k] = th;
+  resid[k] = (st == kExhausted) ? 0.0 : r;
+  for (int i = 0; i < ldT; ++i) {
+    coef[(size_t(k) * ldT + i) * 2 + 0] = (i < n) ? z[i] : 0.0;
+    coef[(size_t(k) * ldT + i) * 2 + 1] = 0.0;
+  }
+  if (st == kExhausted || r <= tol) status[k] = kConverged;
+}
+
+// Implicit QL with eigenvectors (symmetric tridiagonal, Wilkinson-type
+// shift), one block per point, thread r owning row r of Z.  Thread 0 runs
+// the scalar chase and records the plane rotations; all threads then apply
+// them to their own row, so no row depends on another.
+__device__ bool ql_eigen(double* d, double* e, double* Z, int n, int ldz, double* rc, double* rs,
+                         int* nrot_out) {
+  const int r = threadIdx.x;
+  for (int i = r; i < n; i += blockDim.x)
+    for (int j = 0; j < n; ++j) Z[i * ldz + j] = (i == j) ? 1.0 : 0.0;
+  __shared__ int s_l, s_m, s_nrot, s_done, s_fail;
+  if (r == 0) {
+    e[n - 1] = 0.0;
+    s_l = 0;
+    s_fail = 0;
+  }
+  __syncthreads();
+  int iters = 0;
+  while (true) {
+    if (r == 0) {
+      s_done = 0;
+      s_nrot = 0;
+      int l = s_l;
+      // advance l past converged eigenvalues
+      while (l < n) {
+        int m = l;
+        for (; m < n - 1; ++m) {
+          const double dd = fabs(d[m]) + fabs(d[m + 1]);
+          if (fabs(e[m]) <= 2.2e-16 * dd) break;
+        }
+        if (m == l) {
+          ++l;
+          iters = 0;
+          continue;
+        }
+        s_m = m;
+        break;
+      }
+      s_l = l;
+      if (l >= n) {
+        s_done = 1;
+      } else if (++iters > 100) {
+        s_fail = 1;
+        s_done = 1;
+      } else {
+        const int m = s_m;
+        double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+        double rr = hypot(g, 1.0);
+        g = d[m] - d[l] + e[l] / (g + copysign(rr, g));
+        double s = 1.0, c = 1.0, p = 0.0;
+        int nrot = 0;
+        bool early = false;
+        for (int i = m - 1; i >= l; --i) {
+          double f = s * e[i];
+          const double b = c * e[i];
+          rr = hypot(f, g);
+          e[i + 1] = rr;
+          if (rr == 0.0) {
+            d[i + 1] -= p;
+            e[m] = 0.0;
+            early = true;
+            break;
+          }
+          s = f / rr;
+          c = g / rr;
+          g = d[i + 1] - p;
+          rr = (d[i] - g) * s + 2.0 * c * b;
+          p = s * rr;
+          d[i + 1] = g + p;
+          g = c * rr - b;
+          rc[nrot] = c;
+          rs[nrot] = s;
+          ++nrot;
+        }
+        if (!early) {
+          d[l] -= p;
+          e[l] = g;
+          e[m] = 0.0;
+        }
+        s_nrot = nrot;
+      }
+    }
+    __syncthreads();
+    if (s_done) break;
+    const int m = s_m, nrot = s_nrot;
+    for (int row = r; row < n; row += blockDim.x) {
+      double* zr = Z + row * ldz;
+      for (int q = 0; q < nrot; ++q) {
+        const int i = m - 1 - q;
+        const double f = zr[i + 1];
+        zr[i + 1] = rs[q] * zr[i] + rc[q] * f;
+        zr[i] = rc[q] * zr[i] - rs[q] * f;
+      }
+    }
+    __syncthreads();
+  }
+  if (nrot_out) *nrot_out = 0;
+  return s_fail == 0;
+}
+
+// Krylov exponential check, one block per point: c = rho exp(-i tau T) e_0
+// from the eigendecomposition of T_n, error estimate rho beta_{n-1} |c_{n-1}|.
+// force: store the coefficients and mark converged regardless of the error.
+__global__ void k_check_expm(const double* alpha, const double* beta, int ldT, int* status,
+                             const int* len, const double* rho, double tau, double* err_out,
+                             double* coef, double tol, int force, int* fail) {
+  __shared__ double d[kMaxDim], e[kMaxDim], Z[kMaxDim * kMaxDim], rc[kMaxDim], rs[kMaxDim];
+  __shared__ double cre[kMaxDim], cim[kMaxDim];
+  const int k = blockIdx.x;
+  const int st = status[k];
+  if (st >= kConverged) return;
+  const int n = len[k];
+  if (n <= 0) return;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    d[i] = alpha[size_t(k) * ldT + i];
+    e[i] = (i < n - 1) ? beta[size_t(k) * ldT + i] : 0.0;
+  }
+  __syncthreads();
+  const bool ok = ql_eigen(d, e, Z, n, kMaxDim, rc, rs, nullptr);
+  if (!ok && threadIdx.x == 0) atomicOr(fail, 1);
+  __syncthreads();
+  // c_i = rho * sum_l Z[i][l] exp(-i tau lambda_l) Z[0][l]
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double sr = 0.0, si = 0.0;
+    for (int l = 0; l < n; ++l) {
+      double sn, cs;
+      sincos(-tau * d[l], &sn, &cs);
+      const double w = Z[i * kMaxDim + l] * Z[l];
+      sr = fma(w, cs, sr);
+      si = fma(w, sn, si);
+    }
+    cre[i] = rho[k] * sr;
+    cim[i] = rho[k] * si;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double bl = beta[size_t(k) * ldT + n - 1];
+    const double err = (st == kExhausted) ? 0.0 : fabs(bl) * hypot(cre[n - 1], cim[n - 1]);
+    err_out[k] = err;
+    if (force || st == kExhausted || err <= tol) {
+      for (int i = 0; i < ldT; ++i) {
+        coef[(size_t(k) * ldT + i) * 2 + 0] = (i < n) ? cre[i] : 0.0;
+        coef[(size_t(k) * ldT + i) * 2 + 1] = (i < n) ? cim[i] : 0.0;
+      }
+      status[k] = kConverged;
+    }
+  }
+}
+
+// out = sum_{i < len[k]} coef[k][i] V_i for points with status == sel
+// (complex coefficients for NC = 2).
+template <typename S, int NC>
+__global__ void k_combine(const S* __restrict__ V, size_t vstride, const double* coef, int ldT,
+                          const int* len, const int* status, int sel, double* out, int64_t N,
+                          int C, int ncomp) {
+  const int64_t n = N * C;
+  for (int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; idx < n;
+       idx += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t row = idx / C;
+    const int c = int(idx - row * C);
+    const int k = c / ncomp;
+    if (status[k] != sel) continue;
+    const int nk = len[k];
+    const size_t off = size_t(row) * C;
+    double acc = 0.0;
+    for (int i = 0; i < nk; ++i) {
+      const double cr = coef[(size_t(k) * ldT + i) * 2 + 0];
+      const double v = double(V[size_t(i) * vstride + off + c]);
+      if (NC == 1) {
+        acc = fma(cr, v, acc);
+      } else {
+        const double ci = coef[(size_t(k) * ldT + i) * 2 + 1];
+        const double vp = double(V[size_t(i) * vstride + off + (c ^ 1)]);
+        acc += (c & 1) ? (cr * v + ci * vp) : (cr * v - ci * vp);
+      }
+    }
+    out[off + c] = acc;
+  }
+}
+
+__global__ void k_residual_parts(const double* X, const double* HX, const double* E, int64_t N,
+                                 int C, int ncomp, int64_t rpb, double* npart) {
+  __shared__ double red[kT];
+  const int RG = kT / C;
+  const int c = threadIdx.x % C, rg = threadIdx.x / C;
+  const int k = c / ncomp;
+  const int64_t r0 = int64_t(blockIdx.x) * rpb;
+  const int64_t r1 = (r0 + rpb < N) ? r0 + rpb : N;
+  double nrm = 0.0;
+  if (rg < RG) {
+    for (int64_t row = r0 + rg; row < r1; row += RG) {
+      const size_t off = size_t(row) * C + c;
+      const double r = HX[off] - E[k] * X[off];
+      nrm = fma(r, r, nrm);
+    }
+  }
+  red[threadIdx.x] = (rg < RG) ? nrm : 0.0;
+  __syncthreads();
+  if (threadIdx.x < C) {
+    double s = 0.0;
+    for (int g = 0; g < RG; ++g) s += red[g * C + threadIdx.x];
+    npart[size_t(blockIdx.x) * C + threadIdx.x] = s;
+  }
+}
+
+
+
+// ---- host-side machinery -------------------------------------------------------
+
+int grid_for(int64_t n) {
+  int64_t b = (n + kT - 1) / kT;
+  if (b > 152 * 16) b = 152 * 16;
+  if (b < 1) b = 1;
+  return int(b);
+}
+
+// Row partition of the two-stage reductions: enough rows per block to keep
+// its threads busy, at most two blocks per SM.
+struct Reducer {
+  int nblk = 1;
+  int64_t rpb = 1;
+  void plan(int64_t N, int C) {
+    const int RG = kT / C;
+    int64_t want = (N * C + 4095) / 4096;
+    if (want > 304) want = 304;
+    if (want < 1) want = 1;
+    rpb = (N + want - 1) / want;
+    if (rpb < RG) rpb = RG;
+    nblk = int((N + rpb - 1) / rpb);
+    if (nblk < 1) nblk = 1;
+  }
+};
+
+// Device workspace of one driver in one storage precision, reused across
+// calls while the shape is unchanged (allocation synchronises the device).
+template <typename S>
+struct Work {
+  int64_t N = -1;
+  int C = 0, K = 0, ncomp = 1, m = 0, ldT = 0;
+  size_t vstride = 0;
+  S* V = nullptr;        // m+1 Krylov panels
+  S* W = nullptr;        // H V_j, then the new residual vector
+  double* R = nullptr;   // FP64 panel for H X and residuals
+  double* part = nullptr;
+  double* npart = nullptr;
+  double* h = nullptr;
+  double* alpha = nullptr;
+  double* beta = nullptr;
+  double* coef = nullptr;
+  double* theta = nullptr;
+  double* resid = nullptr;
+  double* bnorm = nullptr;
+  double* rho = nullptr;
+  double* zeros = nullptr;
+  int* status = nullptr;
+  int* len = nullptr;
+  int* jstate = nullptr;
+  int* fail = nullptr;
+  Reducer red;
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = 0, graph_reorth = 0;
+  double graph_tiny = 0.0;
+
+  std::string ensure(int64_t N_, int C_, int K_, int ncomp_, int m_) {
+    if (N_ == N && C_ == C && K_ == K && ncomp_ == ncomp && m_ == m && V) return std::string();
+    release();
+    N = N_;
+    C = C_;
+    K = K_;
+    ncomp = ncomp_;
+    m = m_;
+    ldT = m + 1;
+    vstride = size_t(N) * C;
+    red.plan(N, C);
+    KCK(cudaMalloc(&V, sizeof(S) * vstride * (m + 1)));
+    KCK(cudaMalloc(&W, sizeof(S) * vstride));
+    KCK(cudaMalloc(&R, sizeof(double) * vstride));
+    KCK(cudaMalloc(&part, sizeof(double) * size_t(red.nblk) * ldT * 2 * C));
+    KCK(cudaMalloc(&npart, sizeof(double) * size_t(red.nblk) * C));
+    KCK(cudaMalloc(&h, sizeof(double) * size_t(ldT) * K * 2));
+    KCK(cudaMalloc(&alpha, sizeof(double) * size_t(K) * ldT));
+    KCK(cudaMalloc(&beta, sizeof(double) * size_t(K) * ldT));
+    KCK(cudaMalloc(&coef, sizeof(double) * size_t(K) * ldT * 2));
+    KCK(cudaMalloc(&theta, sizeof(double) * K));
+    KCK(cudaMalloc(&resid, sizeof(double) * K));
+    KCK(cudaMalloc(&bnorm, sizeof(double) * K));
+    KCK(cudaMalloc(&rho, sizeof(double) * K));
+    KCK(cudaMalloc(&zeros, sizeof(double) * K));
+    KCK(cudaMemset(zeros, 0, sizeof(double) * K));
+    KCK(cudaMalloc(&status, sizeof(int) * K));
+    KCK(cudaMalloc(&len, sizeof(int) * K));
+    KCK(cudaMalloc(&jstate, sizeof(int) * 4));
+    KCK(cudaMalloc(&fail, sizeof(int)));
+    return std::string();
+  }
+  void release() {
+    if (graph) cudaGraphExecDestroy(graph);
+    graph = nullptr;
+    graph_steps = 0;
+    cudaFree(V);
+    cudaFree(W);
+    cudaFree(R);
+    cudaFree(part);
+    cudaFree(npart);
+    cudaFree(h);
+    cudaFree(alpha);
+    cudaFree(beta);
+    cudaFree(coef);
+    cudaFree(theta);
+    cudaFree(resid);
+    cudaFree(bnorm);
+    cudaFree(rho);
+    cudaFree(zeros);
+    cudaFree(status);
+    cudaFree(len);
+    cudaFree(jstate);
+    cudaFree(fail);
+    V = W = nullptr;
+    R = part = npart = h = alpha = beta = coef = theta = resid = bnorm = rho = zeros = nullptr;
+    status = len = jstate = fail = nullptr;
+    N = -1;
+  }
+};
+
+template <typename S>
+cudaError_t apply_h(const OpDev& op, const S* x, const int* xsel, size_t xstride, S* y, int ncomp,
+                    cudaStream_t s);
+
+template <>
+cudaError_t apply_h<double>(const OpDev& op, const double* x, const int* xsel, size_t xstride,
+                            double* y, int ncomp, cudaStream_t s) {
+  HpsiArgs<double> a;
+  a.G = op.G;
+  a.R = op.R;
+  a.x = x;
+  a.y = y;
+  a.N = op.R.dim;
+  a.C = op.K * ncomp;
+  a.ncomp = ncomp;
+  a.K = op.K;
+  a.cE = op.cE_d;
+  a.cm = op.cm_d;
+  a.ch = op.ch_d;
+  a.cp = op.cp_d;
+  a.err = op.err;
+  a.seg_smem = op.seg_smem;
+  a.xsel = xsel;
+  a.xstride = xstride;
+  return launch_hpsi<double>(a, op.model, s);
+}
+
+template <>
+cudaError_t apply_h<float>(const OpDev& op, const float* x, const int* xsel, size_t xstride,
+                           float* y, int ncomp, cudaStream_t s) {
+  HpsiArgs<float> a;
+  a.G = op.G;
+  a.R = op.R;
+  a.x = x;
+  a.y = y;
+  a.N = op.R.dim;
+  a.C = op.K * ncomp;
+  a.ncomp = ncomp;
+  a.K = op.K;
+  a.cE = op.cE_f;
+  a.cm = op.cm_f;
+  a.ch = op.ch_f;
+  a.cp = op.cp_f;
+  a.err = op.err;
+  a.seg_smem = op.seg_smem;
+  a.xsel = xsel;
+  a.xstride = xstride;
+  return launch_hpsi<float>(a, op.model, s);
+}
+
+template <typename S, typename SV>
+cudaError_t launch_multidot(Work<S>& w, const SV* V, size_t vstride, const int* jstate, int jfixed,
+                            const SV* Wp, cudaStream_t s) {
+  const int RG = kT / w.C;
+  const size_t sh = sizeof(double) * size_t(RG) * kIC * 2 * w.C;
+  if (w.ncomp == 1)
+    k_multidot<SV, 1><<<w.red.nblk, kT, sh, s>>>(V, vstride, jstate, jfixed, Wp, w.N, w.C,
+                                                 w.red.rpb, w.part, w.ldT);
+  else
+    k_multidot<SV, 2><<<w.red.nblk, kT, sh, s>>>(V, vstride, jstate, jfixed, Wp, w.N, w.C,
+                                                 w.red.rpb, w.part, w.ldT);
+  return cudaGetLastError();
+}
+
+template <typename S>
+cudaError_t launch_update(Work<S>& w, S* Wp, cudaStream_t s) {
+  if (w.ncomp == 1)
+    k_update<S, 1><<<w.red.nblk, kT, 0, s>>>(w.V, w.vstride, w.jstate, 0, Wp, w.N, w.C, w.ncomp,
+                                             w.h, w.K, w.status, w.red.rpb, w.npart);
+  else
+    k_update<S, 2><<<w.red.nblk, kT, 0, s>>>(w.V, w.vstride, w.jstate, 0, Wp, w.N, w.C, w.ncomp,
+                                             w.h, w.K, w.status, w.red.rpb, w.npart);
+  return cudaGetLastError();
+}
+
+// One Lanczos step on the device; every kernel reads j from w.jstate.
+template <typename S>
+cudaError_t lanczos_step(const OpDev& op, Work<S>& w, int reorth, double tiny_rel,
+                         cudaStream_t s) {
+  cudaError_t e = apply_h<S>(op, w.V, w.jstate, w.vstride, w.W, w.ncomp, s);
+  if (e != cudaSuccess) return e;
+  const int fdb = (w.ldT * w.K + 127) / 128;
+  for (int pass = 0; pass < reorth; ++pass) {
+    e = launch_multidot<S, S>(w, w.V, w.vstride, w.jstate, 0, w.W, s);
+    if (e != cudaSuccess) return e;
+    k_finish_dots<<<fdb, 128, 0, s>>>(w.part, w.red.nblk, w.ldT, w.jstate, 0, w.K, w.C, w.ncomp,
+                                      w.h, w.alpha, w.ldT, pass == 0, w.status);
+    e = launch_update<S>(w, w.W, s);
+    if (e != cudaSuccess) return e;
+  }
+  k_finish_norm<<<(w.K + 63) / 64, 64, 0, s>>>(w.npart, w.red.nblk, w.K, w.C, w.ncomp, w.jstate,
+                                               w.beta, w.alpha, w.ldT, w.status, w.len, w.bnorm,
+                                               tiny_rel, 1);
+  k_scale<S, S><<<grid_for(int64_t(w.vstride)), kT, 0, s>>>(w.W, w.V, w.vstride, w.jstate, 1, w.N,
+                                                            w.C, w.ncomp, w.bnorm, w.status,
+                                                            kActive);
+  k_advance<<<1, 1, 0, s>>>(w.jstate);
+  return cudaGetLastError();
+}
+
+// ||X_k|| of a double panel into out_norm (device, K).
+template <typename S>
+std::string colnorms_double(Work<S>& w, const double* X, double* out_norm, cudaStream_t s) {
+  k_residual_parts<<<w.red.nblk, kT, 0, s>>>(X, X, w.zeros, w.N, w.C, w.ncomp, w.red.rpb,
+                                             w.npart);
+  KCK(cudaGetLastError());
+  k_finish_norm<<<(w.K + 63) / 64, 64, 0, s>>>(w.npart, w.red.nblk, w.K, w.C, w.ncomp, w.jstate,
+                                               w.beta, w.alpha, w.ldT, w.status, w.len, out_norm,
+                                               0.0, 0);
+  KCK(cudaGetLastError());
+  return std::string();
+}
+
+// Per-point Re <x|y> of two double panels through the workspace buffers.
+template <typename S>
+std::string dots_ws(Work<S>& w, const double* x, const double* y, double* out_host,
+                    cudaStream_t s) {
+  KCK((launch_multidot<S, double>(w, x, 0, nullptr, 1, y, s)));
+  k_finish_dots<<<(w.K + 127) / 128, 128, 0, s>>>(w.part, w.red.nblk, w.ldT, nullptr, 1, w.K, w.C,
+                                                  w.ncomp, w.h, nullptr, 0, 0, nullptr);
+  KCK(cudaGetLastError());
+  std::vector<double> hh(2 * size_t(w.K));
+  KCK(cudaMemcpyAsync(hh.data(), w.h, sizeof(double) * 2 * w.K, cudaMemcpyDeviceToHost, s));
+  KCK(cudaStreamSynchronize(s));
+  for (int k = 0; k < w.K; ++k) out_host[k] = hh[2 * k];
+  return std::string();
+}
+
+template <typename S>
+std::string capture_steps(const OpDev& op, Work<S>& w, int steps, int reorth, double tiny_rel,
+                          cudaStream_t s) {
+  if (w.graph) {
+    cudaGraphExecDestroy(w.graph);
+    w.graph = nullptr;
+    w.graph_steps = 0;
+  }
+  cudaGraph_t g;
+  KCK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < steps && e == cudaSuccess; ++i) e = lanczos_step<S>(op, w, reorth, tiny_rel, s);
+  cudaError_t e2 = cudaStreamEndCapture(s, &g);
+  if (e != cudaSuccess) return std::string("graph capture: ") + cudaGetErrorString(e);
+  if (e2 != cudaSuccess) return std::string("graph capture end: ") + cudaGetErrorString(e2);
+  e = cudaGraphInstantiate(&w.graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return std::string("graph instantiate: ") + cudaGetErrorString(e);
+  w.graph_steps = steps;
+  w.graph_reorth = reorth;
+  w.graph_tiny = tiny_rel;
+  return std::string();
+}
+
+// `steps` Lanczos steps.  Full chunks replay a captured graph; the first
+// chunk of a new configuration runs eagerly (which also sets the kernels'
+// shared-memory attributes) and is captured for later chunks.
+template <typename S>
+std::string run_steps(const OpDev& op, Work<S>& w, const KrylovParams& p, int steps,
+                      double tiny_rel, cudaStream_t s, int64_t* matvecs) {
+  if (steps <= 0) return std::string();
+  const bool cached = w.graph && w.graph_steps == steps && w.graph_reorth == p.reorth &&
+                      w.graph_tiny == tiny_rel;
+  if (p.use_graph && steps == p.check_every && cached) {
+    KCK(cudaGraphLaunch(w.graph, s));
+  } else {
+    for (int i = 0; i < steps; ++i) KCK(lanczos_step<S>(op, w, p.reorth, tiny_rel, s));
+    if (p.use_graph && steps == p.check_every) {
+      std::string err = capture_steps<S>(op, w, steps, p.reorth, tiny_rel, s);
+      if (!err.empty()) return err;
+    }
+  }
+  *matvecs += steps;
+  return std::string();
+}
+
+// V_0 = X / ||X|| for active points (X double, storage S); rho = ||X||.
+template <typename S>
+std::string start_from(Work<S>& w, const double* X, cudaStream_t s) {
+  std::string err = colnorms_double<S>(w, X, w.rho, s);
+  if (!err.empty()) return err;
+  k_scale<double, S><<<grid_for(int64_t(w.vstride)), kT, 0, s>>>(
+      X, w.V, w.vstride, nullptr, 0, w.N, w.C, w.ncomp, w.rho, w.status, kActive);
+  KCK(cudaGetLastError());
+  return std::string();
+}
+
+template <typename S>
+std::string reset_cycle(Work<S>& w, cudaStream_t s) {
+  KCK(cudaMemsetAsync(w.jstate, 0, sizeof(int), s));
+  KCK(cudaMemsetAsync(w.alpha, 0, sizeof(double) * size_t(w.K) * w.ldT, s));
+  KCK(cudaMemsetAsync(w.beta, 0, sizeof(double) * size_t(w.K) * w.ldT, s));
+  k_set_int<<<(w.K + 127) / 128, 128, 0, s>>>(w.len, w.K, 0, w.status, kActive);
+  KCK(cudaGetLastError());
+  return std::string();
+}
+
+template <typename S>
+std::string ground_state_impl(const OpDev& op, const KrylovParams& p, Work<S>& w, double* X,
+                              double* E0, double* resid_out, cudaStream_t s, KrylovReport* rep) {
+  const int64_t N = op.R.dim;
+  const int K = op.K;
+  const int ncomp = 1, C = K;
+  int m = p.krylovdim;
+  if (m > N) m = int(N);
+  if (m > kMaxDim - 1) m = kMaxDim - 1;
+  if (m < 1) m = 1;
+  std::string err = w.ensure(N, C, K, ncomp, m);
+  if (!err.empty()) {
+    w.release();
+    return err;
+  }
+  const bool fp32 = sizeof(S) == 4;
+  const double tiny_rel = fp32 ? 1e-6 : 1e-12;
+  // FP32 panels cannot resolve residuals much below 1e-6 |H|: the inner
+  // solve stops there and the Ritz pair is finished in FP64 below.
+  const double tol_inner = fp32 ? fmax(p.tol, 2e-5) : p.tol;
+
+  cudaEvent_t ev0, ev1;
+  cudaEventCreate(&ev0);
+  cudaEventCreate(&ev1);
+  cudaEventRecord(ev0, s);
+  KCK(cudaMemsetAsync(w.status, 0, sizeof(int) * K, s));
+  KCK(cudaMemsetAsync(w.len, 0, sizeof(int) * K, s));
+  KCK(cudaMemsetAsync(w.fail, 0, sizeof(int), s));
+  if (!p.start_given) {
+    k_randn<double><<<grid_for(N * C), kT, 0, s>>>(X, N, C, ncomp, p.seed);
+    KCK(cudaGetLastError());
+  }
+  err = reset_cycle<S>(w, s);
+  if (!err.empty()) return err;
+  err = start_from<S>(w, X, s);
+  if (!err.empty()) return err;
+
+  std::vector<int> st(K);
+  int j = 0, restarts = 0;
+  int64_t matvecs = 0;
+  bool noconv = false;
+  while (true) {
+    const int steps = (m - j < p.check_every) ? (m - j) : p.check_every;
+    err = run_steps<S>(op, w, p, steps, tiny_rel, s, &matvecs);
+    if (!err.empty()) return err;
+    j += steps;
+    k_check_lowest<<<K, 32, 0, s>>>(w.alpha, w.beta, w.ldT, w.status, w.len, w.theta, w.resid,
+                                    w.coef, tol_inner);
+    KCK(cudaGetLastError());
+    KCK(cudaMemcpyAsync(st.data(), w.status, sizeof(int) * K, cudaMemcpyDeviceToHost, s));
+    KCK(cudaStreamSynchronize(s));
+    bool all = true;
+    for (int k = 0; k < K; ++k) all = all && (st[k] >= kConverged);
+    if (all) break;
+    if (j >= m) {
+      if (restarts >= p.maxiter) {
+        noconv = true;
+        break;
+      }
+      // keep the points that converged in this cycle, restart the others
+      // from their current Ritz vectors
+      k_combine<S, 1><<<grid_for(N * C), kT, 0, s>>>(w.V, w.vstride, w.coef, w.ldT, w.len,
+                                                     w.status, kConverged, X, N, C, ncomp);
+      k_set_int<<<(K + 127) / 128, 128, 0, s>>>(w.status, K, kWritten, w.status, kConverged);
+      k_combine<S, 1><<<grid_for(N * C), kT, 0, s>>>(w.V, w.vstride, w.coef, w.ldT, w.len,
+                                                     w.status, kActive, X, N, C, ncomp);
+      KCK(cudaGetLastError());
+      err = reset_cycle<S>(w, s);
+      if (!err.empty()) return err;
+      err = start_from<S>(w, X, s);
+      if (!err.empty()) return err;
+      j = 0;
+      ++restarts;
+    }
+  }
+  // final vectors of the points still on the current basis
+  k_set_int<<<(K + 127) / 128, 128, 0, s>>>(w.status, K, kConverged, w.status, kActive);
+  k_set_int<<<(K + 127) / 128, 128, 0, s>>>(w.status, K, kConverged, w.status, kExhausted);
+  k_combine<S, 1><<<grid_for(N * C), kT, 0, s>>>(w.V, w.vstride, w.coef, w.ldT, w.len, w.status,
+                                                 kConverged, X, N, C, ncomp);
+  KCK(cudaGetLastError());
+  std::vector<double> theta(K);
+  KCK(cudaMemcpyAsync(theta.data(), w.theta, sizeof(double) * K, cudaMemcpyDeviceToHost, s));
+
+  // FP64 finish: normalise X, R = H X in FP64, E = <X|R>, ||R - E X||.
+  KCK(cudaMemsetAsync(w.status, 0, sizeof(int) * K, s));
+  err = colnorms_double<S>(w, X, w.rho, s);
+  if (!err.empty()) return err;
+  k_scale<double, double><<<grid_for(N * C), kT, 0, s>>>(X, X, 0, nullptr, 0, N, C, ncomp, w.rho,
+                                                          nullptr, 0);
+  KCK(cudaGetLastError());
+  KCK(apply_h<double>(op, X, nullptr, 0, w.R, ncomp, s));
+  ++matvecs;
+  std::vector<double> erq(K), r2(K);
+  err = dots_ws<S>(w, X, w.R, erq.data(), s);
+  if (!err.empty()) return err;
+  KCK(cudaMemcpyAsync(w.theta, erq.data(), sizeof(double) * K, cudaMemcpyHostToDevice, s));
+  k_residual_parts<<<w.red.nblk, kT, 0, s>>>(X, w.R, w.theta, N, C, ncomp, w.red.rpb, w.npart);
+  k_finish_norm<<<(K + 63) / 64, 64, 0, s>>>(w.npart, w.red.nblk, K, C, ncomp, w.jstate, w.beta,
+                                             w.alpha, w.ldT, w.status, w.len, w.bnorm, 0.0, 0);
+  KCK(cudaGetLastError());
+  KCK(cudaMemcpyAsync(r2.data(), w.bnorm, sizeof(double) * K, cudaMemcpyDeviceToHost, s));
+  cudaEventRecord(ev1, s);
+  KCK(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ev0, ev1);
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  int conv = 0;
+  double maxr = 0.0;
+  for (int k = 0; k < K; ++k) {
+    // FP64: the Ritz value, as eigsolve returns; FP32-mixed: the FP64
+    // Rayleigh quotient of the FP32-converged vector.
+    E0[k] = fp32 ? erq[k] : theta[k];
+    if (resid_out) resid_out[k] = r2[k];
+    if (r2[k] <= tol_inner * 1.01 + 1e-300) ++conv;
+    maxr = fmax(maxr, r2[k]);
+  }
+  if (rep) {
+    rep->matvecs += matvecs;
+    rep->restarts += restarts;
+    rep->converged = conv;
+    rep->max_residual = maxr;
+    rep->seconds += ms * 1e-3;
+  }
+  if (noconv) return std::string("NOCONV: Lanczos did not converge within maxiter restarts");
+  return std::string();
+}
+
+template <typename S>
+std::string expm_impl(const OpDev& op, const KrylovParams& p, Work<S>& w, double dt, int n_steps,
+                      double* X, double* drift, StepObserver* obs, cudaStream_t s,
+                      KrylovReport* rep) {
+  const int64_t N = op.R.dim;
+  const int K = op.K;
+  const int ncomp = 2, C = 2 * K;
+  int m = p.krylovdim;
+  if (m > N) m = int(N);
+  if (m > kMaxDim - 1) m = kMaxDim - 1;
+  if (m < 1) m = 1;
+  std::string err = w.ensure(N, C, K, ncomp, m);
+  if (!err.empty()) {
+    w.release();
+    return err;
+  }
+  const double tiny_rel = (sizeof(S) == 8) ? 1e-12 : 1e-6;
+  std::vector<int> st(K);
+  std::vector<double> errs(K, 0.0), nrm(K);
+  if (drift)
+    for (int k = 0; k < K; ++k) drift[k] = 0.0;
+  int64_t matvecs = 0;
+  int substeps = 0;
+  double maxerr = 0.0;
+  cudaEvent_t ev0, ev1;
+  cudaEventCreate(&ev0);
+  cudaEventCreate(&ev1);
+  cudaEventRecord(ev0, s);
+  KCK(cudaMemsetAsync(w.fail, 0, sizeof(int), s));
+  if (obs) {
+    err = obs->on_step(0, X);
+    if (!err.empty()) return err;
+  }
+  for (int step = 1; step <= n_steps; ++step) {
+    double remaining = dt;
+    int guard_sub = 0;
+    while (remaining > 0.0) {
+      KCK(cudaMemsetAsync(w.status, 0, sizeof(int) * K, s));
+      KCK(cudaMemsetAsync(w.len, 0, sizeof(int) * K, s));
+      err = reset_cycle<S>(w, s);
+      if (!err.empty()) return err;
+      err = start_from<S>(w, X, s);
+      if (!err.empty()) return err;
+      int j = 0;
+      bool all = false;
+      while (j < m) {
+        const int steps = (m - j < p.check_every) ? (m - j) : p.check_every;
+        err = run_steps<S>(op, w, p, steps, tiny_rel, s, &matvecs);
+        if (!err.empty()) return err;
+        j += steps;
+        k_check_expm<<<K, 64, 0, s>>>(w.alpha, w.beta, w.ldT, w.status, w.len, w.rho, remaining,
+                                      w.resid, w.coef, p.tol, 0, w.fail);
+        KCK(cudaGetLastError());
+        KCK(cudaMemcpyAsync(st.data(), w.status, sizeof(int) * K, cudaMemcpyDeviceToHost, s));
+        KCK(cudaStreamSynchronize(s));
+        all = true;
+        for (int k = 0; k < K; ++k) all = all && (st[k] >= kConverged);
+        if (all) break;
+      }
+      double tau = remaining;
+      if (!all) {
+        // The Krylov space is too small for the whole interval: take the
+        // largest tau = remaining / 2^q meeting the tolerance (scaled to the
+        // sub-interval) for every point, then continue from there.
+        double t = remaining;
+        for (int q = 0; q < 40; ++q) {
+          t *= 0.5;
+          k_check_expm<<<K, 64, 0, s>>>(w.alpha, w.beta, w.ldT, w.status, w.len, w.rho, t,
+                                        w.resid, w.coef, p.tol * (t / dt), 0, w.fail);
+          KCK(cudaMemcpyAsync(st.data(), w.status, sizeof(int) * K, cudaMemcpyDeviceToHost, s));
+          KCK(cudaStreamSynchronize(s));
+          bool ok = true;
+          for (int k = 0; k < K; ++k) ok = ok && (st[k] >= kConverged);
+          if (ok) break;
+        }
+        tau = t;
+        KCK(cudaMemsetAsync(w.status, 0, sizeof(int) * K, s));
+        k_check_expm<<<K, 64, 0, s>>>(w.alpha, w.beta, w.ldT, w.status, w.len, w.rho, tau,
+                                      w.resid, w.coef, p.tol, 1, w.fail);
+        KCK(cudaGetLastError());
+        ++substeps;
+        if (++guard_sub > 4096) return std::string("NOCONV: exponential step could not be split");
+      }
+      KCK(cudaMemcpyAsync(errs.data(), w.resid, sizeof(double) * K, cudaMemcpyDeviceToHost, s));
+      k_combine<S, 2><<<grid_for(N * C), kT, 0, s>>>(w.V, w.vstride, w.coef, w.ldT, w.len,
+                                                     w.status, kConverged, X, N, C, ncomp);
+      KCK(cudaGetLastError());
+      KCK(cudaStreamSynchronize(s));
+      for (int k = 0; k < K; ++k) maxerr = fmax(maxerr, errs[k]);
+      remaining -= tau;
+      if (remaining < 1e-15 * dt) remaining = 0.0;
+    }
+    // psi ./= norm(psi)   (finite_ed.jl:420)
+    KCK(cudaMemsetAsync(w.status, 0, sizeof(int) * K, s));
+    err = colnorms_double<S>(w, X, w.rho, s);
+    if (!err.empty()) return err;
+    k_scale<double, double><<<grid_for(N * C), kT, 0, s>>>(X, X, 0, nullptr, 0, N, C, ncomp, w.rho,
+                                                            nullptr, 0);
+    KCK(cudaGetLastError());
+    if (drift) {
+      KCK(cudaMemcpyAsync(nrm.data(), w.rho, sizeof(double) * K, cudaMemcpyDeviceToHost, s));
+      KCK(cudaStreamSynchronize(s));
+      for (int k = 0; k < K; ++k) drift[k] = fmax(drift[k], fabs(nrm[k] - 1.0));
+    }
+    if (obs) {
+      err = obs->on_step(step, X);
+      if (!err.empty()) return err;
+    }
+  }
+  int fail = 0;
+  KCK(cudaMemcpyAsync(&fail, w.fail, sizeof(int), cudaMemcpyDeviceToHost, s));
+  cudaEventRecord(ev1, s);
+  KCK(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ev0, ev1);
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  if (rep) {
+    rep->matvecs += matvecs;
+    rep->restarts += substeps;
+    rep->converged = K;
+    rep->max_residual = maxerr;
+    rep->seconds += ms * 1e-3;
+  }
+  if (fail) return std::string("NOCONV: tridiagonal eigensolver did not converge");
+  return std::string();
+}
+
+}  // namespace
+
+struct KrylovCache {
+  Work<double> gs_d;
+  Work<float> gs_f;
+  Work<double> ex_d;
+  Work<float> ex_f;
+  ~KrylovCache() {
+    gs_d.release();
+    gs_f.release();
+    ex_d.release();
+    ex_f.release();
+  }
+};
+
+KrylovCache* krylov_cache_new() { return new KrylovCache(); }
+void krylov_cache_free(KrylovCache* c) { delete c; }
+
+cudaError_t apply_h_d(const OpDev& op, const double* x, double* y, int ncomp, cudaStream_t s) {
+  return apply_h<double>(op, x, nullptr, 0, y, ncomp, s);
+}
+
+cudaError_t apply_h_f(const OpDev& op, const float* x, float* y, int ncomp, cudaStream_t s) {
+  return apply_h<float>(op, x, nullptr, 0, y, ncomp, s);
+}
+
+std::string panel_dots(KrylovCache* cache, const double* x, const double* y, int64_t N, int K,
+                       int ncomp, double* out, cudaStream_t s) {
+  Work<double>& w = cache->ex_d;
+  // any workspace of matching shape serves; (re)shape the exponential one
+  std::string err = w.ensure(N, K * ncomp, K, ncomp, w.m > 0 ? w.m : 1);
+  if (!err.empty()) return err;
+  return dots_ws<double>(w, x, y, out, s);
+}
+
+std::string lanczos_ground_state(const OpDev& op, const KrylovParams& p, KrylovCache* cache,
+                                 double* X, double* E0, double* resid, cudaStream_t s,
+                                 KrylovReport* rep) {
+  if (op.K > kT) return "at most 256 real columns per panel";
+  if (!p.mixed) return ground_state_impl<double>(op, p, cache->gs_d, X, E0, resid, s, rep);
+  std::string err = ground_state_impl<float>(op, p, cache->gs_f, X, E0, resid, s, rep);
+  if (!err.empty() || p.refine <= 0) return err;
+  // FP64 correction: a short FP64 Lanczos started from the FP32 solution
+  KrylovParams q = p;
+  q.mixed = 0;
+  q.start_given = 1;
+  q.krylovdim = p.refine;
+  if (q.check_every > q.krylovdim) q.check_every = q.krylovdim;
+  return ground_state_impl<double>(op, q, cache->gs_d, X, E0, resid, s, rep);
+}
+
+std::string krylov_expm(const OpDev& op, const KrylovParams& p, KrylovCache* cache, double dt,
+                        int n_steps, double* X, double* norm_drift, StepObserver* obs,
+                        cudaStream_t s, KrylovReport* rep) {
+  if (op.K * 2 > kT) return "at most 128 complex points per panel";
+  if (p.mixed)
+    return expm_impl<float>(op, p, cache->ex_f, dt, n_steps, X, norm_drift, obs, s, rep);
+  return expm_impl<double>(op, p, cache->ex_d, dt, n_steps, X, norm_drift, obs, s, rep);
+}
+
+}  // namespace lgt

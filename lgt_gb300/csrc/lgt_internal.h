@@ -1,0 +1,79 @@
+// lgt_internal.h -- internal host-side structures of the library (not part of
+// the C-ABI).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "lgt_common.cuh"
+
+namespace lgt {
+
+// Everything a kernel needs to turn an order key into a basis index.
+//
+// Two-level sorted index: the top level is the segment table `segc`, one
+// entry per fermion mask with the sector's particle number, addressed by the
+// mask's colexicographic rank (masks with k set bits in ascending numeric
+// order are in colex order, rank = sum_j C(p_j, j) over the set-bit
+// positions p_1 < ... < p_k).  segc[r] is the first index of mask r's
+// segment.  The hop kernels stage this level in shared memory when it fits.
+// The bottom level is a binary search over the segment's low key parts.
+struct RankView {
+  const uint64_t* keys;   // sorted order keys [dim]
+  const uint32_t* low;    // low (e_U) parts of the keys [dim] (when ushift <= 32)
+  const uint32_t* segc;   // segment starts [nmasks + 1]
+  const uint32_t* binom;  // C(p, j) at [p * 33 + j], p < 32, j <= 32
+  int64_t dim;
+  int nmasks;
+  int ushift;
+  int low32;              // 1 when `low` is valid
+};
+
+struct BasisDev {
+  Geom G{};
+  int64_t dim = 0;
+  int nmasks = 0;
+  uint64_t* keys = nullptr;
+  uint32_t* low = nullptr;
+  uint32_t* segc = nullptr;
+  uint32_t* masks = nullptr;
+  uint32_t* binom = nullptr;
+  int* err = nullptr;           // device error word (DevErr bits)
+  cudaStream_t stream = nullptr;
+  RankView view() const {
+    RankView v;
+    v.keys = keys;
+    v.low = low;
+    v.segc = segc;
+    v.binom = binom;
+    v.dim = dim;
+    v.nmasks = nmasks;
+    v.ushift = G.ushift;
+    v.low32 = (G.ushift <= 32) ? 1 : 0;
+    return v;
+  }
+};
+
+// Host geometry set-up; returns an empty string or an error message.
+std::string make_geom(int nx, int ny, int dg, const int32_t* g_charges, Geom* G);
+
+// Enumerates the sector basis on the GPU (kernels in basis.cu).  Allocates
+// the device tables of `B`.  Returns an empty string or an error message.
+std::string build_basis_device(BasisDev* B);
+void free_basis_device(BasisDev* B);
+
+// Decode device keys [i0, i0+n) into Julia-layout int8 arrays on the device.
+void launch_decode_states(const BasisDev& B, int64_t i0, int64_t n, int8_t* nf, int8_t* eR,
+                          int8_t* eU, cudaStream_t s);
+void launch_ref_keys(const BasisDev& B, int64_t i0, int64_t n, uint64_t* out, cudaStream_t s);
+// Rank reference (_encode) keys; out = 1-based index or 0 when absent.
+void launch_rank_ref_keys(const BasisDev& B, const uint64_t* in, int64_t n, int64_t* out,
+                          cudaStream_t s);
+// Rank order keys; out = 0-based index or -1 when absent.
+void launch_rank_order_keys(const BasisDev& B, const uint64_t* in, int64_t n, int64_t* out,
+                            cudaStream_t s);
+
+}  // namespace lgt

@@ -1,0 +1,76 @@
+// lgt_krylov.h -- batched Krylov drivers (Lanczos ground state and Krylov
+// exp(-iHt) steps) on K-interleaved panels.
+#pragma once
+
+#include <string>
+
+#include "lgt_hpsi.h"
+
+namespace lgt {
+
+// Host-side description of the operator the drivers apply: the basis, the
+// model and per-point coefficient arrays on the device in both precisions.
+struct OpDev {
+  Geom G;
+  RankView R;
+  int* err;
+  uint32_t model;
+  int K;
+  int seg_smem;
+  const double *cE_d, *cm_d, *ch_d, *cp_d;
+  const float *cE_f, *cm_f, *ch_f, *cp_f;
+};
+
+struct KrylovParams {
+  int krylovdim;
+  int maxiter;
+  double tol;
+  int mixed;        // FP32 storage + H*psi, FP64 dots
+  int reorth;       // Gram-Schmidt passes
+  int check_every;
+  int refine;       // FP64 Lanczos correction steps after a mixed solve
+  uint64_t seed;
+  int use_graph;
+  int start_given;
+};
+
+struct KrylovReport {
+  int64_t matvecs = 0;
+  int restarts = 0;
+  int converged = 0;
+  double max_residual = 0.0;
+  double seconds = 0.0;
+};
+
+// Workspaces and captured graphs of the drivers, kept per Hamiltonian.
+struct KrylovCache;
+KrylovCache* krylov_cache_new();
+void krylov_cache_free(KrylovCache* c);
+
+// Lowest eigenpair of each of the K operators.  X (device, double, [N][K])
+// receives the normalised eigenvectors; when start_given, X holds the start
+// vectors on entry.  E0, resid: host arrays of K.
+std::string lanczos_ground_state(const OpDev& op, const KrylovParams& p, KrylovCache* cache,
+                                 double* X, double* E0, double* resid, cudaStream_t s,
+                                 KrylovReport* rep);
+
+// n_steps steps psi <- exp(-i H dt) psi (renormalised) on the complex panel
+// X (device, double, [N][K][2]).  After each step (and before the first)
+// `observe_cb(step)` is called with X holding the current state.
+struct StepObserver {
+  virtual ~StepObserver() {}
+  virtual std::string on_step(int step, const double* X) = 0;
+};
+std::string krylov_expm(const OpDev& op, const KrylovParams& p, KrylovCache* cache, double dt,
+                        int n_steps, double* X, double* norm_drift, StepObserver* obs,
+                        cudaStream_t s, KrylovReport* rep);
+
+// y = H x on a double or float panel (C = K * ncomp columns).
+cudaError_t apply_h_d(const OpDev& op, const double* x, double* y, int ncomp, cudaStream_t s);
+cudaError_t apply_h_f(const OpDev& op, const float* x, float* y, int ncomp, cudaStream_t s);
+
+// Per-point Re <x|y> (FP64) of two double panels: out[K] on host.
+std::string panel_dots(KrylovCache* cache, const double* x, const double* y, int64_t N, int K,
+                       int ncomp, double* out, cudaStream_t s);
+
+}  // namespace lgt
