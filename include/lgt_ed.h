@@ -73,7 +73,11 @@ enum {
                           refinement                                           */
 };
 
-enum { LGT_DEVICE_PTRS = 1 };
+enum {
+  LGT_DEVICE_PTRS = 1, /* amplitude pointers are device pointers                  */
+  LGT_ASYNC = 2        /* with LGT_DEVICE_PTRS: lgt_matvec returns without waiting
+                          for the kernel (stream-ordered; no self-check read)   */
+};
 
 typedef struct lgt_basis lgt_basis;
 typedef struct lgt_ham lgt_ham;
@@ -151,6 +155,16 @@ LGT_API lgt_status lgt_basis_rank(const lgt_basis* b, const uint64_t* order_keys
                           int64_t* index0);
 
 LGT_API void lgt_basis_destroy(lgt_basis* b);
+
+/* Run this basis' work (and that of its Hamiltonians) on a caller-owned
+   cudaStream_t (passed as void*), e.g. a CUDA.jl or PyTorch stream; NULL
+   restores the basis' own stream.  No reference counterpart (the reference
+   has no device). */
+LGT_API lgt_status lgt_basis_set_stream(lgt_basis* b, void* stream);
+
+/* Number of kernels this process has launched through the library so far
+   (graph replays count their kernel nodes).  No reference counterpart. */
+LGT_API lgt_status lgt_launch_count(uint64_t* count);
 
 /* ---- Hamiltonian -------------------------------------------------------- */
 

@@ -32,12 +32,14 @@ LGT_FP32 = 1
 LGT_FP32_MIXED = 2
 
 LGT_DEVICE_PTRS = 1
+LGT_ASYNC = 2
 
 # every symbol include/lgt_ed.h declares
 EXPORTS = (
     "lgt_krylov_defaults", "lgt_last_error", "lgt_version",
     "lgt_basis_create", "lgt_basis_dim", "lgt_basis_keys", "lgt_basis_states",
-    "lgt_basis_lookup", "lgt_basis_rank", "lgt_basis_destroy",
+    "lgt_basis_lookup", "lgt_basis_rank", "lgt_basis_destroy", "lgt_basis_set_stream",
+    "lgt_launch_count",
     "lgt_ham_create", "lgt_ham_set_couplings", "lgt_ham_nnz", "lgt_ham_export_csr",
     "lgt_matvec", "lgt_ground_state", "lgt_expm_steps", "lgt_observe", "lgt_energy",
     "lgt_ham_destroy",
@@ -127,6 +129,8 @@ def load(build_if_missing: bool = True):
         "lgt_basis_lookup": (i32, [vp, vp, i64, vp]),
         "lgt_basis_rank": (i32, [vp, vp, i64, vp]),
         "lgt_basis_destroy": (None, [vp]),
+        "lgt_basis_set_stream": (i32, [vp, vp]),
+        "lgt_launch_count": (i32, [ctypes.POINTER(ctypes.c_uint64)]),
         "lgt_ham_create": (i32, [vp, i32, vp, vp, vp, u32, pvp]),
         "lgt_ham_set_couplings": (i32, [vp, vp, vp, vp]),
         "lgt_ham_nnz": (i32, [vp, ctypes.POINTER(ctypes.c_int64)]),
@@ -157,6 +161,13 @@ def check(code: int):
     if code in (LGT_ERR_SECTOR, LGT_ERR_ARG, LGT_ERR_KEYWIDTH, LGT_ERR_UNSUPPORTED):
         raise ValueError("lgt error %d: %s" % (code, msg))
     raise LgtError(code, msg)
+
+
+def launch_count() -> int:
+    """Kernels launched by the library in this process so far."""
+    n = ctypes.c_uint64()
+    check(load().lgt_launch_count(ctypes.byref(n)))
+    return int(n.value)
 
 
 def defaults(for_exponentiate: bool = False) -> KrylovOpts:

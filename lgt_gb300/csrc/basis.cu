@@ -286,9 +286,9 @@ std::string compact(const Pred& p, Out** out, int64_t* count, cudaStream_t s) {
   uint64_t* offs = nullptr;
   CK(cudaMallocAsync(&counts, sizeof(uint32_t) * nblk, s));
   CK(cudaMallocAsync(&offs, sizeof(uint64_t) * (nblk + 1), s));
-  k_compact_count<<<nblk, kThreads, 0, s>>>(p, counts);
+  k_compact_count<<<nblk, kThreads, 0, s>>>(p, counts), lgt::note_launch();
   CK(cudaGetLastError());
-  k_scan_counts<<<1, 1024, 0, s>>>(counts, nblk, offs);
+  k_scan_counts<<<1, 1024, 0, s>>>(counts, nblk, offs), lgt::note_launch();
   CK(cudaGetLastError());
   uint64_t total = 0;
   CK(cudaMemcpyAsync(&total, offs + nblk, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
@@ -296,7 +296,7 @@ std::string compact(const Pred& p, Out** out, int64_t* count, cudaStream_t s) {
   Out* o = nullptr;
   if (total > 0) {
     CK(cudaMalloc(&o, sizeof(Out) * total));
-    k_compact_write<<<nblk, kThreads, 0, s>>>(p, offs, o);
+    k_compact_write<<<nblk, kThreads, 0, s>>>(p, offs, o), lgt::note_launch();
     CK(cudaGetLastError());
   }
   CK(cudaFreeAsync(counts, s));
@@ -372,7 +372,7 @@ std::string build_basis_device(BasisDev* B) {
   CK(cudaMalloc(&B->err, sizeof(int)));
   CK(cudaMemsetAsync(B->err, 0, sizeof(int), s));
   CK(cudaMalloc(&B->binom, sizeof(uint32_t) * 32 * 33));
-  k_binom<<<1, 32, 0, s>>>(B->binom);
+  k_binom<<<1, 32, 0, s>>>(B->binom), lgt::note_launch();
   CK(cudaGetLastError());
 
   // 1. masks with N_f set bits, ascending
@@ -418,11 +418,11 @@ std::string build_basis_device(BasisDev* B) {
   // 3. ranking tables
   CK(cudaMalloc(&B->segc, sizeof(uint32_t) * (nmasks + 1)));
   k_segments<<<int((nmasks + 1 + 255) / 256), 256, 0, s>>>(B->keys, dim, B->masks, int(nmasks),
-                                                          G.ushift, B->segc);
+                                                          G.ushift, B->segc), lgt::note_launch();
   CK(cudaGetLastError());
   if (G.ushift <= 32 && dim > 0) {
     CK(cudaMalloc(&B->low, sizeof(uint32_t) * dim));
-    k_low_parts<<<int((dim + 255) / 256), 256, 0, s>>>(B->keys, dim, G.ushift, B->low);
+    k_low_parts<<<int((dim + 255) / 256), 256, 0, s>>>(B->keys, dim, G.ushift, B->low), lgt::note_launch();
     CK(cudaGetLastError());
   }
   CK(cudaStreamSynchronize(s));
@@ -447,24 +447,24 @@ void free_basis_device(BasisDev* B) {
 void launch_decode_states(const BasisDev& B, int64_t i0, int64_t n, int8_t* nf, int8_t* eR,
                           int8_t* eU, cudaStream_t s) {
   if (n <= 0) return;
-  k_decode_states<<<int((n + 255) / 256), 256, 0, s>>>(B.G, B.keys, i0, n, nf, eR, eU);
+  k_decode_states<<<int((n + 255) / 256), 256, 0, s>>>(B.G, B.keys, i0, n, nf, eR, eU), lgt::note_launch();
 }
 
 void launch_ref_keys(const BasisDev& B, int64_t i0, int64_t n, uint64_t* out, cudaStream_t s) {
   if (n <= 0) return;
-  k_ref_keys<<<int((n + 255) / 256), 256, 0, s>>>(B.G, B.keys, i0, n, out);
+  k_ref_keys<<<int((n + 255) / 256), 256, 0, s>>>(B.G, B.keys, i0, n, out), lgt::note_launch();
 }
 
 void launch_rank_ref_keys(const BasisDev& B, const uint64_t* in, int64_t n, int64_t* out,
                           cudaStream_t s) {
   if (n <= 0) return;
-  k_rank_ref_keys<<<int((n + 255) / 256), 256, 0, s>>>(B.G, B.view(), in, n, out);
+  k_rank_ref_keys<<<int((n + 255) / 256), 256, 0, s>>>(B.G, B.view(), in, n, out), lgt::note_launch();
 }
 
 void launch_rank_order_keys(const BasisDev& B, const uint64_t* in, int64_t n, int64_t* out,
                             cudaStream_t s) {
   if (n <= 0) return;
-  k_rank_order_keys<<<int((n + 255) / 256), 256, 0, s>>>(B.G, B.view(), in, n, out);
+  k_rank_order_keys<<<int((n + 255) / 256), 256, 0, s>>>(B.G, B.view(), in, n, out), lgt::note_launch();
 }
 
 }  // namespace lgt

@@ -1,5 +1,6 @@
 // capi.cu -- the extern "C" boundary (include/lgt_ed.h): handles, argument
 // checks, host<->device staging and error reporting around the kernels.
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -18,6 +19,8 @@ using namespace lgt;
 namespace {
 
 thread_local std::string g_last_error;
+std::atomic<uint64_t> g_launches{0};
+thread_local bool g_capturing = false;
 
 lgt_status fail(lgt_status code, const std::string& msg) {
   g_last_error = msg;
@@ -64,9 +67,17 @@ struct DevBuf {
 
 }  // namespace
 
+namespace lgt {
+void note_launch(int n) {
+  if (!g_capturing) g_launches.fetch_add(uint64_t(n), std::memory_order_relaxed);
+}
+void set_capturing(bool on) { g_capturing = on; }
+}  // namespace lgt
+
 struct lgt_basis {
   BasisDev B;
   int device = 0;
+  cudaStream_t own_stream = nullptr;
 };
 
 struct lgt_ham {
@@ -191,6 +202,7 @@ lgt_status lgt_basis_create(int32_t nx, int32_t ny, int32_t dg, const int32_t* g
   }
   cudaError_t e = cudaSetDevice(b->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->B.stream, cudaStreamNonBlocking);
+  b->own_stream = b->B.stream;
   if (e != cudaSuccess) {
     delete b;
     return cuda_fail(e, "lgt_basis_create");
@@ -301,8 +313,23 @@ void lgt_basis_destroy(lgt_basis* b) {
   cudaSetDevice(b->device);
   cudaStreamSynchronize(b->B.stream);
   free_basis_device(&b->B);
-  cudaStreamDestroy(b->B.stream);
+  cudaStreamDestroy(b->own_stream);
   delete b;
+}
+
+lgt_status lgt_basis_set_stream(lgt_basis* b, void* stream) {
+  if (!b) return fail(LGT_ERR_ARG, "null basis");
+  lgt_status st = set_device(b);
+  if (st) return st;
+  CUDA_OR_FAIL(cudaStreamSynchronize(b->B.stream));
+  b->B.stream = stream ? static_cast<cudaStream_t>(stream) : b->own_stream;
+  return LGT_OK;
+}
+
+lgt_status lgt_launch_count(uint64_t* count) {
+  if (!count) return fail(LGT_ERR_ARG, "null argument");
+  *count = g_launches.load();
+  return LGT_OK;
 }
 
 lgt_status lgt_ham_create(const lgt_basis* b, int32_t K, const double* g, const double* t,
@@ -438,6 +465,7 @@ lgt_status lgt_matvec(const lgt_ham* hc, const void* x, void* y, int32_t ncomp, 
                       ? apply_h_d(op, static_cast<const double*>(dx), static_cast<double*>(dy), ncomp, s)
                       : apply_h_f(op, static_cast<const float*>(dx), static_cast<float*>(dy), ncomp, s);
   if (e != cudaSuccess) return cuda_fail(e, "lgt_matvec");
+  if (on_device(flags) && (flags & LGT_ASYNC)) return LGT_OK;
   if (!on_device(flags)) CUDA_OR_FAIL(cudaMemcpyAsync(y, dy, bytes, cudaMemcpyDeviceToHost, s));
   CUDA_OR_FAIL(cudaStreamSynchronize(s));
   return check_device_errors(h->b);

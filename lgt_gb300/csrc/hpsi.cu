@@ -198,7 +198,7 @@ cudaError_t launch_t(const HpsiArgs<T>& a, cudaStream_t s) {
   }
   const int64_t blocks = (a.N + kThreads - 1) / kThreads;
   if (blocks <= 0) return cudaSuccess;
-  kern<<<unsigned(blocks), kThreads, L.total, s>>>(a);
+  kern<<<unsigned(blocks), kThreads, L.total, s>>>(a), lgt::note_launch();
   return cudaGetLastError();
 }
 
@@ -304,10 +304,10 @@ cudaError_t launch_row_nnz(const Geom& G, const RankView& R, uint32_t model, int
   if (N == 0) return cudaSuccess;
   const unsigned blocks = unsigned((N + 255) / 256);
   const bool plaq = model & kModelPlaq, jw = model & kModelJW;
-  if (plaq && jw) k_row_nnz<true, true><<<blocks, 256, 0, s>>>(G, R, N, counts);
-  else if (plaq) k_row_nnz<true, false><<<blocks, 256, 0, s>>>(G, R, N, counts);
-  else if (jw) k_row_nnz<false, true><<<blocks, 256, 0, s>>>(G, R, N, counts);
-  else k_row_nnz<false, false><<<blocks, 256, 0, s>>>(G, R, N, counts);
+  if (plaq && jw) k_row_nnz<true, true><<<blocks, 256, 0, s>>>(G, R, N, counts), lgt::note_launch();
+  else if (plaq) k_row_nnz<true, false><<<blocks, 256, 0, s>>>(G, R, N, counts), lgt::note_launch();
+  else if (jw) k_row_nnz<false, true><<<blocks, 256, 0, s>>>(G, R, N, counts), lgt::note_launch();
+  else k_row_nnz<false, false><<<blocks, 256, 0, s>>>(G, R, N, counts), lgt::note_launch();
   return cudaGetLastError();
 }
 
@@ -319,13 +319,13 @@ cudaError_t launch_row_fill(const Geom& G, const RankView& R, uint32_t model,
   const unsigned blocks = unsigned((N + 255) / 256);
   const bool plaq = model & kModelPlaq, jw = model & kModelJW;
   if (plaq && jw)
-    k_row_fill<true, true><<<blocks, 256, 0, s>>>(G, R, N, rowptr, g, t, m, cols, vals, err);
+    k_row_fill<true, true><<<blocks, 256, 0, s>>>(G, R, N, rowptr, g, t, m, cols, vals, err), lgt::note_launch();
   else if (plaq)
-    k_row_fill<true, false><<<blocks, 256, 0, s>>>(G, R, N, rowptr, g, t, m, cols, vals, err);
+    k_row_fill<true, false><<<blocks, 256, 0, s>>>(G, R, N, rowptr, g, t, m, cols, vals, err), lgt::note_launch();
   else if (jw)
-    k_row_fill<false, true><<<blocks, 256, 0, s>>>(G, R, N, rowptr, g, t, m, cols, vals, err);
+    k_row_fill<false, true><<<blocks, 256, 0, s>>>(G, R, N, rowptr, g, t, m, cols, vals, err), lgt::note_launch();
   else
-    k_row_fill<false, false><<<blocks, 256, 0, s>>>(G, R, N, rowptr, g, t, m, cols, vals, err);
+    k_row_fill<false, false><<<blocks, 256, 0, s>>>(G, R, N, rowptr, g, t, m, cols, vals, err), lgt::note_launch();
   return cudaGetLastError();
 }
 

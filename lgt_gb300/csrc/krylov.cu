@@ -587,6 +587,7 @@ struct Work {
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0, graph_reorth = 0;
   double graph_tiny = 0.0;
+  int graph_nodes = 0;
 
   std::string ensure(int64_t N_, int C_, int K_, int ncomp_, int m_) {
     if (N_ == N && C_ == C && K_ == K && ncomp_ == ncomp && m_ == m && V) return std::string();
@@ -706,10 +707,10 @@ cudaError_t launch_multidot(Work<S>& w, const SV* V, size_t vstride, const int* 
   const size_t sh = sizeof(double) * size_t(RG) * kIC * 2 * w.C;
   if (w.ncomp == 1)
     k_multidot<SV, 1><<<w.red.nblk, kT, sh, s>>>(V, vstride, jstate, jfixed, Wp, w.N, w.C,
-                                                 w.red.rpb, w.part, w.ldT);
+                                                 w.red.rpb, w.part, w.ldT), lgt::note_launch();
   else
     k_multidot<SV, 2><<<w.red.nblk, kT, sh, s>>>(V, vstride, jstate, jfixed, Wp, w.N, w.C,
-                                                 w.red.rpb, w.part, w.ldT);
+                                                 w.red.rpb, w.part, w.ldT), lgt::note_launch();
   return cudaGetLastError();
 }
 
@@ -717,10 +718,10 @@ template <typename S>
 cudaError_t launch_update(Work<S>& w, S* Wp, cudaStream_t s) {
   if (w.ncomp == 1)
     k_update<S, 1><<<w.red.nblk, kT, 0, s>>>(w.V, w.vstride, w.jstate, 0, Wp, w.N, w.C, w.ncomp,
-                                             w.h, w.K, w.status, w.red.rpb, w.npart);
+                                             w.h, w.K, w.status, w.red.rpb, w.npart), lgt::note_launch();
   else
     k_update<S, 2><<<w.red.nblk, kT, 0, s>>>(w.V, w.vstride, w.jstate, 0, Wp, w.N, w.C, w.ncomp,
-                                             w.h, w.K, w.status, w.red.rpb, w.npart);
+                                             w.h, w.K, w.status, w.red.rpb, w.npart), lgt::note_launch();
   return cudaGetLastError();
 }
 
@@ -735,17 +736,17 @@ cudaError_t lanczos_step(const OpDev& op, Work<S>& w, int reorth, double tiny_re
     e = launch_multidot<S, S>(w, w.V, w.vstride, w.jstate, 0, w.W, s);
     if (e != cudaSuccess) return e;
     k_finish_dots<<<fdb, 128, 0, s>>>(w.part, w.red.nblk, w.ldT, w.jstate, 0, w.K, w.C, w.ncomp,
-                                      w.h, w.alpha, w.ldT, pass == 0, w.status);
+                                      w.h, w.alpha, w.ldT, pass == 0, w.status), lgt::note_launch();
     e = launch_update<S>(w, w.W, s);
     if (e != cudaSuccess) return e;
   }
   k_finish_norm<<<(w.K + 63) / 64, 64, 0, s>>>(w.npart, w.red.nblk, w.K, w.C, w.ncomp, w.jstate,
                                                w.beta, w.alpha, w.ldT, w.status, w.len, w.bnorm,
-                                               tiny_rel, 1);
+                                               tiny_rel, 1), lgt::note_launch();
   k_scale<S, S><<<grid_for(int64_t(w.vstride)), kT, 0, s>>>(w.W, w.V, w.vstride, w.jstate, 1, w.N,
                                                             w.C, w.ncomp, w.bnorm, w.status,
-                                                            kActive);
-  k_advance<<<1, 1, 0, s>>>(w.jstate);
+                                                            kActive), lgt::note_launch();
+  k_advance<<<1, 1, 0, s>>>(w.jstate), lgt::note_launch();
   return cudaGetLastError();
 }
 
@@ -753,11 +754,11 @@ cudaError_t lanczos_step(const OpDev& op, Work<S>& w, int reorth, double tiny_re
 template <typename S>
 std::string colnorms_double(Work<S>& w, const double* X, double* out_norm, cudaStream_t s) {
   k_residual_parts<<<w.red.nblk, kT, 0, s>>>(X, X, w.zeros, w.N, w.C, w.ncomp, w.red.rpb,
-                                             w.npart);
+                                             w.npart), lgt::note_launch();
   KCK(cudaGetLastError());
   k_finish_norm<<<(w.K + 63) / 64, 64, 0, s>>>(w.npart, w.red.nblk, w.K, w.C, w.ncomp, w.jstate,
                                                w.beta, w.alpha, w.ldT, w.status, w.len, out_norm,
-                                               0.0, 0);
+                                               0.0, 0), lgt::note_launch();
   KCK(cudaGetLastError());
   return std::string();
 }
@@ -768,7 +769,7 @@ std::string dots_ws(Work<S>& w, const double* x, const double* y, double* out_ho
                     cudaStream_t s) {
   KCK((launch_multidot<S, double>(w, x, 0, nullptr, 1, y, s)));
   k_finish_dots<<<(w.K + 127) / 128, 128, 0, s>>>(w.part, w.red.nblk, w.ldT, nullptr, 1, w.K, w.C,
-                                                  w.ncomp, w.h, nullptr, 0, 0, nullptr);
+                                                  w.ncomp, w.h, nullptr, 0, 0, nullptr), lgt::note_launch();
   KCK(cudaGetLastError());
   std::vector<double> hh(2 * size_t(w.K));
   KCK(cudaMemcpyAsync(hh.data(), w.h, sizeof(double) * 2 * w.K, cudaMemcpyDeviceToHost, s));
@@ -787,11 +788,16 @@ std::string capture_steps(const OpDev& op, Work<S>& w, int steps, int reorth, do
   }
   cudaGraph_t g;
   KCK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  set_capturing(true);
   cudaError_t e = cudaSuccess;
   for (int i = 0; i < steps && e == cudaSuccess; ++i) e = lanczos_step<S>(op, w, reorth, tiny_rel, s);
+  set_capturing(false);
   cudaError_t e2 = cudaStreamEndCapture(s, &g);
   if (e != cudaSuccess) return std::string("graph capture: ") + cudaGetErrorString(e);
   if (e2 != cudaSuccess) return std::string("graph capture end: ") + cudaGetErrorString(e2);
+  size_t nodes = 0;
+  cudaGraphGetNodes(g, nullptr, &nodes);
+  w.graph_nodes = int(nodes);
   e = cudaGraphInstantiate(&w.graph, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return std::string("graph instantiate: ") + cudaGetErrorString(e);
@@ -812,6 +818,7 @@ std::string run_steps(const OpDev& op, Work<S>& w, const KrylovParams& p, int st
                       w.graph_tiny == tiny_rel;
   if (p.use_graph && steps == p.check_every && cached) {
     KCK(cudaGraphLaunch(w.graph, s));
+    note_launch(w.graph_nodes);
   } else {
     for (int i = 0; i < steps; ++i) KCK(lanczos_step<S>(op, w, p.reorth, tiny_rel, s));
     if (p.use_graph && steps == p.check_every) {
@@ -829,7 +836,7 @@ std::string start_from(Work<S>& w, const double* X, cudaStream_t s) {
   std::string err = colnorms_double<S>(w, X, w.rho, s);
   if (!err.empty()) return err;
   k_scale<double, S><<<grid_for(int64_t(w.vstride)), kT, 0, s>>>(
-      X, w.V, w.vstride, nullptr, 0, w.N, w.C, w.ncomp, w.rho, w.status, kActive);
+      X, w.V, w.vstride, nullptr, 0, w.N, w.C, w.ncomp, w.rho, w.status, kActive), lgt::note_launch();
   KCK(cudaGetLastError());
   return std::string();
 }
@@ -839,7 +846,7 @@ std::string reset_cycle(Work<S>& w, cudaStream_t s) {
   KCK(cudaMemsetAsync(w.jstate, 0, sizeof(int), s));
   KCK(cudaMemsetAsync(w.alpha, 0, sizeof(double) * size_t(w.K) * w.ldT, s));
   KCK(cudaMemsetAsync(w.beta, 0, sizeof(double) * size_t(w.K) * w.ldT, s));
-  k_set_int<<<(w.K + 127) / 128, 128, 0, s>>>(w.len, w.K, 0, w.status, kActive);
+  k_set_int<<<(w.K + 127) / 128, 128, 0, s>>>(w.len, w.K, 0, w.status, kActive), lgt::note_launch();
   KCK(cudaGetLastError());
   return std::string();
 }
@@ -873,7 +880,7 @@ std::string ground_state_impl(const OpDev& op, const KrylovParams& p, Work<S>& w
   KCK(cudaMemsetAsync(w.len, 0, sizeof(int) * K, s));
   KCK(cudaMemsetAsync(w.fail, 0, sizeof(int), s));
   if (!p.start_given) {
-    k_randn<double><<<grid_for(N * C), kT, 0, s>>>(X, N, C, ncomp, p.seed);
+    k_randn<double><<<grid_for(N * C), kT, 0, s>>>(X, N, C, ncomp, p.seed), lgt::note_launch();
     KCK(cudaGetLastError());
   }
   err = reset_cycle<S>(w, s);
@@ -891,7 +898,7 @@ std::string ground_state_impl(const OpDev& op, const KrylovParams& p, Work<S>& w
     if (!err.empty()) return err;
     j += steps;
     k_check_lowest<<<K, 32, 0, s>>>(w.alpha, w.beta, w.ldT, w.status, w.len, w.theta, w.resid,
-                                    w.coef, tol_inner);
+                                    w.coef, tol_inner), lgt::note_launch();
     KCK(cudaGetLastError());
     KCK(cudaMemcpyAsync(st.data(), w.status, sizeof(int) * K, cudaMemcpyDeviceToHost, s));
     KCK(cudaStreamSynchronize(s));
@@ -906,10 +913,10 @@ std::string ground_state_impl(const OpDev& op, const KrylovParams& p, Work<S>& w
       // keep the points that converged in this cycle, restart the others
       // from their current Ritz vectors
       k_combine<S, 1><<<grid_for(N * C), kT, 0, s>>>(w.V, w.vstride, w.coef, w.ldT, w.len,
-                                                     w.status, kConverged, X, N, C, ncomp);
-      k_set_int<<<(K + 127) / 128, 128, 0, s>>>(w.status, K, kWritten, w.status, kConverged);
+                                                     w.status, kConverged, X, N, C, ncomp), lgt::note_launch();
+      k_set_int<<<(K + 127) / 128, 128, 0, s>>>(w.status, K, kWritten, w.status, kConverged), lgt::note_launch();
       k_combine<S, 1><<<grid_for(N * C), kT, 0, s>>>(w.V, w.vstride, w.coef, w.ldT, w.len,
-                                                     w.status, kActive, X, N, C, ncomp);
+                                                     w.status, kActive, X, N, C, ncomp), lgt::note_launch();
       KCK(cudaGetLastError());
       err = reset_cycle<S>(w, s);
       if (!err.empty()) return err;
@@ -920,10 +927,10 @@ std::string ground_state_impl(const OpDev& op, const KrylovParams& p, Work<S>& w
     }
   }
   // final vectors of the points still on the current basis
-  k_set_int<<<(K + 127) / 128, 128, 0, s>>>(w.status, K, kConverged, w.status, kActive);
-  k_set_int<<<(K + 127) / 128, 128, 0, s>>>(w.status, K, kConverged, w.status, kExhausted);
+  k_set_int<<<(K + 127) / 128, 128, 0, s>>>(w.status, K, kConverged, w.status, kActive), lgt::note_launch();
+  k_set_int<<<(K + 127) / 128, 128, 0, s>>>(w.status, K, kConverged, w.status, kExhausted), lgt::note_launch();
   k_combine<S, 1><<<grid_for(N * C), kT, 0, s>>>(w.V, w.vstride, w.coef, w.ldT, w.len, w.status,
-                                                 kConverged, X, N, C, ncomp);
+                                                 kConverged, X, N, C, ncomp), lgt::note_launch();
   KCK(cudaGetLastError());
   std::vector<double> theta(K);
   KCK(cudaMemcpyAsync(theta.data(), w.theta, sizeof(double) * K, cudaMemcpyDeviceToHost, s));
@@ -933,7 +940,7 @@ std::string ground_state_impl(const OpDev& op, const KrylovParams& p, Work<S>& w
   err = colnorms_double<S>(w, X, w.rho, s);
   if (!err.empty()) return err;
   k_scale<double, double><<<grid_for(N * C), kT, 0, s>>>(X, X, 0, nullptr, 0, N, C, ncomp, w.rho,
-                                                          nullptr, 0);
+                                                          nullptr, 0), lgt::note_launch();
   KCK(cudaGetLastError());
   KCK(apply_h<double>(op, X, nullptr, 0, w.R, ncomp, s));
   ++matvecs;
@@ -941,9 +948,9 @@ std::string ground_state_impl(const OpDev& op, const KrylovParams& p, Work<S>& w
   err = dots_ws<S>(w, X, w.R, erq.data(), s);
   if (!err.empty()) return err;
   KCK(cudaMemcpyAsync(w.theta, erq.data(), sizeof(double) * K, cudaMemcpyHostToDevice, s));
-  k_residual_parts<<<w.red.nblk, kT, 0, s>>>(X, w.R, w.theta, N, C, ncomp, w.red.rpb, w.npart);
+  k_residual_parts<<<w.red.nblk, kT, 0, s>>>(X, w.R, w.theta, N, C, ncomp, w.red.rpb, w.npart), lgt::note_launch();
   k_finish_norm<<<(K + 63) / 64, 64, 0, s>>>(w.npart, w.red.nblk, K, C, ncomp, w.jstate, w.beta,
-                                             w.alpha, w.ldT, w.status, w.len, w.bnorm, 0.0, 0);
+                                             w.alpha, w.ldT, w.status, w.len, w.bnorm, 0.0, 0), lgt::note_launch();
   KCK(cudaGetLastError());
   KCK(cudaMemcpyAsync(r2.data(), w.bnorm, sizeof(double) * K, cudaMemcpyDeviceToHost, s));
   cudaEventRecord(ev1, s);
@@ -1024,7 +1031,7 @@ std::string expm_impl(const OpDev& op, const KrylovParams& p, Work<S>& w, double
         if (!err.empty()) return err;
         j += steps;
         k_check_expm<<<K, 64, 0, s>>>(w.alpha, w.beta, w.ldT, w.status, w.len, w.rho, remaining,
-                                      w.resid, w.coef, p.tol, 0, w.fail);
+                                      w.resid, w.coef, p.tol, 0, w.fail), lgt::note_launch();
         KCK(cudaGetLastError());
         KCK(cudaMemcpyAsync(st.data(), w.status, sizeof(int) * K, cudaMemcpyDeviceToHost, s));
         KCK(cudaStreamSynchronize(s));
@@ -1041,7 +1048,7 @@ std::string expm_impl(const OpDev& op, const KrylovParams& p, Work<S>& w, double
         for (int q = 0; q < 40; ++q) {
           t *= 0.5;
           k_check_expm<<<K, 64, 0, s>>>(w.alpha, w.beta, w.ldT, w.status, w.len, w.rho, t,
-                                        w.resid, w.coef, p.tol * (t / dt), 0, w.fail);
+                                        w.resid, w.coef, p.tol * (t / dt), 0, w.fail), lgt::note_launch();
           KCK(cudaMemcpyAsync(st.data(), w.status, sizeof(int) * K, cudaMemcpyDeviceToHost, s));
           KCK(cudaStreamSynchronize(s));
           bool ok = true;
@@ -1051,14 +1058,14 @@ std::string expm_impl(const OpDev& op, const KrylovParams& p, Work<S>& w, double
         tau = t;
         KCK(cudaMemsetAsync(w.status, 0, sizeof(int) * K, s));
         k_check_expm<<<K, 64, 0, s>>>(w.alpha, w.beta, w.ldT, w.status, w.len, w.rho, tau,
-                                      w.resid, w.coef, p.tol, 1, w.fail);
+                                      w.resid, w.coef, p.tol, 1, w.fail), lgt::note_launch();
         KCK(cudaGetLastError());
         ++substeps;
         if (++guard_sub > 4096) return std::string("NOCONV: exponential step could not be split");
       }
       KCK(cudaMemcpyAsync(errs.data(), w.resid, sizeof(double) * K, cudaMemcpyDeviceToHost, s));
       k_combine<S, 2><<<grid_for(N * C), kT, 0, s>>>(w.V, w.vstride, w.coef, w.ldT, w.len,
-                                                     w.status, kConverged, X, N, C, ncomp);
+                                                     w.status, kConverged, X, N, C, ncomp), lgt::note_launch();
       KCK(cudaGetLastError());
       KCK(cudaStreamSynchronize(s));
       for (int k = 0; k < K; ++k) maxerr = fmax(maxerr, errs[k]);
@@ -1070,7 +1077,7 @@ std::string expm_impl(const OpDev& op, const KrylovParams& p, Work<S>& w, double
     err = colnorms_double<S>(w, X, w.rho, s);
     if (!err.empty()) return err;
     k_scale<double, double><<<grid_for(N * C), kT, 0, s>>>(X, X, 0, nullptr, 0, N, C, ncomp, w.rho,
-                                                            nullptr, 0);
+                                                            nullptr, 0), lgt::note_launch();
     KCK(cudaGetLastError());
     if (drift) {
       KCK(cudaMemcpyAsync(nrm.data(), w.rho, sizeof(double) * K, cudaMemcpyDeviceToHost, s));

@@ -57,6 +57,12 @@ struct BasisDev {
   }
 };
 
+// Kernel-launch accounting, reported by lgt_launch_count: every launch site
+// adds one, a graph replay adds its kernel-node count, and launches recorded
+// into a graph while the calling thread captures are not counted.
+void note_launch(int n = 1);
+void set_capturing(bool on);
+
 // Host geometry set-up; returns an empty string or an error message.
 std::string make_geom(int nx, int ny, int dg, const int32_t* g_charges, Geom* G);
 

@@ -149,7 +149,7 @@ cudaError_t launch_obs3(const Geom& G, const RankView& R, const T* x, int K, int
     if (e != cudaSuccess) return e;
     attr_bytes = sh;
   }
-  kern<<<nblk, kT, sh, s>>>(G, R, x, R.dim, K, nfeat, rpb, part, err);
+  kern<<<nblk, kT, sh, s>>>(G, R, x, R.dim, K, nfeat, rpb, part, err), lgt::note_launch();
   return cudaGetLastError();
 }
 
@@ -188,7 +188,7 @@ cudaError_t launch_observe(const Geom& G, const RankView& R, const T* x, int K, 
                       ? launch_obs2<T, 1>(G, R, x, K, nfeat, nblk, rpb, part, err, s)
                       : launch_obs2<T, 2>(G, R, x, K, nfeat, nblk, rpb, part, err, s);
   if (e != cudaSuccess) return e;
-  k_observe_finish<<<(K * nfeat + 127) / 128, 128, 0, s>>>(part, nblk, K, nfeat, out);
+  k_observe_finish<<<(K * nfeat + 127) / 128, 128, 0, s>>>(part, nblk, K, nfeat, out), lgt::note_launch();
   return cudaGetLastError();
 }
 
