@@ -95,7 +95,15 @@ typedef struct lgt_krylov_opts {
   uint64_t seed;         /* start vector of point k: normal(seed, k)           */
   int32_t use_graph;     /* replay the step sequence as a CUDA graph           */
   int32_t start_given;   /* ground state: 1 = psi holds the start vectors      */
+  int32_t solver;        /* ground state: LGT_SOLVER_*                          */
 } lgt_krylov_opts;
+
+/* Ground-state solver selection. */
+enum {
+  LGT_SOLVER_AUTO = 0,   /* per-CTA for sectors up to 8192 states, else panel   */
+  LGT_SOLVER_PANEL = 1,  /* K-interleaved panels, CUDA-graph Lanczos steps      */
+  LGT_SOLVER_CTA = 2     /* one CTA per coupling point, whole solve in a kernel */
+};
 
 /* Per-call solver report. */
 typedef struct lgt_info {
@@ -202,6 +210,19 @@ LGT_API lgt_status lgt_matvec(const lgt_ham* h, const void* x, void* y, int32_t 
    K doubles (final FP64 residual norm ||H psi - E0 psi||), may be NULL. */
 LGT_API lgt_status lgt_ground_state(lgt_ham* h, const lgt_krylov_opts* opts, double* E0, void* psi,
                             double* residual, uint32_t flags, lgt_info* info);
+
+/* find_ground_state over several Hamiltonians at once (the GS benchmark
+   grid, gs_benchmark.jl:36-52,86-175, and lattices / sectors of uneven
+   dimension): every (Hamiltonian, point) pair of a sector up to 8192 states
+   runs in ONE persistent launch, one CTA each, largest sectors first;
+   larger sectors go through the panel solver.  E0[i], psi[i], residual[i]
+   are the per-Hamiltonian arrays of lgt_ground_state (psi[i] and
+   residual[i] may be NULL; psi must be device pointers with
+   LGT_DEVICE_PTRS).  All Hamiltonians must live on one device. */
+LGT_API lgt_status lgt_ground_state_batch(int32_t nham, lgt_ham* const* hams,
+                                          const lgt_krylov_opts* opts, double* const* E0,
+                                          void* const* psi, double* const* residual,
+                                          uint32_t flags, lgt_info* info);
 
 /* evolve_ED! (finite_ed.jl:405-431): n_steps Krylov steps
    psi <- exp(-i H dt) psi, each followed by renormalisation, for all K

@@ -31,6 +31,10 @@ LGT_FP64 = 0
 LGT_FP32 = 1
 LGT_FP32_MIXED = 2
 
+LGT_SOLVER_AUTO = 0
+LGT_SOLVER_PANEL = 1
+LGT_SOLVER_CTA = 2
+
 LGT_DEVICE_PTRS = 1
 LGT_ASYNC = 2
 
@@ -41,7 +45,7 @@ EXPORTS = (
     "lgt_basis_lookup", "lgt_basis_rank", "lgt_basis_destroy", "lgt_basis_set_stream",
     "lgt_launch_count",
     "lgt_ham_create", "lgt_ham_set_couplings", "lgt_ham_nnz", "lgt_ham_export_csr",
-    "lgt_matvec", "lgt_ground_state", "lgt_expm_steps", "lgt_observe", "lgt_energy",
+    "lgt_matvec", "lgt_ground_state", "lgt_ground_state_batch", "lgt_expm_steps", "lgt_observe", "lgt_energy",
     "lgt_ham_destroy",
 )
 
@@ -58,6 +62,7 @@ class KrylovOpts(ctypes.Structure):
         ("seed", ctypes.c_uint64),
         ("use_graph", ctypes.c_int32),
         ("start_given", ctypes.c_int32),
+        ("solver", ctypes.c_int32),
     ]
 
 
@@ -138,6 +143,8 @@ def load(build_if_missing: bool = True):
         "lgt_matvec": (i32, [vp, vp, vp, i32, i32, u32]),
         "lgt_ground_state": (i32, [vp, ctypes.POINTER(KrylovOpts), vp, vp, vp, u32,
                                    ctypes.POINTER(Info)]),
+        "lgt_ground_state_batch": (i32, [i32, vp, ctypes.POINTER(KrylovOpts), vp, vp, vp, u32,
+                                         ctypes.POINTER(Info)]),
         "lgt_expm_steps": (i32, [vp, ctypes.POINTER(KrylovOpts), dbl, i32, vp, vp, vp, u32,
                                  ctypes.POINTER(Info)]),
         "lgt_observe": (i32, [vp, vp, i32, i32, u32, dbl, vp, vp, vp, vp]),

@@ -1,7 +1,9 @@
 // capi.cu -- the extern "C" boundary (include/lgt_ed.h): handles, argument
 // checks, host<->device staging and error reporting around the kernels.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <memory>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -13,6 +15,7 @@
 #include "lgt_internal.h"
 #include "lgt_krylov.h"
 #include "lgt_observe.h"
+#include "lgt_small.h"
 
 using namespace lgt;
 
@@ -90,6 +93,8 @@ struct lgt_ham {
   int seg_smem = 0;
   KrylovCache* cache = nullptr;
   DevBuf x, y, part, out;
+  Pattern pattern;          // lookup pass of the per-CTA solver (built on demand)
+  SmallWork small;
   OpDev op() const {
     OpDev o;
     o.G = b->B.G;
@@ -489,6 +494,113 @@ static KrylovParams to_params(const lgt_krylov_opts* o, int for_exp) {
   return p;
 }
 
+}  // extern "C"
+
+namespace {
+
+bool use_cta(const lgt_ham* h, const lgt_krylov_opts* opts, const KrylovParams& p) {
+  const int solver = opts ? opts->solver : LGT_SOLVER_AUTO;
+  if (solver == LGT_SOLVER_PANEL) return false;
+  const bool fits = h->b->B.dim <= kSmallMaxN && p.krylovdim <= 63;
+  return fits && (solver == LGT_SOLVER_CTA || solver == LGT_SOLVER_AUTO);
+}
+
+lgt_status ensure_pattern(lgt_ham* h) {
+  if (h->pattern.rowptr) return LGT_OK;
+  std::string m = build_pattern(h->b->B, h->model, &h->pattern, h->b->B.stream);
+  if (!m.empty()) {
+    free_pattern(&h->pattern);
+    return from_msg(m);
+  }
+  return LGT_OK;
+}
+
+SmallParams small_params(const KrylovParams& p) {
+  SmallParams q;
+  q.m = p.krylovdim;
+  q.maxiter = p.maxiter;
+  q.tol = p.tol;
+  q.reorth = p.reorth;
+  q.check_every = p.check_every;
+  q.seed = p.seed;
+  q.start_given = p.start_given;
+  return q;
+}
+
+// Per-CTA solves of several Hamiltonians (device panels X[i]).
+lgt_status cta_solve(const std::vector<lgt_ham*>& hams, const KrylovParams& p,
+                     const std::vector<double*>& X, double* const* E0, double* const* residual,
+                     lgt_info* info) {
+  std::vector<SmallJob> jobs;
+  std::vector<std::vector<double>> coef(hams.size());
+  std::vector<std::vector<int>> steps(hams.size()), rest(hams.size());
+  std::vector<std::unique_ptr<bool[]>> conv(hams.size());
+  for (size_t i = 0; i < hams.size(); ++i) {
+    lgt_ham* h = hams[i];
+    lgt_status st = ensure_pattern(h);
+    if (st) return st;
+    const int K = h->K;
+    coef[i].resize(4 * size_t(K));
+    for (int k = 0; k < K; ++k) {
+      const double g = h->g[k], t = h->t[k], m = h->m[k];
+      coef[i][k] = (g * g) / 2;
+      coef[i][K + k] = m;
+      coef[i][2 * K + k] = -t;
+      coef[i][3 * K + k] = -(1.0 / (2.0 * (g * g)));
+    }
+    steps[i].assign(K, 0);
+    rest[i].assign(K, 0);
+    conv[i].reset(new bool[K]);
+    SmallJob J;
+    J.pattern = &h->pattern;
+    J.K = K;
+    J.cE = coef[i].data();
+    J.cm = coef[i].data() + K;
+    J.ch = coef[i].data() + 2 * K;
+    J.cp = coef[i].data() + 3 * K;
+    J.psi = X[i];
+    J.E0 = E0[i];
+    J.resid = residual ? residual[i] : nullptr;
+    J.steps = steps[i].data();
+    J.restarts = rest[i].data();
+    J.converged = conv[i].get();
+    jobs.push_back(J);
+  }
+  lgt_ham* h0 = hams[0];
+  double secs = 0.0;
+  std::string m = small_ground_states(jobs, small_params(p), p.mixed, &h0->small,
+                                      h0->b->B.stream, &secs);
+  if (!m.empty()) return from_msg(m);
+  int nconv = 0, maxsteps = 0, maxrest = 0;
+  double maxr = 0.0;
+  bool all = true;
+  for (size_t i = 0; i < hams.size(); ++i)
+    for (int k = 0; k < hams[i]->K; ++k) {
+      nconv += conv[i][k] ? 1 : 0;
+      all = all && conv[i][k];
+      maxsteps = std::max(maxsteps, steps[i][k]);
+      maxrest = std::max(maxrest, rest[i][k]);
+      if (residual) maxr = std::max(maxr, residual[i][k]);
+    }
+  if (info) {
+    info->matvecs = maxsteps + 1;
+    info->restarts = maxrest;
+    info->converged = nconv;
+    info->max_residual = maxr;
+    info->seconds = secs;
+  }
+  for (lgt_ham* h : hams) {
+    lgt_status de = check_device_errors(h->b);
+    if (de) return de;
+  }
+  if (!all) return fail(LGT_ERR_NOCONV, "NOCONV: Lanczos did not converge within maxiter restarts");
+  return LGT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 lgt_status lgt_ground_state(lgt_ham* h, const lgt_krylov_opts* opts, double* E0, void* psi,
                             double* residual, uint32_t flags, lgt_info* info) {
   if (!h || !E0) return fail(LGT_ERR_ARG, "null argument");
@@ -510,6 +622,16 @@ lgt_status lgt_ground_state(lgt_ham* h, const lgt_krylov_opts* opts, double* E0,
     if (p.start_given) CUDA_OR_FAIL(cudaMemcpyAsync(X, psi, bytes, cudaMemcpyHostToDevice, s));
   }
   std::vector<double> res(h->K);
+  if (use_cta(h, opts, p)) {
+    double* r = res.data();
+    lgt_status rc = cta_solve({h}, p, {X}, &E0, &r, info);
+    if (residual) std::memcpy(residual, res.data(), sizeof(double) * h->K);
+    if (rc != LGT_OK && rc != LGT_ERR_NOCONV) return rc;
+    if (psi && !on_device(flags))
+      CUDA_OR_FAIL(cudaMemcpyAsync(psi, X, bytes, cudaMemcpyDeviceToHost, s));
+    CUDA_OR_FAIL(cudaStreamSynchronize(s));
+    return rc;
+  }
   KrylovReport rep;
   std::string m = lanczos_ground_state(h->op(), p, h->cache, X, E0, res.data(), s, &rep);
   if (residual) std::memcpy(residual, res.data(), sizeof(double) * h->K);
@@ -528,6 +650,77 @@ lgt_status lgt_ground_state(lgt_ham* h, const lgt_krylov_opts* opts, double* E0,
   lgt_status de = check_device_errors(h->b);
   if (de) return de;
   if (rc == LGT_ERR_NOCONV) return fail(LGT_ERR_NOCONV, m);
+  return LGT_OK;
+}
+
+lgt_status lgt_ground_state_batch(int32_t nham, lgt_ham* const* hams, const lgt_krylov_opts* opts,
+                                  double* const* E0, void* const* psi, double* const* residual,
+                                  uint32_t flags, lgt_info* info) {
+  if (nham < 1 || !hams || !E0) return fail(LGT_ERR_ARG, "null argument");
+  for (int i = 0; i < nham; ++i) {
+    if (!hams[i] || !E0[i]) return fail(LGT_ERR_ARG, "null Hamiltonian or E0");
+    if (hams[i]->b->device != hams[0]->b->device)
+      return fail(LGT_ERR_ARG, "all Hamiltonians must live on one device");
+    if (psi && psi[i] && !on_device(flags))
+      return fail(LGT_ERR_ARG, "lgt_ground_state_batch takes device psi panels");
+  }
+  KrylovParams p = to_params(opts, 0);
+  if (p.check_every > p.krylovdim) p.check_every = p.krylovdim;
+  lgt_status st = set_device(hams[0]->b);
+  if (st) return st;
+  std::vector<lgt_ham*> small;
+  std::vector<double*> xs;
+  std::vector<double*> e0s, rs;
+  std::vector<int> large;
+  for (int i = 0; i < nham; ++i) {
+    lgt_ham* h = hams[i];
+    const size_t bytes = size_t(h->b->B.dim) * h->K * sizeof(double);
+    if (use_cta(h, opts, p)) {
+      double* X = (psi && psi[i]) ? static_cast<double*>(psi[i]) : nullptr;
+      if (!X) {
+        CUDA_OR_FAIL(h->x.need(bytes));
+        X = static_cast<double*>(h->x.p);
+      }
+      small.push_back(h);
+      xs.push_back(X);
+      e0s.push_back(E0[i]);
+      rs.push_back(residual ? residual[i] : nullptr);
+    } else {
+      large.push_back(i);
+    }
+  }
+  lgt_info tot;
+  std::memset(&tot, 0, sizeof(tot));
+  lgt_status worst = LGT_OK;
+  if (!small.empty()) {
+    std::vector<std::vector<double>> rbuf(small.size());
+    std::vector<double*> rp(small.size());
+    for (size_t i = 0; i < small.size(); ++i) {
+      rbuf[i].resize(small[i]->K);
+      rp[i] = rs[i] ? rs[i] : rbuf[i].data();
+    }
+    lgt_info one;
+    std::memset(&one, 0, sizeof(one));
+    lgt_status rc = cta_solve(small, p, xs, e0s.data(), rp.data(), &one);
+    if (rc != LGT_OK && rc != LGT_ERR_NOCONV) return rc;
+    if (rc) worst = rc;
+    tot = one;
+  }
+  for (int i : large) {
+    lgt_info one;
+    std::memset(&one, 0, sizeof(one));
+    lgt_status rc = lgt_ground_state(hams[i], opts, E0[i], psi ? psi[i] : nullptr,
+                                     residual ? residual[i] : nullptr, flags, &one);
+    if (rc != LGT_OK && rc != LGT_ERR_NOCONV) return rc;
+    if (rc) worst = rc;
+    tot.matvecs = std::max(tot.matvecs, one.matvecs);
+    tot.restarts = std::max(tot.restarts, one.restarts);
+    tot.converged += one.converged;
+    tot.max_residual = std::max(tot.max_residual, one.max_residual);
+    tot.seconds += one.seconds;
+  }
+  if (info) *info = tot;
+  if (worst) return fail(worst, "NOCONV: some points did not converge within maxiter restarts");
   return LGT_OK;
 }
 
@@ -724,6 +917,8 @@ void lgt_ham_destroy(lgt_ham* h) {
   h->y.release();
   h->part.release();
   h->out.release();
+  free_pattern(&h->pattern);
+  cudaFree(h->small.base);
   cudaFree(h->coef_d);
   cudaFree(h->coef_f);
   delete h;

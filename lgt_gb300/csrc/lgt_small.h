@@ -1,0 +1,81 @@
+// lgt_small.h -- persistent per-CTA Lanczos for small sectors.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "lgt_internal.h"
+
+namespace lgt {
+
+// Largest sector the per-CTA solver takes (rows held in registers:
+// 16 per thread x 512 threads).
+constexpr int kSmallMaxN = 8192;
+
+// Result of the lookup pass: neighbour ranks of every row (index << 2 |
+// kind) in CSR order, and the integer parts of the diagonal.
+struct Pattern {
+  int N = 0;
+  int nnz = 0;
+  uint32_t model = 0;
+  int* rowptr = nullptr;
+  uint32_t* nbr = nullptr;
+  int16_t* e2 = nullptr;
+  int16_t* stag = nullptr;
+};
+
+struct SmallProblem {
+  int N;
+  const int* rowptr;
+  const uint32_t* nbr;
+  const int16_t* e2;
+  const int16_t* stag;
+};
+
+struct SmallUnit {
+  int prob;        // index into the problem table
+  int k;           // coupling point (start-vector stream)
+  double cE, cm, ch, cp;
+  double* psi;     // output (and start vector when given), stride psi_stride
+  int psi_stride;
+  void* V;         // (m + 1) x N Krylov basis, storage precision
+  double* x;       // N doubles
+  double* out;     // 8 doubles: E0, residual, steps, restarts, converged, estimate
+};
+
+struct SmallParams {
+  int m;
+  int maxiter;
+  double tol;
+  int reorth;
+  int check_every;
+  uint64_t seed;
+  int start_given;
+};
+
+// One Hamiltonian's share of a batched launch.
+struct SmallJob {
+  const Pattern* pattern;
+  int K;
+  const double *cE, *cm, *ch, *cp;  // host arrays [K]
+  double* psi;                      // device panel [N][K]
+  double* E0;                       // host [K]
+  double* resid;                    // host [K] or null
+  int* steps;                       // host [K] or null
+  int* restarts;                    // host [K] or null
+  bool* converged;                  // host [K] or null
+};
+
+struct SmallWork {
+  void* base = nullptr;
+  size_t bytes = 0;
+};
+
+std::string build_pattern(const BasisDev& B, uint32_t model, Pattern* P, cudaStream_t s);
+void free_pattern(Pattern* P);
+
+// All (job, point) units in one launch, largest sectors first.
+std::string small_ground_states(const std::vector<SmallJob>& jobs, const SmallParams& prm,
+                                int mixed, SmallWork* ws, cudaStream_t s, double* seconds);
+
+}  // namespace lgt

@@ -1,0 +1,622 @@
+// small.cu -- persistent batched Lanczos for small sectors: one CTA per
+// (lattice, coupling point) runs a whole ground-state solve.
+//
+// For sectors up to kSmallMaxN states the step latency of the panel path
+// (about ten dependent kernels per Lanczos step) dominates, so here every
+// (problem, point) unit is one 512-thread CTA that keeps the current Lanczos
+// residual in registers (row r of thread t: r = t + i*512) and the Krylov
+// basis in global memory (L2-resident), and runs matvec, classical
+// Gram-Schmidt twice against the whole basis (FP64 accumulation), the
+// tridiagonal check, restarts and the FP64 finish without leaving the
+// kernel.  Units of different sectors and sizes share one launch (uneven
+// batch); the largest are scheduled first.
+//
+// The neighbour ranks of a lattice are computed once by a device "lookup
+// pass" (k_pattern_*: the move enumeration and rank of the H*psi kernel)
+// and shared by all K coupling points; coefficients are per point, so
+// nothing of the matrix values is stored.
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "lgt_moves.cuh"
+#include "lgt_rank.cuh"
+#include "lgt_small.h"
+
+namespace lgt {
+
+namespace {
+
+constexpr int kCta = 512;
+constexpr int kWarpsCta = kCta / 32;
+constexpr int kMaxM = 64;
+
+#define SCK(call)                                                                  \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess) return std::string(#call ": ") + cudaGetErrorString(e_); \
+  } while (0)
+
+// ---- lookup pass --------------------------------------------------------------
+
+template <bool PLAQ, bool JW>
+__global__ void k_pattern_count(Geom G, RankView R, int64_t N, int* counts) {
+  int64_t row = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (row >= N) return;
+  const Config c = decode(G, R.keys[row]);
+  int n = 0;
+  for_each_move<PLAQ, JW>(G, c, [&](uint64_t, uint32_t) { ++n; });
+  counts[row] = n;
+}
+
+// Single-block exclusive scan of int counts into int32 row pointers.
+__global__ void __launch_bounds__(1024) k_scan_rows(const int* counts, int64_t n, int* rowptr) {
+  __shared__ int warp_sum[32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int64_t start = 0; start < n; start += 1024) {
+    const int64_t i = start + threadIdx.x;
+    const int v = (i < n) ? counts[i] : 0;
+    int x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, d);
+      if (lane >= d) x += y;
+    }
+    if (lane == 31) warp_sum[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      int s = warp_sum[lane];
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, s, d);
+        if (lane >= d) s += y;
+      }
+      warp_sum[lane] = s;
+    }
+    __syncthreads();
+    const int excl = (wid > 0) ? warp_sum[wid - 1] : 0;
+    if (i < n) rowptr[i] = carry + excl + x - v;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += warp_sum[31];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) rowptr[n] = carry;
+}
+
+template <bool PLAQ, bool JW>
+__global__ void k_pattern_fill(Geom G, RankView R, int64_t N, const int* rowptr, uint32_t* nbr,
+                               int16_t* e2, int16_t* stag, int* err) {
+  int64_t row = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (row >= N) return;
+  const Config c = decode(G, R.keys[row]);
+  int a, s;
+  diag_parts(G, c, &a, &s);
+  e2[row] = int16_t(a);
+  stag[row] = int16_t(s);
+  int p = rowptr[row];
+  const int end = rowptr[row + 1];
+  for_each_move<PLAQ, JW>(G, c, [&](uint64_t nk, uint32_t kind) {
+    const int64_t j = rank_key(R, R.segc, R.binom, nk);
+    if (j < 0 || p >= end) {
+      raise_err(err, j < 0 ? kDevErrRank : kDevErrBounds);
+      return;
+    }
+    nbr[p++] = (uint32_t(j) << 2) | kind;
+  });
+}
+
+// ---- device helpers -----------------------------------------------------------
+
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+// Same stream of normals as the panel path's start vectors (point k, row r).
+__device__ __forceinline__ double start_normal(uint64_t seed, int k, int64_t row) {
+  uint64_t h = mix64(mix64(seed) ^ mix64(uint64_t(k) + 0x5851F42D4C957F2Dull));
+  h = mix64(h ^ uint64_t(row));
+  const uint64_t h2 = mix64(h);
+  const double u1 = (double((h >> 11) + 1)) * 0x1.0p-53;
+  const double u2 = double(h2 >> 11) * 0x1.0p-53;
+  return sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum of one double per thread (all threads get the result).
+__device__ double block_sum(double v, double* red) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int w = 0; w < kWarpsCta; ++w) s += red[w];
+  return s;
+}
+
+__device__ int sturm_below(const double* a, const double* b, int n, double x) {
+  int cnt = 0;
+  double q = 1.0;
+  for (int i = 0; i < n; ++i) {
+    q = (a[i] - x) - ((i > 0) ? (b[i - 1] * b[i - 1]) / q : 0.0);
+    if (q == 0.0) q = -1e-300;
+    if (q < 0.0) ++cnt;
+  }
+  return cnt;
+}
+
+// Lowest eigenpair of the n x n symmetric tridiagonal (a, b) by warp-parallel
+// multisection of the Sturm count (32 probes per round), then inverse
+// iteration on the positive-definite T - (theta - delta) I by lane 0.
+// Called by one full warp; z (n entries) is written by lane 0.
+__device__ double warp_lowest_eig(const double* a, const double* b, int n, double* z,
+                                  double* work) {
+  const int lane = threadIdx.x & 31;
+  double lo = a[0], hi = a[0];
+  for (int i = 0; i < n; ++i) {
+    const double r = ((i > 0) ? fabs(b[i - 1]) : 0.0) + ((i < n - 1) ? fabs(b[i]) : 0.0);
+    lo = fmin(lo, a[i] - r);
+    hi = fmax(hi, a[i] + r);
+  }
+  const double scale = fmax(fmax(fabs(lo), fabs(hi)), 1e-300);
+  for (int it = 0; it < 40; ++it) {
+    if (hi - lo <= 2.2e-16 * scale) break;
+    const double step = (hi - lo) / 33.0;
+    const double x = lo + step * double(lane + 1);
+    const unsigned bal = __ballot_sync(0xffffffffu, sturm_below(a, b, n, x) >= 1);
+    if (bal) {
+      const int L = __ffs(bal) - 1;
+      const double nhi = lo + step * double(L + 1);
+      const double nlo = (L > 0) ? lo + step * double(L) : lo;
+      if (!(nhi < hi) && !(nlo > lo)) break;  // no progress at this precision
+      hi = nhi;
+      lo = nlo;
+    } else {
+      const double nlo = lo + step * 32.0;
+      if (!(nlo > lo)) break;
+      lo = nlo;
+    }
+  }
+  const double theta = 0.5 * (lo + hi);
+  if (lane == 0) {
+    const double shift = theta - 4.0 * 2.2e-16 * scale;
+    double* d = work;
+    double* l = work + kMaxM;
+    for (int i = 0; i < n; ++i) z[i] = 1.0;
+    for (int rep = 0; rep < 3; ++rep) {
+      d[0] = a[0] - shift;
+      if (d[0] <= 0.0) d[0] = 1e-300;
+      for (int i = 1; i < n; ++i) {
+        l[i - 1] = b[i - 1] / d[i - 1];
+        d[i] = (a[i] - shift) - l[i - 1] * b[i - 1];
+        if (d[i] <= 0.0) d[i] = 1e-300;
+      }
+      for (int i = 1; i < n; ++i) z[i] -= l[i - 1] * z[i - 1];
+      for (int i = 0; i < n; ++i) z[i] /= d[i];
+      for (int i = n - 2; i >= 0; --i) z[i] -= l[i] * z[i + 1];
+      double mx = 0.0, nn = 0.0;
+      for (int i = 0; i < n; ++i) mx = fmax(mx, fabs(z[i]));
+      for (int i = 0; i < n; ++i) {
+        z[i] /= mx;
+        nn += z[i] * z[i];
+      }
+      nn = sqrt(nn);
+      for (int i = 0; i < n; ++i) z[i] /= nn;
+    }
+    if (z[0] < 0.0)
+      for (int i = 0; i < n; ++i) z[i] = -z[i];
+  }
+  __syncwarp();
+  return theta;
+}
+
+// One ground-state solve per CTA.  S: storage/matvec precision of the
+// Krylov basis (double, or float for the FP32-mixed path); R: rows per
+// thread held in registers (N <= R * 512).
+template <typename S, int R>
+__global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* probs,
+                                                      const SmallUnit* units, SmallParams prm) {
+  __shared__ double s_alpha[kMaxM + 1], s_beta[kMaxM + 1], s_h[kMaxM + 1], s_z[kMaxM + 1];
+  __shared__ double s_part[kMaxM + 1][kWarpsCta];
+  __shared__ double s_red[kWarpsCta];
+  __shared__ double s_work[2 * kMaxM];
+  __shared__ double s_theta, s_resid;
+  __shared__ int s_flag;
+  const SmallUnit U = units[blockIdx.x];
+  const SmallProblem P = probs[U.prob];
+  const int N = P.N;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int m = (prm.m < N) ? prm.m : N;
+  S* V = reinterpret_cast<S*>(U.V);
+  const S cE = S(U.cE), cm = S(U.cm), ch = S(U.ch), cp = S(U.cp);
+  const bool fp32 = sizeof(S) == 4;
+  const double tiny_rel = fp32 ? 1e-6 : 1e-12;
+  const double tol = fp32 ? fmax(prm.tol, 2e-5) : prm.tol;
+
+  double w[R];  // this thread's rows of the current residual vector
+  // start vector: normal(seed, k) into V_0, normalised
+  double nrm = 0.0;
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int r = tid + i * kCta;
+    w[i] = (r < N) ? (prm.start_given ? U.psi[size_t(r) * U.psi_stride]
+                                      : start_normal(prm.seed, U.k, r))
+                   : 0.0;
+    nrm += w[i] * w[i];
+  }
+  nrm = sqrt(block_sum(nrm, s_red));
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int r = tid + i * kCta;
+    if (r < N) V[r] = S(w[i] / nrm);
+  }
+  __syncthreads();
+
+  int n = 0, restarts = 0, steps = 0;
+  bool converged = false;
+  double theta = 0.0, resid = 0.0;
+  for (int cycle = 0;; ++cycle) {
+    n = 0;
+    bool exhausted = false;
+    for (int j = 0; j < m; ++j) {
+      const S* vj = V + size_t(j) * N;
+      // w = H v_j (matvec in the storage precision)
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        const int r = tid + i * kCta;
+        if (r < N) {
+          S acc = (cE * S(P.e2[r]) + cm * S(P.stag[r])) * vj[r];
+          const int q1 = P.rowptr[r + 1];
+          for (int q = P.rowptr[r]; q < q1; ++q) {
+            const uint32_t e = __ldg(P.nbr + q);
+            const uint32_t kind = e & 3u;
+            const S c = (kind == kPlaq) ? cp : ((kind == kHopNeg) ? -ch : ch);
+            acc = fma(c, vj[e >> 2], acc);
+          }
+          w[i] = double(acc);
+        } else {
+          w[i] = 0.0;
+        }
+      }
+      // classical Gram-Schmidt against V_0..V_j, prm.reorth passes
+      for (int pass = 0; pass < prm.reorth; ++pass) {
+        for (int b = 0; b <= j; ++b) {
+          const S* vb = V + size_t(b) * N;
+          double p = 0.0;
+#pragma unroll
+          for (int i = 0; i < R; ++i) {
+            const int r = tid + i * kCta;
+            if (r < N) p = fma(double(vb[r]), w[i], p);
+          }
+          p = warp_sum(p);
+          if (lane == 0) s_part[b][wid] = p;
+        }
+        __syncthreads();
+        if (tid <= j) {
+          double s = 0.0;
+          for (int ww = 0; ww < kWarpsCta; ++ww) s += s_part[tid][ww];
+          s_h[tid] = s;
+          if (tid == j) s_alpha[j] = (pass == 0) ? s : s_alpha[j] + s;
+        }
+        __syncthreads();
+        for (int b = 0; b <= j; ++b) {
+          const double hb = s_h[b];
+          const S* vb = V + size_t(b) * N;
+#pragma unroll
+          for (int i = 0; i < R; ++i) {
+            const int r = tid + i * kCta;
+            if (r < N) w[i] = fma(-hb, double(vb[r]), w[i]);
+          }
+        }
+        __syncthreads();
+      }
+      double ss = 0.0;
+#pragma unroll
+      for (int i = 0; i < R; ++i) ss = fma(w[i], w[i], ss);
+      const double beta = sqrt(block_sum(ss, s_red));
+      if (tid == 0) s_beta[j] = beta;
+      n = j + 1;
+      ++steps;
+      double scl = fabs(s_alpha[j]);
+      if (j > 0) scl = fmax(scl, s_beta[j - 1]);
+      if (!(beta > tiny_rel * fmax(scl, 1.0))) {
+        exhausted = true;
+      } else if (j + 1 < m + 1) {
+        S* vn = V + size_t(j + 1) * N;
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+          const int r = tid + i * kCta;
+          if (r < N) vn[r] = S(w[i] / beta);
+        }
+      }
+      const bool check = exhausted || ((j + 1) % prm.check_every == 0) || (j + 1 == m);
+      if (check) {
+        __syncthreads();
+        if (wid == 0) {
+          const double th = warp_lowest_eig(s_alpha, s_beta, n, s_z, s_work);
+          if (lane == 0) {
+            const double rr = exhausted ? 0.0 : fabs(s_beta[n - 1] * s_z[n - 1]);
+            // FP32 panels resolve residuals to ~1e-6 |H|: relative floor
+            const double tl = fp32 ? fmax(tol, 3e-6 * fmax(fabs(th), 1.0)) : tol;
+            s_flag = (exhausted || rr <= tl) ? 1 : 0;
+            s_theta = th;
+            s_resid = rr;
+          }
+        }
+        __syncthreads();
+        theta = s_theta;
+        resid = s_resid;
+        if (s_flag) {
+          converged = true;
+          break;
+        }
+      } else {
+        __syncthreads();
+      }
+      if (exhausted) break;
+    }
+    // Ritz vector x = sum z_i V_i (z of the last check, at size n)
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int r = tid + i * kCta;
+      double xv = 0.0;
+      if (r < N)
+        for (int b = 0; b < n; ++b) xv = fma(s_z[b], double(V[size_t(b) * N + r]), xv);
+      w[i] = xv;
+    }
+    if (converged || cycle >= prm.maxiter) break;
+    // restart from the Ritz vector
+    double s2 = 0.0;
+#pragma unroll
+    for (int i = 0; i < R; ++i) s2 = fma(w[i], w[i], s2);
+    const double xn = sqrt(block_sum(s2, s_red));
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int r = tid + i * kCta;
+      if (r < N) V[r] = S(w[i] / xn);
+    }
+    __syncthreads();
+    ++restarts;
+  }
+
+  // FP64 finish: x normalised, y = H x in FP64, E = <x|y>, ||y - E x||
+  double s2 = 0.0;
+#pragma unroll
+  for (int i = 0; i < R; ++i) s2 = fma(w[i], w[i], s2);
+  const double xn = sqrt(block_sum(s2, s_red));
+  double* X = U.x;
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int r = tid + i * kCta;
+    w[i] /= xn;
+    if (r < N) X[r] = w[i];
+  }
+  __syncthreads();
+  double y[R];
+  double ey = 0.0;
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int r = tid + i * kCta;
+    y[i] = 0.0;
+    if (r < N) {
+      double acc = (U.cE * double(P.e2[r]) + U.cm * double(P.stag[r])) * X[r];
+      const int q1 = P.rowptr[r + 1];
+      for (int q = P.rowptr[r]; q < q1; ++q) {
+        const uint32_t e = __ldg(P.nbr + q);
+        const uint32_t kind = e & 3u;
+        const double c = (kind == kPlaq) ? U.cp : ((kind == kHopNeg) ? -U.ch : U.ch);
+        acc = fma(c, X[e >> 2], acc);
+      }
+      y[i] = acc;
+    }
+    ey = fma(w[i], y[i], ey);
+  }
+  const double Erq = block_sum(ey, s_red);
+  double rs = 0.0;
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const double d = y[i] - Erq * w[i];
+    rs = fma(d, d, rs);
+  }
+  const double rnorm = sqrt(block_sum(rs, s_red));
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int r = tid + i * kCta;
+    if (r < N) U.psi[size_t(r) * U.psi_stride] = w[i];
+  }
+  if (tid == 0) {
+    U.out[0] = fp32 ? Erq : theta;
+    U.out[1] = rnorm;
+    U.out[2] = double(steps);
+    U.out[3] = double(restarts);
+    U.out[4] = converged ? 1.0 : 0.0;
+    U.out[5] = resid;
+  }
+}
+
+template <typename S>
+cudaError_t launch_cta(const SmallProblem* probs, const SmallUnit* units, int nunits, int maxN,
+                       const SmallParams& prm, cudaStream_t s) {
+  const int R = (maxN + kCta - 1) / kCta;
+#define LGT_CTA_CASE(RR)                                                                  \
+  if (R <= RR) {                                                                          \
+    k_lanczos_cta<S, RR><<<nunits, kCta, 0, s>>>(probs, units, prm), lgt::note_launch(); \
+    return cudaGetLastError();                                                            \
+  }
+  LGT_CTA_CASE(1)
+  LGT_CTA_CASE(2)
+  LGT_CTA_CASE(4)
+  LGT_CTA_CASE(8)
+  LGT_CTA_CASE(16)
+#undef LGT_CTA_CASE
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+std::string build_pattern(const BasisDev& B, uint32_t model, Pattern* P, cudaStream_t s) {
+  const int64_t N = B.dim;
+  if (N > kSmallMaxN) return "sector too large for the per-CTA solver";
+  P->N = int(N);
+  P->model = model;
+  SCK(cudaMalloc(&P->rowptr, sizeof(int) * (N + 1)));
+  SCK(cudaMalloc(&P->e2, sizeof(int16_t) * (N + 1)));
+  SCK(cudaMalloc(&P->stag, sizeof(int16_t) * (N + 1)));
+  int* counts = nullptr;
+  SCK(cudaMalloc(&counts, sizeof(int) * (N + 1)));
+  const unsigned blocks = unsigned((N + 255) / 256);
+  const Geom& G = B.G;
+  const RankView R = B.view();
+  const bool plaq = model & kModelPlaq, jw = model & kModelJW;
+  if (plaq && jw) k_pattern_count<true, true><<<blocks, 256, 0, s>>>(G, R, N, counts), lgt::note_launch();
+  else if (plaq) k_pattern_count<true, false><<<blocks, 256, 0, s>>>(G, R, N, counts), lgt::note_launch();
+  else if (jw) k_pattern_count<false, true><<<blocks, 256, 0, s>>>(G, R, N, counts), lgt::note_launch();
+  else k_pattern_count<false, false><<<blocks, 256, 0, s>>>(G, R, N, counts), lgt::note_launch();
+  k_scan_rows<<<1, 1024, 0, s>>>(counts, N, P->rowptr), lgt::note_launch();
+  int nnz = 0;
+  SCK(cudaMemcpyAsync(&nnz, P->rowptr + N, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SCK(cudaStreamSynchronize(s));
+  P->nnz = nnz;
+  SCK(cudaMalloc(&P->nbr, sizeof(uint32_t) * (nnz + 1)));
+  if (plaq && jw)
+    k_pattern_fill<true, true><<<blocks, 256, 0, s>>>(G, R, N, P->rowptr, P->nbr, P->e2, P->stag, B.err), lgt::note_launch();
+  else if (plaq)
+    k_pattern_fill<true, false><<<blocks, 256, 0, s>>>(G, R, N, P->rowptr, P->nbr, P->e2, P->stag, B.err), lgt::note_launch();
+  else if (jw)
+    k_pattern_fill<false, true><<<blocks, 256, 0, s>>>(G, R, N, P->rowptr, P->nbr, P->e2, P->stag, B.err), lgt::note_launch();
+  else
+    k_pattern_fill<false, false><<<blocks, 256, 0, s>>>(G, R, N, P->rowptr, P->nbr, P->e2, P->stag, B.err), lgt::note_launch();
+  SCK(cudaGetLastError());
+  SCK(cudaFreeAsync(counts, s));
+  SCK(cudaStreamSynchronize(s));
+  return std::string();
+}
+
+void free_pattern(Pattern* P) {
+  cudaFree(P->rowptr);
+  cudaFree(P->nbr);
+  cudaFree(P->e2);
+  cudaFree(P->stag);
+  *P = Pattern();
+}
+
+std::string small_ground_states(const std::vector<SmallJob>& jobs, const SmallParams& prm,
+                                int mixed, SmallWork* ws, cudaStream_t s, double* seconds) {
+  // problems and units, the largest sectors first
+  std::vector<SmallProblem> probs;
+  std::vector<SmallUnit> units;
+  std::vector<int> order(jobs.size());
+  for (size_t i = 0; i < jobs.size(); ++i) order[i] = int(i);
+  std::vector<std::pair<int, int>> sz;
+  int maxN = 0;
+  size_t vbytes = 0, xbytes = 0;
+  const size_t es = mixed ? sizeof(float) : sizeof(double);
+  for (size_t i = 0; i < jobs.size(); ++i) {
+    const Pattern* P = jobs[i].pattern;
+    SmallProblem q;
+    q.N = P->N;
+    q.rowptr = P->rowptr;
+    q.nbr = P->nbr;
+    q.e2 = P->e2;
+    q.stag = P->stag;
+    probs.push_back(q);
+    if (P->N > maxN) maxN = P->N;
+    const int m = (prm.m < P->N) ? prm.m : P->N;
+    vbytes += size_t(jobs[i].K) * (size_t(m + 1) * P->N * es + 256);
+    xbytes += size_t(jobs[i].K) * (size_t(P->N) * sizeof(double) + 256);
+  }
+  if (maxN > kSmallMaxN) return "sector too large for the per-CTA solver";
+  if (prm.m > kMaxM - 1) return "krylovdim too large for the per-CTA solver";
+  size_t nunits = 0;
+  for (auto& j : jobs) nunits += size_t(j.K);
+  const size_t need = vbytes + xbytes + nunits * (sizeof(SmallUnit) + 8 * sizeof(double)) +
+                      probs.size() * sizeof(SmallProblem) + 4096;
+  if (ws->bytes < need) {
+    cudaFree(ws->base);
+    ws->base = nullptr;
+    ws->bytes = 0;
+    SCK(cudaMalloc(&ws->base, need));
+    ws->bytes = need;
+  }
+  char* base = static_cast<char*>(ws->base);
+  size_t off = 0;
+  auto take = [&](size_t b) {
+    char* p = base + off;
+    off += (b + 255) / 256 * 256;
+    return p;
+  };
+  SmallProblem* d_probs = reinterpret_cast<SmallProblem*>(take(probs.size() * sizeof(SmallProblem)));
+  SmallUnit* d_units = reinterpret_cast<SmallUnit*>(take(nunits * sizeof(SmallUnit)));
+  double* d_out = reinterpret_cast<double*>(take(nunits * 8 * sizeof(double)));
+  // units sorted by sector size, descending
+  std::vector<std::pair<int, size_t>> jorder;
+  for (size_t i = 0; i < jobs.size(); ++i) jorder.push_back({-jobs[i].pattern->N, i});
+  std::sort(jorder.begin(), jorder.end());
+  std::vector<std::pair<size_t, int>> unit_src;  // (job, k)
+  for (auto& jo : jorder) {
+    const SmallJob& J = jobs[jo.second];
+    const int N = J.pattern->N;
+    const int m = (prm.m < N) ? prm.m : N;
+    for (int k = 0; k < J.K; ++k) {
+      SmallUnit u;
+      u.prob = int(jo.second);
+      u.k = k;
+      u.cE = J.cE[k];
+      u.cm = J.cm[k];
+      u.ch = J.ch[k];
+      u.cp = J.cp[k];
+      u.psi = J.psi + k;
+      u.psi_stride = J.K;
+      u.V = take(size_t(m + 1) * N * es);
+      u.x = reinterpret_cast<double*>(take(size_t(N) * sizeof(double)));
+      u.out = d_out + units.size() * 8;
+      units.push_back(u);
+      unit_src.push_back({jo.second, k});
+    }
+  }
+  SCK(cudaMemcpyAsync(d_probs, probs.data(), sizeof(SmallProblem) * probs.size(),
+                      cudaMemcpyHostToDevice, s));
+  SCK(cudaMemcpyAsync(d_units, units.data(), sizeof(SmallUnit) * units.size(),
+                      cudaMemcpyHostToDevice, s));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, s);
+  cudaError_t e = mixed ? launch_cta<float>(d_probs, d_units, int(nunits), maxN, prm, s)
+                        : launch_cta<double>(d_probs, d_units, int(nunits), maxN, prm, s);
+  cudaEventRecord(e1, s);
+  if (e != cudaSuccess) return std::string("k_lanczos_cta: ") + cudaGetErrorString(e);
+  std::vector<double> out(nunits * 8);
+  SCK(cudaMemcpyAsync(out.data(), d_out, sizeof(double) * out.size(), cudaMemcpyDeviceToHost, s));
+  SCK(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (seconds) *seconds = ms * 1e-3;
+  for (size_t u = 0; u < nunits; ++u) {
+    const SmallJob& J = jobs[unit_src[u].first];
+    const int k = unit_src[u].second;
+    J.E0[k] = out[u * 8 + 0];
+    if (J.resid) J.resid[k] = out[u * 8 + 1];
+    if (J.steps) J.steps[k] = int(out[u * 8 + 2]);
+    if (J.restarts) J.restarts[k] = int(out[u * 8 + 3]);
+    if (J.converged) J.converged[k] = out[u * 8 + 4] != 0.0;
+  }
+  return std::string();
+}
+
+}  // namespace lgt

@@ -367,9 +367,13 @@ def build_hamiltonian(states: Basis, key_dict=None, nx=None, ny=None, dg=None, *
 # solvers and observables
 # ---------------------------------------------------------------------------
 
+_SOLVERS = {"auto": C.LGT_SOLVER_AUTO, "panel": C.LGT_SOLVER_PANEL, "cta": C.LGT_SOLVER_CTA}
+
+
 def _opts(for_exp, tol, krylovdim, maxiter, precision, seed, check_every, refine_steps,
-          use_graph=True, start_given=False, reorth_passes=2):
+          use_graph=True, start_given=False, reorth_passes=2, solver="auto"):
     o = C.defaults(for_exp)
+    o.solver = _SOLVERS[solver]
     if tol is not None:
         o.tol = tol
     if krylovdim is not None:
@@ -389,7 +393,7 @@ def _opts(for_exp, tol, krylovdim, maxiter, precision, seed, check_every, refine
 
 def find_ground_state(H: Hamiltonian, *, tol=1e-10, krylovdim=50, maxiter=300, precision="fp64",
                       seed=0, v0=None, check_every=None, refine_steps=0, use_graph=True,
-                      as_complex=True, return_info=False):
+                      solver="auto", as_complex=True, return_info=False):
     """find_ground_state (finite_ed.jl:333-341): lowest eigenpair by Lanczos
     (full reorthogonalisation, restarts), on the GPU.  Defaults are the
     reference's eigsolve settings.  For K = 1 returns (E0: float, psi: [N]);
@@ -397,10 +401,12 @@ def find_ground_state(H: Hamiltonian, *, tol=1e-10, krylovdim=50, maxiter=300, p
     part, like the reference's ComplexF64 vector) unless as_complex=False.
     precision "fp32_mixed": FP32 H*psi and Krylov storage, FP64 dots,
     reorthogonalisation and tridiagonal solve; E0 is the FP64 Rayleigh
-    quotient.  Raises NotConverged like the reference's @assert (:339)."""
+    quotient.  solver: "auto" (one CTA per point for sectors up to 8192
+    states, else K-interleaved panels), "cta" or "panel".  Raises
+    NotConverged like the reference's @assert (:339)."""
     N, K = H.basis.dim, H.K
     o = _opts(False, tol, krylovdim, maxiter, precision, seed, check_every, refine_steps,
-              use_graph, v0 is not None)
+              use_graph, v0 is not None, solver=solver)
     psi = np.zeros((N, K), np.float64)
     if v0 is not None:
         v = np.asarray(v0)
@@ -420,6 +426,46 @@ def find_ground_state(H: Hamiltonian, *, tol=1e-10, krylovdim=50, maxiter=300, p
                       "restarts": info.restarts, "converged": info.converged,
                       "max_residual": info.max_residual, "seconds": info.seconds}
     return E, P
+
+
+def find_ground_states(Hs, *, tol=1e-10, krylovdim=50, maxiter=300, precision="fp64", seed=0,
+                       check_every=None, solver="auto", device_psi=None, return_info=False):
+    """Ground states of several Hamiltonians (lattices, sectors, coupling
+    grids) in one call: every (H, point) pair of a sector up to 8192 states
+    runs in one persistent launch, one CTA each (uneven batch), larger
+    sectors through the panel solver.  Returns a list of (E0 [K], psi
+    [N, K]) per Hamiltonian (psi as float64 host arrays, or None when
+    ``device_psi`` gives device panels: a list of device pointers)."""
+    import torch  # device panels for the batch
+    n = len(Hs)
+    o = _opts(False, tol, krylovdim, maxiter, precision, seed, check_every, 0, True, False,
+              solver=solver)
+    E0s = [np.zeros(H.K) for H in Hs]
+    res = [np.zeros(H.K) for H in Hs]
+    if device_psi is None:
+        panels = [torch.zeros((H.basis.dim, H.K), dtype=torch.float64,
+                              device="cuda:%d" % _device_of(H)) for H in Hs]
+        ptrs = [p.data_ptr() for p in panels]
+    else:
+        panels, ptrs = None, list(device_psi)
+    arr_h = (ctypes.c_void_p * n)(*[H.handle.value for H in Hs])
+    arr_e = (ctypes.c_void_p * n)(*[e.ctypes.data for e in E0s])
+    arr_p = (ctypes.c_void_p * n)(*ptrs)
+    arr_r = (ctypes.c_void_p * n)(*[r.ctypes.data for r in res])
+    info = C.Info()
+    C.check(C.load().lgt_ground_state_batch(n, arr_h, ctypes.byref(o), arr_e, arr_p, arr_r,
+                                            C.LGT_DEVICE_PTRS, ctypes.byref(info)))
+    out = [(E0s[i], panels[i].cpu().numpy() if panels is not None else None) for i in range(n)]
+    if return_info:
+        return out, {"residual": res, "matvecs": info.matvecs, "restarts": info.restarts,
+                     "converged": info.converged, "max_residual": info.max_residual,
+                     "seconds": info.seconds}
+    return out
+
+
+def _device_of(H):
+    import torch
+    return torch.cuda.current_device()
 
 
 def ite_ground_state_ED(states, key_dict, nx, ny, dg, *, g, t, m, model="ref", **kw):

@@ -201,11 +201,16 @@ def order_key(nx, ny, dg, nf, eU) -> int:
     return (mask << (w * nx * (ny - 1))) | dig
 
 
-def py_build_basis(nx: int, ny: int, dg: int, g_charges):
+def py_build_basis(nx: int, ny: int, dg: int, g_charges, dedup: str = "encode"):
     """Literal pure-Python restatement of build_basis and its recursion
     (finite_ed.jl:125-232), for tiny lattices.  Returns the list of
     (n_f, e_R, e_U) int arrays in reference index order and the list of
-    _encode keys (finite_ed.jl:80-97) as signed Int64 values."""
+    _encode keys (finite_ed.jl:80-97) as signed Int64 values.
+
+    dedup="encode" keys the dictionary by _encode exactly as the reference
+    does (finite_ed.jl:227-228); for dg > 1 its 2-bit fields collide and
+    states are silently dropped.  dedup="config" keys it by the whole
+    configuration, which is what the oracle and the GPU library define."""
     g = np.asarray(g_charges, dtype=np.int64).reshape(nx, ny)
     nft = -int(g.sum())
     assert 0 <= nft <= nx * ny, "Inconsistent sector"
@@ -246,10 +251,11 @@ def py_build_basis(nx: int, ny: int, dg: int, g_charges):
                 elif acc != 0:
                     return
         k = encode(n_f, e_R, e_U)
-        if k not in key_dict:
+        dk = k if dedup == "encode" else (n_f.tobytes(), e_R.tobytes(), e_U.tobytes())
+        if dk not in key_dict:
             states.append((n_f.copy(), e_R.copy(), e_U.copy()))
             keys.append(k)
-            key_dict[k] = len(states) - 1
+            key_dict[dk] = len(states) - 1
 
     def eU_row(q, S, iy):
         if iy == ny - 1:

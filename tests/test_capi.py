@@ -1,0 +1,97 @@
+"""CPU tests of the C ABI boundary: the library builds for sm_103a, loads,
+exports every symbol include/lgt_ed.h declares, and its argument checks and
+error codes behave without a GPU (no compute call is made here)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_symbols():
+    src = open(os.path.join(ROOT, "include", "lgt_ed.h")).read()
+    return sorted(set(re.findall(r"LGT_API[^;{]*?\b(lgt_[a-z_0-9]+)\s*\(", src, re.S)))
+
+
+def test_header_lists_the_python_binding():
+    from lgt_gb300 import _capi
+    assert header_symbols() == sorted(_capi.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol():
+    from lgt_gb300 import _capi
+    path = _capi.library_path()
+    _capi.load()
+    lib = ctypes.CDLL(path)
+    for name in header_symbols():
+        assert hasattr(lib, name), name
+
+
+def test_library_is_sm_103a_only():
+    from lgt_gb300 import build
+    assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def test_defaults_are_the_reference_settings():
+    from lgt_gb300 import _capi as C
+    o = C.defaults(False)
+    assert (o.krylovdim, o.maxiter, o.tol) == (50, 300, 1e-10)   # finite_ed.jl:336-338
+    o = C.defaults(True)
+    assert (o.krylovdim, o.maxiter, o.tol) == (30, 100, 1e-10)   # finite_ed.jl:417-419
+
+
+def _create(nx, ny, dg, g):
+    from lgt_gb300 import _capi as C
+    lib = C.load()
+    h = ctypes.c_void_p()
+    gf = np.asfortranarray(np.asarray(g, np.int32).reshape(max(nx, 1), max(ny, 1)))
+    code = lib.lgt_basis_create(nx, ny, dg, gf.ctypes.data_as(ctypes.c_void_p), -1,
+                                ctypes.byref(h))
+    return code, lib.lgt_last_error().decode()
+
+
+def test_inconsistent_sector_is_a_status_not_an_abort():
+    from lgt_gb300 import _capi as C
+    g = np.zeros((3, 2), np.int32)
+    g[0, 0] = 2  # N_f = -2  (finite_ed.jl:127 @assert)
+    code, msg = _create(3, 2, 1, g)
+    assert code == C.LGT_ERR_SECTOR and "Inconsistent sector" in msg
+    g[0, 0] = -7  # N_f = 7 > 6 sites
+    assert _create(3, 2, 1, g)[0] == C.LGT_ERR_SECTOR
+
+
+def test_key_width_and_range_checks():
+    from lgt_gb300 import _capi as C
+    assert _create(6, 6, 1, np.zeros((6, 6)))[0] == C.LGT_ERR_KEYWIDTH   # 36 sites
+    assert _create(5, 5, 1, np.zeros((5, 5)))[0] == C.LGT_ERR_KEYWIDTH   # 25 + 2*20 > 64 bits
+    assert _create(3, 3, 9, np.zeros((3, 3)))[0] == C.LGT_ERR_ARG        # dg out of range
+    assert _create(0, 3, 1, np.zeros((1, 3)))[0] == C.LGT_ERR_ARG
+
+
+def test_null_arguments():
+    from lgt_gb300 import _capi as C
+    lib = C.load()
+    assert lib.lgt_basis_dim(None, None) == C.LGT_ERR_ARG
+    assert lib.lgt_ham_create(None, 1, None, None, None, 0, None) == C.LGT_ERR_ARG
+    assert lib.lgt_matvec(None, None, None, 1, 0, 0) == C.LGT_ERR_ARG
+    assert lib.lgt_launch_count(None) == C.LGT_ERR_ARG
+    n = ctypes.c_uint64()
+    assert lib.lgt_launch_count(ctypes.byref(n)) == C.LGT_OK
+    assert b"sm_103a" in lib.lgt_version()
+
+
+def test_python_encode_matches_oracle(oracle):
+    import lgt_gb300 as L
+    b = oracle.build_basis(4, 3, 1, oracle.staggered_charges(4, 3))
+    for i in range(0, b.dim, 997):
+        assert L.encode(b.nf[i], b.eR[i], b.eU[i]) == int(b.ref_keys[i])
+
+
+def test_sector_helpers_match_oracle(oracle):
+    import lgt_gb300 as L
+    for nx, ny in [(3, 2), (4, 4), (3, 4)]:
+        assert np.array_equal(L.staggered_charges(nx, ny), oracle.staggered_charges(nx, ny))
+        assert np.array_equal(L.string_charges(nx, ny), oracle.string_charges(nx, ny))

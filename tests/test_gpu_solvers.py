@@ -1,0 +1,86 @@
+"""GPU tests of the two ground-state solvers (one CTA per point, and
+K-interleaved panels) and of the uneven multi-lattice batch, against the
+FP64 oracle.  Tolerances: |dE|/|E| <= 1e-10 (FP64 and FP32-mixed),
+observables 1e-9 absolute (FP64), eigenvector 1e-9/gap."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _basis(O, L, nx, ny, kind="stag"):
+    g = O.staggered_charges(nx, ny) if kind == "stag" else O.string_charges(nx, ny)
+    return O.build_basis(nx, ny, 1, g), L.build_basis(nx, ny, 1, g)[0]
+
+
+@pytest.mark.parametrize("solver", ["cta", "panel"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32_mixed"])
+@pytest.mark.parametrize("nx,ny,model", [(3, 2, "ref"), (4, 2, "pjw"), (3, 3, "ref"),
+                                          (2, 4, "pjw"), (2, 2, "ref")])
+def test_solver_vs_oracle(oracle, lgt, solver, precision, nx, ny, model):
+    ob, gb = _basis(oracle, lgt, nx, ny)
+    gs = np.array([0.55, 1.0, 1.9])
+    ms = np.array([0.5, 0.1, 0.8])
+    H = lgt.build_hamiltonian(gb, g=gs, t=1.0, m=ms, model=model)
+    E0, psi, info = lgt.find_ground_state(H, tol=1e-12, precision=precision, solver=solver,
+                                          as_complex=False, return_info=True)
+    obs = lgt.measure_ED(psi, gb)
+    for k in range(3):
+        Ho = oracle.build_hamiltonian(ob, g=gs[k], t=1.0, m=ms[k], model=model)
+        E0o, psio = oracle.ground_state(Ho)
+        assert abs(E0[k] - E0o) <= 1e-10 * abs(E0o), (k, E0[k], E0o)
+        if precision == "fp64":
+            gap = np.diff(oracle.spectrum_low(Ho, 2))[0]
+            if gap > 1e-3:
+                v = psi[:, k] * np.sign(np.dot(psi[:, k], psio))
+                assert np.linalg.norm(v - psio) <= 1e-9 / min(gap, 1.0)
+                mo = oracle.measure(psio, ob)
+                for key in ("E2_mean", "plaq_mean", "nf_even", "nf_odd", "n_stag"):
+                    assert abs(obs[k][key] - mo[key]) <= 1e-9, key
+        assert info["residual"][k] <= (1e-11 if precision == "fp64" else 1e-3)
+    H.close()
+
+
+def test_cta_and_panel_agree(oracle, lgt):
+    ob, gb = _basis(oracle, lgt, 4, 2)
+    gs = np.linspace(0.5, 2.0, 16)
+    H = lgt.build_hamiltonian(gb, g=gs, t=1.0, m=0.5, model="pjw")
+    Ec, pc = lgt.find_ground_state(H, tol=1e-12, solver="cta", as_complex=False)
+    Ep, pp = lgt.find_ground_state(H, tol=1e-12, solver="panel", as_complex=False)
+    np.testing.assert_allclose(Ec, Ep, rtol=1e-12, atol=0)
+    ov = np.abs(np.sum(pc * pp, axis=0))
+    assert np.all(ov > 1 - 1e-12)
+    H.close()
+
+
+def test_uneven_batch_one_launch(oracle, lgt):
+    """3x2, 4x2, 3x3 (one persistent launch, one CTA per point) and 4x3
+    (panel solver), 4 (g, m) points each, FP32-mixed."""
+    rng = np.random.default_rng(0)
+    Hs, obs = [], []
+    for nx, ny in [(3, 2), (4, 2), (3, 3), (4, 3)]:
+        ob, gb = _basis(oracle, lgt, nx, ny)
+        g = np.exp(rng.uniform(np.log(0.3), np.log(3.0), 4))
+        m = rng.uniform(0.0, 1.0, 4)
+        Hs.append(lgt.build_hamiltonian(gb, g=g, t=1.0, m=m, model="ref"))
+        obs.append((ob, g, m))
+    res = lgt.find_ground_states(Hs, precision="fp32_mixed")
+    for (E0, psi), (ob, g, m) in zip(res, obs):
+        for k in range(4):
+            E0o = oracle.ground_state(oracle.build_hamiltonian(ob, g=g[k], t=1.0, m=m[k]))[0]
+            assert abs(E0[k] - E0o) <= 1e-10 * abs(E0o)
+        assert psi.shape == (ob.dim, 4)
+    for H in Hs:
+        H.close()
+
+
+def test_string_sector_and_start_vector(oracle, lgt):
+    """Quench-A sector; a given start vector (the string state) converges to
+    the same ground state."""
+    ob, gb = _basis(oracle, lgt, 3, 4, "string")
+    H = lgt.build_hamiltonian(gb, g=1.0, t=1.0, m=2.0)
+    v0 = lgt.string_state(gb)
+    E0, psi = lgt.find_ground_state(H, tol=1e-12, v0=v0.real)
+    E0o = oracle.ground_state(oracle.build_hamiltonian(ob, g=1.0, t=1.0, m=2.0))[0]
+    assert abs(E0 - E0o) <= 1e-10 * abs(E0o)
+    H.close()
