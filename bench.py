@@ -263,6 +263,43 @@ def gpu_workloads(args, rank, world):
                 matvecs_mix=info_mix.matvecs, restarts_mix=info_mix.restarts)
 
 
+def gs_only(args):
+    """The headline loop alone (device panels, no CPU pool, no sampler)."""
+    import torch
+
+    import lgt_gb300 as L
+    from lgt_gb300 import _capi as C
+    torch.cuda.set_device(0)
+    lib = C.load()
+    stream = torch.cuda.Stream()
+    states, key_dict = L.build_basis(NX, NY, DG, L.staggered_charges(NX, NY), device=0)
+    C.check(lib.lgt_basis_set_stream(states.handle, ctypes_ptr(stream.cuda_stream)))
+    H = L.build_hamiltonian(states, key_dict, NX, NY, DG, g=points(0), t=T_HOP, m=MASS)
+    psi = torch.zeros((len(states), KPTS), dtype=torch.float64, device="cuda")
+    o = C.defaults(False)
+    o.precision = C.LGT_FP32_MIXED
+    E0 = np.zeros(KPTS)
+    info = C.Info()
+    summ = (C.Obs * KPTS)()
+    ts = []
+    for it in range(args.warmup + args.steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            C.check(lib.lgt_ground_state(H.handle, o, E0.ctypes.data, psi.data_ptr(), None,
+                                         C.LGT_DEVICE_PTRS, info))
+            C.check(lib.lgt_observe(H.handle, psi.data_ptr(), 1, C.LGT_FP64, C.LGT_DEVICE_PTRS,
+                                    0.0, None, None, None, summ))
+            e1.record(stream)
+        e1.synchronize()
+        if it >= args.warmup:
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+    H.close()
+    states.close()
+    return {"gs_per_s": KPTS / statistics.mean(ts), "ms_per_step": 1e3 * statistics.mean(ts)}
+
+
 def ctypes_ptr(v):
     import ctypes
     return ctypes.c_void_p(v)
@@ -321,8 +358,9 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--part", default="all", choices=["all", "hpsi"],
-                    help="hpsi: only the 4x4 H*psi roofline loop (for profiling)")
+    ap.add_argument("--part", default="all", choices=["all", "hpsi", "gs"],
+                    help="hpsi: only the 4x4 H*psi roofline loop; gs: only the headline "
+                         "ground-state loop (both for profiling: no child processes)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank = int(os.environ.get("RANK", "0"))
@@ -356,6 +394,10 @@ def main():
                                        "(C basis + H, scipy ARPACK eigsh tol 1e-10 ncv 50)"},
             "e2e": {"value": val, "unit": "GS/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}))
+        return
+
+    if args.part == "gs":
+        print(json.dumps({"part": "gs", **gs_only(args)}))
         return
 
     if args.part == "hpsi":

@@ -16,6 +16,7 @@
 #include "lgt_krylov.h"
 #include "lgt_observe.h"
 #include "lgt_small.h"
+#include "lgt_handles.h"
 
 using namespace lgt;
 
@@ -48,26 +49,6 @@ lgt_status from_msg(const std::string& m) {
     if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
   } while (0)
 
-// Device buffer owned by a handle, grown on demand.
-struct DevBuf {
-  void* p = nullptr;
-  size_t bytes = 0;
-  cudaError_t need(size_t b) {
-    if (b <= bytes) return cudaSuccess;
-    cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-    cudaError_t e = cudaMalloc(&p, b);
-    if (e == cudaSuccess) bytes = b;
-    return e;
-  }
-  void release() {
-    cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-  }
-};
-
 }  // namespace
 
 namespace lgt {
@@ -77,43 +58,6 @@ void note_launch(int n) {
 void set_capturing(bool on) { g_capturing = on; }
 }  // namespace lgt
 
-struct lgt_basis {
-  BasisDev B;
-  int device = 0;
-  cudaStream_t own_stream = nullptr;
-};
-
-struct lgt_ham {
-  const lgt_basis* b = nullptr;
-  int K = 0;
-  uint32_t model = 0;
-  std::vector<double> g, t, m;
-  double* coef_d = nullptr;  // [4][K]: g^2/2, m, -t, -1/(2g^2)
-  float* coef_f = nullptr;
-  int seg_smem = 0;
-  KrylovCache* cache = nullptr;
-  DevBuf x, y, part, out;
-  Pattern pattern;          // lookup pass of the per-CTA solver (built on demand)
-  SmallWork small;
-  OpDev op() const {
-    OpDev o;
-    o.G = b->B.G;
-    o.R = b->B.view();
-    o.err = b->B.err;
-    o.model = model;
-    o.K = K;
-    o.seg_smem = seg_smem;
-    o.cE_d = coef_d;
-    o.cm_d = coef_d + K;
-    o.ch_d = coef_d + 2 * K;
-    o.cp_d = coef_d + 3 * K;
-    o.cE_f = coef_f;
-    o.cm_f = coef_f + K;
-    o.ch_f = coef_f + 2 * K;
-    o.cp_f = coef_f + 3 * K;
-    return o;
-  }
-};
 
 namespace {
 
@@ -726,9 +670,9 @@ lgt_status lgt_ground_state_batch(int32_t nham, lgt_ham* const* hams, const lgt_
 
 }  // extern "C"
 
-namespace {
+void lgt::set_last_error(const std::string& msg) { g_last_error = msg; }
 
-void summarize(const Geom& G, const double* feat, double t_now, lgt_obs* o) {
+void lgt::summarize_obs(const Geom& G, const double* feat, double t_now, lgt_obs* o) {
   // measure_ED's means (finite_ed.jl:387-390) plus plaquette / staggered density
   const int ns = G.ns;
   double nf = 0, e2 = 0, ne = 0, no = 0, st = 0, pl = 0;
@@ -758,6 +702,8 @@ void summarize(const Geom& G, const double* feat, double t_now, lgt_obs* o) {
   o->n_stag = st / ns;
   o->norm2 = feat[2 * ns + G.nP];
 }
+
+namespace {
 
 template <typename T>
 lgt_status observe_dev(lgt_ham* h, const T* x, int ncomp, std::vector<double>* feat) {
@@ -790,7 +736,7 @@ struct ObsRecorder : StepObserver {
     if (observe_dev<double>(h, X, 2, &feat) != LGT_OK) return std::string(lgt_last_error());
     const int nf = observe_nfeat(h->b->B.G);
     for (int k = 0; k < h->K; ++k)
-      summarize(h->b->B.G, feat.data() + size_t(k) * nf, step * dt, obs + size_t(step) * h->K + k);
+      summarize_obs(h->b->B.G, feat.data() + size_t(k) * nf, step * dt, obs + size_t(step) * h->K + k);
     return std::string();
   }
 };
@@ -872,7 +818,7 @@ lgt_status lgt_observe(const lgt_ham* hc, const void* psi, int32_t ncomp, int32_
     if (E2_grid) std::memcpy(E2_grid + size_t(k) * G.ns, f + G.ns, sizeof(double) * G.ns);
     if (plaq_grid && G.nP)
       std::memcpy(plaq_grid + size_t(k) * G.nP, f + 2 * G.ns, sizeof(double) * G.nP);
-    if (summary) summarize(G, f, t_now, summary + k);
+    if (summary) summarize_obs(G, f, t_now, summary + k);
   }
   return check_device_errors(h->b);
 }

@@ -1,0 +1,87 @@
+// lgt_handles.h -- definitions of the opaque C-ABI handles (shared by the
+// translation units that implement entry points).
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "../../include/lgt_ed.h"
+#include "lgt_internal.h"
+#include "lgt_krylov.h"
+#include "lgt_small.h"
+
+namespace lgt {
+
+// Device buffer owned by a handle, grown on demand.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t need(size_t b) {
+    if (b <= bytes) return cudaSuccess;
+    cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e == cudaSuccess) bytes = b;
+    return e;
+  }
+  void release() {
+    cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+
+// Sets the calling thread's lgt_last_error() message.
+void set_last_error(const std::string& msg);
+
+// measure_ED's means (finite_ed.jl:387-390) plus plaquette and staggered
+// density, from the per-point feature vector of the observables kernel.
+void summarize_obs(const Geom& G, const double* feat, double t_now, lgt_obs* o);
+
+}  // namespace lgt
+
+struct lgt_basis {
+  using BasisDev = lgt::BasisDev;
+  BasisDev B;
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+};
+
+struct lgt_ham {
+  using DevBuf = lgt::DevBuf;
+  using KrylovCache = lgt::KrylovCache;
+  using Pattern = lgt::Pattern;
+  using SmallWork = lgt::SmallWork;
+  using OpDev = lgt::OpDev;
+  const lgt_basis* b = nullptr;
+  int K = 0;
+  uint32_t model = 0;
+  std::vector<double> g, t, m;
+  double* coef_d = nullptr;  // [4][K]: g^2/2, m, -t, -1/(2g^2)
+  float* coef_f = nullptr;
+  int seg_smem = 0;
+  KrylovCache* cache = nullptr;
+  DevBuf x, y, part, out;
+  Pattern pattern;          // lookup pass of the per-CTA solver (built on demand)
+  SmallWork small;
+  OpDev op() const {
+    OpDev o;
+    o.G = b->B.G;
+    o.R = b->B.view();
+    o.err = b->B.err;
+    o.model = model;
+    o.K = K;
+    o.seg_smem = seg_smem;
+    o.cE_d = coef_d;
+    o.cm_d = coef_d + K;
+    o.ch_d = coef_d + 2 * K;
+    o.cp_d = coef_d + 3 * K;
+    o.cE_f = coef_f;
+    o.cm_f = coef_f + K;
+    o.ch_f = coef_f + 2 * K;
+    o.cp_f = coef_f + 3 * K;
+    return o;
+  }
+};
