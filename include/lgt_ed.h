@@ -242,6 +242,22 @@ LGT_API lgt_status lgt_observe(const lgt_ham* h, const void* psi, int32_t ncomp,
                        uint32_t flags, double t_now, double* nf_grid, double* E2_grid,
                        double* plaq_grid, lgt_obs* summary);
 
+/* lgt_observe without any device allocation.  No counterpart in the
+   reference (finite_ed.jl measures on the host); it exists for callers that
+   cannot call cudaMalloc: applications that reserve all device memory for
+   their own pool, and loops that must not trigger the device
+   synchronisation an allocation can cause.  psi must be a device panel
+   [N][K][ncomp] on the basis' device (the LGT_DEVICE_PTRS form of
+   lgt_observe); outputs are host arrays as in lgt_observe.  Its scratch is a
+   fixed 2 MiB static device array per GPU: calls whose K * (2 nx ny +
+   (nx-1)(ny-1) + 1) doubles per block do not fit are rejected with
+   LGT_ERR_ARG.  All calls share that array, so calls that overlap on the GPU
+   race.  The first call on a device looks up the array's address (make it
+   before any stream capture on that device). */
+LGT_API lgt_status lgt_observe_noalloc(const lgt_ham* h, const void* psi, int32_t ncomp,
+                                       int32_t precision, double t_now, double* nf_grid,
+                                       double* E2_grid, double* plaq_grid, lgt_obs* summary);
+
 /* Energy <psi|H|psi> / <psi|psi> per point, FP64 (finite_ed.jl has no
    counterpart; used for energy-drift reports of evolve_ED!). */
 LGT_API lgt_status lgt_energy(const lgt_ham* h, const void* psi, int32_t ncomp, uint32_t flags,

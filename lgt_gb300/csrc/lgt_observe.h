@@ -16,4 +16,11 @@ template <typename T>
 cudaError_t launch_observe(const Geom& G, const RankView& R, const T* x, int K, int ncomp,
                            double* part, double* out, int* err, cudaStream_t s);
 
+// Same reduction with a caller-chosen block partition (nblk blocks of rpb
+// rows; part must hold nblk * K * nfeat doubles).
+template <typename T>
+cudaError_t launch_observe_planned(const Geom& G, const RankView& R, const T* x, int K, int ncomp,
+                                   int nblk, int64_t rpb, double* part, double* out, int* err,
+                                   cudaStream_t s);
+
 }  // namespace lgt

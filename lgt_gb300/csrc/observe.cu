@@ -192,6 +192,28 @@ cudaError_t launch_observe(const Geom& G, const RankView& R, const T* x, int K, 
   return cudaGetLastError();
 }
 
+template <typename T>
+cudaError_t launch_observe_planned(const Geom& G, const RankView& R, const T* x, int K, int ncomp,
+                                   int nblk, int64_t rpb, double* part, double* out, int* err,
+                                   cudaStream_t s) {
+  if (K > kT || nblk < 1 || rpb < 1) return cudaErrorInvalidValue;
+  const int nfeat = observe_nfeat(G);
+  if (nfeat > 96) return cudaErrorInvalidValue;
+  cudaError_t e = (ncomp == 1)
+                      ? launch_obs2<T, 1>(G, R, x, K, nfeat, nblk, rpb, part, err, s)
+                      : launch_obs2<T, 2>(G, R, x, K, nfeat, nblk, rpb, part, err, s);
+  if (e != cudaSuccess) return e;
+  k_observe_finish<<<(K * nfeat + 127) / 128, 128, 0, s>>>(part, nblk, K, nfeat, out), lgt::note_launch();
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_observe_planned<double>(const Geom&, const RankView&, const double*,
+                                                    int, int, int, int64_t, double*, double*, int*,
+                                                    cudaStream_t);
+template cudaError_t launch_observe_planned<float>(const Geom&, const RankView&, const float*, int,
+                                                   int, int, int64_t, double*, double*, int*,
+                                                   cudaStream_t);
+
 template cudaError_t launch_observe<double>(const Geom&, const RankView&, const double*, int, int,
                                             double*, double*, int*, cudaStream_t);
 template cudaError_t launch_observe<float>(const Geom&, const RankView&, const float*, int, int,
