@@ -70,16 +70,20 @@ __global__ void k_randn(S* out, int64_t N, int C, int ncomp, uint64_t seed) {
 // Per-block partial dot products of W against V_0..V_{J-1}:
 // part[blk][i][0][c] = sum_rows V_i[row][c] W[row][c]
 // part[blk][i][1][c] = sum_rows V_i[row][c] W[row][c^1]   (complex only)
+// With self = 1, index J holds W against itself (its squared norm).  Columns
+// of points with need[k] == 0 contribute zero (need may be null).
 template <typename S, int NC>
 __global__ void __launch_bounds__(kT) k_multidot(const S* __restrict__ V, size_t vstride,
                                                  const int* jstate, int jfixed,
                                                  const S* __restrict__ W, int64_t N, int C,
-                                                 int64_t rpb, double* part, int Jmax) {
+                                                 int64_t rpb, double* part, int Jmax,
+                                                 int self, const int* need, int ncomp) {
   extern __shared__ double red[];  // [RG][kIC][2][C]
-  const int J = jstate ? (*jstate + 1) : jfixed;
+  const int Jv = jstate ? (*jstate + 1) : jfixed;
+  const int J = Jv + self;
   const int RG = kT / C;
   const int c = threadIdx.x % C, rg = threadIdx.x / C;
-  const bool act = rg < RG;
+  const bool act = rg < RG && (!need || need[c / ncomp] != 0);
   const int64_t r0 = int64_t(blockIdx.x) * rpb;
   const int64_t r1 = (r0 + rpb < N) ? r0 + rpb : N;
   for (int i0 = 0; i0 < J; i0 += kIC) {
@@ -94,7 +98,7 @@ __global__ void __launch_bounds__(kT) k_multidot(const S* __restrict__ V, size_t
 #pragma unroll
         for (int q = 0; q < kIC; ++q) {
           if (i0 + q < J) {
-            const double v = double(V[size_t(i0 + q) * vstride + off + c]);
+            const double v = (i0 + q < Jv) ? double(V[size_t(i0 + q) * vstride + off + c]) : w;
             a[q] = fma(v, w, a[q]);
             if (NC == 2) b[q] = fma(v, wx, b[q]);
           }
@@ -104,6 +108,12 @@ __global__ void __launch_bounds__(kT) k_multidot(const S* __restrict__ V, size_t
       for (int q = 0; q < kIC; ++q) {
         red[((rg * kIC + q) * 2 + 0) * C + c] = a[q];
         red[((rg * kIC + q) * 2 + 1) * C + c] = b[q];
+      }
+    } else if (rg < RG) {
+#pragma unroll
+      for (int q = 0; q < kIC; ++q) {
+        red[((rg * kIC + q) * 2 + 0) * C + c] = 0.0;
+        red[((rg * kIC + q) * 2 + 1) * C + c] = 0.0;
       }
     }
     __syncthreads();
@@ -118,13 +128,14 @@ __global__ void __launch_bounds__(kT) k_multidot(const S* __restrict__ V, size_t
 }
 
 // h[i][k] = <V_i, W>_k (complex for NC = 2), summed over blocks in order.
-// alpha_j of active points accumulates Re h_j (first pass sets it).
+// alpha_j of active points accumulates Re h_j (first pass sets it).  With
+// self = 1 the extra dot (W against itself) goes to nb[k].
 __global__ void k_finish_dots(const double* part, int nblk, int Jmax, const int* jstate,
                               int jfixed, int K, int C, int ncomp, double* h, double* alpha,
-                              int ldT, int first_pass, const int* status) {
+                              int ldT, int first_pass, const int* status, int self, double* nb) {
   const int J = jstate ? (*jstate + 1) : jfixed;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= J * K) return;
+  if (t >= (J + self) * K) return;
   const int i = t / K, k = t - i * K;
   double re = 0.0, im = 0.0;
   for (int b = 0; b < nblk; ++b) {
@@ -136,6 +147,10 @@ __global__ void k_finish_dots(const double* part, int nblk, int Jmax, const int*
       im += p[C + 2 * k] - p[C + 2 * k + 1];
     }
   }
+  if (i == J) {  // self dot
+    nb[k] = re;
+    return;
+  }
   h[(size_t(i) * K + k) * 2 + 0] = re;
   h[(size_t(i) * K + k) * 2 + 1] = im;
   if (alpha && i == J - 1 && status[k] == kActive) {
@@ -144,13 +159,15 @@ __global__ void k_finish_dots(const double* part, int nblk, int Jmax, const int*
   }
 }
 
-// W -= sum_{i<J} h_i V_i (complex product for NC = 2) for active points, and
-// per-block partial sums of |W|^2 per column.
+// W -= sum_{i<J} h_i V_i (complex product for NC = 2) for active points
+// (only those with need[k] != 0 when need is given), and per-block partial
+// sums of |W|^2 per column of every active point.
 template <typename S, int NC>
 __global__ void __launch_bounds__(kT) k_update(const S* __restrict__ V, size_t vstride,
                                                const int* jstate, int jfixed, S* W, int64_t N,
                                                int C, int ncomp, const double* h, int K,
-                                               const int* status, int64_t rpb, double* npart) {
+                                               const int* status, int64_t rpb, double* npart,
+                                               const int* need) {
   __shared__ double red[kT];
   const int J = jstate ? (*jstate + 1) : jfixed;
   const int RG = kT / C;
@@ -160,11 +177,12 @@ __global__ void __launch_bounds__(kT) k_update(const S* __restrict__ V, size_t v
   const int64_t r0 = int64_t(blockIdx.x) * rpb;
   const int64_t r1 = (r0 + rpb < N) ? r0 + rpb : N;
   double nrm = 0.0;
+  const int Ju = (need && need[k] == 0) ? 0 : J;
   if (act) {
     for (int64_t row = r0 + rg; row < r1; row += RG) {
       const size_t off = size_t(row) * C;
       double w = double(W[off + c]);
-      for (int i = 0; i < J; ++i) {
+      for (int i = 0; i < Ju; ++i) {
         const double hr = h[(size_t(i) * K + k) * 2 + 0];
         const double v = double(V[size_t(i) * vstride + off + c]);
         if (NC == 1) {
@@ -176,7 +194,7 @@ __global__ void __launch_bounds__(kT) k_update(const S* __restrict__ V, size_t v
           w = (c & 1) ? (w - (hr * v + hi * vp)) : (w - (hr * v - hi * vp));
         }
       }
-      if (J > 0) W[off + c] = S(w);
+      if (Ju > 0) W[off + c] = S(w);
       const double ws = double(S(w));
       nrm = fma(ws, ws, nrm);
     }
@@ -188,6 +206,19 @@ __global__ void __launch_bounds__(kT) k_update(const S* __restrict__ V, size_t v
     for (int g = 0; g < RG; ++g) s += red[g * C + threadIdx.x];
     npart[size_t(blockIdx.x) * C + threadIdx.x] = s;
   }
+}
+
+// After a Gram-Schmidt pass: a further pass is needed for point k only when
+// the pass cancelled more than two digits, ||W_after||^2 < 1e-4 ||W_before||^2.
+__global__ void k_need_pass(const double* npart, int nblk, int K, int C, int ncomp,
+                            const int* status, double* nb, int* need) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K) return;
+  double s = 0.0;
+  for (int b = 0; b < nblk; ++b)
+    for (int q = 0; q < ncomp; ++q) s += npart[size_t(b) * C + k * ncomp + q];
+  need[k] = (status[k] == kActive && s < 1e-4 * nb[k]) ? 1 : 0;
+  nb[k] = s;
 }
 
 // beta_j = ||W|| per point.  A Krylov space that has become invariant
@@ -579,6 +610,8 @@ struct Work {
   double* bnorm = nullptr;
   double* rho = nullptr;
   double* zeros = nullptr;
+  double* nb = nullptr;   // ||W||^2 before the latest Gram-Schmidt pass
+  int* need = nullptr;    // further pass needed, per point
   int* status = nullptr;
   int* len = nullptr;
   int* jstate = nullptr;
@@ -615,6 +648,8 @@ struct Work {
     KCK(cudaMalloc(&rho, sizeof(double) * K));
     KCK(cudaMalloc(&zeros, sizeof(double) * K));
     KCK(cudaMemset(zeros, 0, sizeof(double) * K));
+    KCK(cudaMalloc(&nb, sizeof(double) * K));
+    KCK(cudaMalloc(&need, sizeof(int) * K));
     KCK(cudaMalloc(&status, sizeof(int) * K));
     KCK(cudaMalloc(&len, sizeof(int) * K));
     KCK(cudaMalloc(&jstate, sizeof(int) * 4));
@@ -639,13 +674,15 @@ struct Work {
     cudaFree(bnorm);
     cudaFree(rho);
     cudaFree(zeros);
+    cudaFree(nb);
+    cudaFree(need);
     cudaFree(status);
     cudaFree(len);
     cudaFree(jstate);
     cudaFree(fail);
     V = W = nullptr;
-    R = part = npart = h = alpha = beta = coef = theta = resid = bnorm = rho = zeros = nullptr;
-    status = len = jstate = fail = nullptr;
+    R = part = npart = h = alpha = beta = coef = theta = resid = bnorm = rho = zeros = nb = nullptr;
+    status = len = jstate = fail = need = nullptr;
     N = -1;
   }
 };
@@ -702,26 +739,31 @@ cudaError_t apply_h<float>(const OpDev& op, const float* x, const int* xsel, siz
 
 template <typename S, typename SV>
 cudaError_t launch_multidot(Work<S>& w, const SV* V, size_t vstride, const int* jstate, int jfixed,
-                            const SV* Wp, cudaStream_t s) {
+                            const SV* Wp, cudaStream_t s, int self = 0,
+                            const int* need = nullptr) {
   const int RG = kT / w.C;
   const size_t sh = sizeof(double) * size_t(RG) * kIC * 2 * w.C;
   if (w.ncomp == 1)
     k_multidot<SV, 1><<<w.red.nblk, kT, sh, s>>>(V, vstride, jstate, jfixed, Wp, w.N, w.C,
-                                                 w.red.rpb, w.part, w.ldT), lgt::note_launch();
+                                                 w.red.rpb, w.part, w.ldT, self, need,
+                                                 w.ncomp), lgt::note_launch();
   else
     k_multidot<SV, 2><<<w.red.nblk, kT, sh, s>>>(V, vstride, jstate, jfixed, Wp, w.N, w.C,
-                                                 w.red.rpb, w.part, w.ldT), lgt::note_launch();
+                                                 w.red.rpb, w.part, w.ldT, self, need,
+                                                 w.ncomp), lgt::note_launch();
   return cudaGetLastError();
 }
 
 template <typename S>
-cudaError_t launch_update(Work<S>& w, S* Wp, cudaStream_t s) {
+cudaError_t launch_update(Work<S>& w, S* Wp, cudaStream_t s, const int* need = nullptr) {
   if (w.ncomp == 1)
     k_update<S, 1><<<w.red.nblk, kT, 0, s>>>(w.V, w.vstride, w.jstate, 0, Wp, w.N, w.C, w.ncomp,
-                                             w.h, w.K, w.status, w.red.rpb, w.npart), lgt::note_launch();
+                                             w.h, w.K, w.status, w.red.rpb, w.npart,
+                                             need), lgt::note_launch();
   else
     k_update<S, 2><<<w.red.nblk, kT, 0, s>>>(w.V, w.vstride, w.jstate, 0, Wp, w.N, w.C, w.ncomp,
-                                             w.h, w.K, w.status, w.red.rpb, w.npart), lgt::note_launch();
+                                             w.h, w.K, w.status, w.red.rpb, w.npart,
+                                             need), lgt::note_launch();
   return cudaGetLastError();
 }
 
@@ -732,12 +774,22 @@ cudaError_t lanczos_step(const OpDev& op, Work<S>& w, int reorth, double tiny_re
   cudaError_t e = apply_h<S>(op, w.V, w.jstate, w.vstride, w.W, w.ncomp, s);
   if (e != cudaSuccess) return e;
   const int fdb = (w.ldT * w.K + 127) / 128;
+  // Classical Gram-Schmidt against the whole basis (this also performs the
+  // three-term recurrence).  Further passes, up to `reorth`, act only on the
+  // points whose previous pass cancelled more than two digits
+  // (||W_after|| < 1e-2 ||W_before||); the first pass also measures
+  // ||W_before||.
   for (int pass = 0; pass < reorth; ++pass) {
-    e = launch_multidot<S, S>(w, w.V, w.vstride, w.jstate, 0, w.W, s);
+    const int* need = (pass == 0) ? nullptr : w.need;
+    if (pass > 0)
+      k_need_pass<<<(w.K + 63) / 64, 64, 0, s>>>(w.npart, w.red.nblk, w.K, w.C, w.ncomp,
+                                                 w.status, w.nb, w.need), lgt::note_launch();
+    e = launch_multidot<S, S>(w, w.V, w.vstride, w.jstate, 0, w.W, s, pass == 0 ? 1 : 0, need);
     if (e != cudaSuccess) return e;
     k_finish_dots<<<fdb, 128, 0, s>>>(w.part, w.red.nblk, w.ldT, w.jstate, 0, w.K, w.C, w.ncomp,
-                                      w.h, w.alpha, w.ldT, pass == 0, w.status), lgt::note_launch();
-    e = launch_update<S>(w, w.W, s);
+                                      w.h, w.alpha, w.ldT, pass == 0, w.status,
+                                      pass == 0 ? 1 : 0, w.nb), lgt::note_launch();
+    e = launch_update<S>(w, w.W, s, need);
     if (e != cudaSuccess) return e;
   }
   k_finish_norm<<<(w.K + 63) / 64, 64, 0, s>>>(w.npart, w.red.nblk, w.K, w.C, w.ncomp, w.jstate,
@@ -769,7 +821,8 @@ std::string dots_ws(Work<S>& w, const double* x, const double* y, double* out_ho
                     cudaStream_t s) {
   KCK((launch_multidot<S, double>(w, x, 0, nullptr, 1, y, s)));
   k_finish_dots<<<(w.K + 127) / 128, 128, 0, s>>>(w.part, w.red.nblk, w.ldT, nullptr, 1, w.K, w.C,
-                                                  w.ncomp, w.h, nullptr, 0, 0, nullptr), lgt::note_launch();
+                                                  w.ncomp, w.h, nullptr, 0, 0, nullptr, 0,
+                                                  nullptr), lgt::note_launch();
   KCK(cudaGetLastError());
   std::vector<double> hh(2 * size_t(w.K));
   KCK(cudaMemcpyAsync(hh.data(), w.h, sizeof(double) * 2 * w.K, cudaMemcpyDeviceToHost, s));

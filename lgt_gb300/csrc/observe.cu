@@ -166,7 +166,9 @@ cudaError_t launch_obs2(const Geom& G, const RankView& R, const T* x, int K, int
 int observe_nfeat(const Geom& G) { return 2 * G.ns + G.nP + 1; }
 
 void observe_plan(int64_t N, int* nblk, int64_t* rpb) {
-  int64_t want = (N + 1023) / 1024;
+  // about 64 rows per block for small sectors (so a K = 64 batch of N = 645
+  // spreads over ten blocks), at most four blocks per SM
+  int64_t want = (N + 63) / 64;
   if (want > 152 * 4) want = 152 * 4;
   if (want < 1) want = 1;
   int64_t r = (N + want - 1) / want;

@@ -146,23 +146,44 @@ __device__ double block_sum(double v, double* red) {
   return s;
 }
 
+// Number of eigenvalues of the tridiagonal (a, b) below x: sign changes of
+// the leading principal minors p_i = det(T_i - x I), from the three-term
+// recurrence p_i = (a_i - x) p_{i-1} - b_{i-1}^2 p_{i-2}.  Division-free (FP64
+// division is a long dependent chain on this part); the minors are rescaled
+// by 2^-600 when they grow past 2^600 and an exact zero takes the sign
+// opposite to its predecessor.
 __device__ int sturm_below(const double* a, const double* b, int n, double x) {
-  int cnt = 0;
-  double q = 1.0;
-  for (int i = 0; i < n; ++i) {
-    q = (a[i] - x) - ((i > 0) ? (b[i - 1] * b[i - 1]) / q : 0.0);
-    if (q == 0.0) q = -1e-300;
-    if (q < 0.0) ++cnt;
+  double p0 = 1.0, p1 = a[0] - x;
+  int sp = 1;
+  int s1 = (p1 > 0.0) ? 1 : ((p1 < 0.0) ? -1 : -sp);
+  int cnt = (s1 != sp) ? 1 : 0;
+  sp = s1;
+  for (int i = 1; i < n; ++i) {
+    double p2 = fma(a[i] - x, p1, -(b[i - 1] * b[i - 1]) * p0);
+    if (fabs(p2) > 0x1.0p600) {
+      p2 *= 0x1.0p-600;
+      p1 *= 0x1.0p-600;
+    } else if (fabs(p2) < 0x1.0p-600 && fabs(p1) < 0x1.0p-600) {
+      p2 *= 0x1.0p600;
+      p1 *= 0x1.0p600;
+    }
+    const int s2 = (p2 > 0.0) ? 1 : ((p2 < 0.0) ? -1 : -sp);
+    cnt += (s2 != sp) ? 1 : 0;
+    sp = s2;
+    p0 = p1;
+    p1 = p2;
   }
   return cnt;
 }
 
 // Lowest eigenpair of the n x n symmetric tridiagonal (a, b) by warp-parallel
 // multisection of the Sturm count (32 probes per round), then inverse
-// iteration on the positive-definite T - (theta - delta) I by lane 0.
-// Called by one full warp; z (n entries) is written by lane 0.
+// iteration on the positive-definite T - (theta - delta) I by lane 0,
+// starting from z when warm (z holds the previous eigenvector, padded with
+// zeros) or from ones.  Called by one full warp; z (n entries) is written by
+// lane 0.
 __device__ double warp_lowest_eig(const double* a, const double* b, int n, double* z,
-                                  double* work) {
+                                  double* work, bool warm) {
   const int lane = threadIdx.x & 31;
   double lo = a[0], hi = a[0];
   for (int i = 0; i < n; ++i) {
@@ -192,28 +213,34 @@ __device__ double warp_lowest_eig(const double* a, const double* b, int n, doubl
   const double theta = 0.5 * (lo + hi);
   if (lane == 0) {
     const double shift = theta - 4.0 * 2.2e-16 * scale;
-    double* d = work;
+    double* d = work;  // reciprocal pivots
     double* l = work + kMaxM;
-    for (int i = 0; i < n; ++i) z[i] = 1.0;
-    for (int rep = 0; rep < 3; ++rep) {
-      d[0] = a[0] - shift;
-      if (d[0] <= 0.0) d[0] = 1e-300;
+    if (!warm)
+      for (int i = 0; i < n; ++i) z[i] = 1.0;
+    const int reps = warm ? 1 : 2;
+    for (int rep = 0; rep < reps; ++rep) {
+      double piv = a[0] - shift;
+      if (piv <= 0.0) piv = 1e-300;
+      d[0] = 1.0 / piv;
       for (int i = 1; i < n; ++i) {
-        l[i - 1] = b[i - 1] / d[i - 1];
-        d[i] = (a[i] - shift) - l[i - 1] * b[i - 1];
-        if (d[i] <= 0.0) d[i] = 1e-300;
+        l[i - 1] = b[i - 1] * d[i - 1];
+        piv = (a[i] - shift) - l[i - 1] * b[i - 1];
+        if (piv <= 0.0) piv = 1e-300;
+        d[i] = 1.0 / piv;
       }
-      for (int i = 1; i < n; ++i) z[i] -= l[i - 1] * z[i - 1];
-      for (int i = 0; i < n; ++i) z[i] /= d[i];
-      for (int i = n - 2; i >= 0; --i) z[i] -= l[i] * z[i + 1];
-      double mx = 0.0, nn = 0.0;
+      for (int i = 1; i < n; ++i) z[i] = fma(-l[i - 1], z[i - 1], z[i]);
+      for (int i = 0; i < n; ++i) z[i] *= d[i];
+      for (int i = n - 2; i >= 0; --i) z[i] = fma(-l[i], z[i + 1], z[i]);
+      double mx = 0.0;
       for (int i = 0; i < n; ++i) mx = fmax(mx, fabs(z[i]));
+      const double inv = 1.0 / mx;
+      double nn = 0.0;
       for (int i = 0; i < n; ++i) {
-        z[i] /= mx;
-        nn += z[i] * z[i];
+        z[i] *= inv;
+        nn = fma(z[i], z[i], nn);
       }
-      nn = sqrt(nn);
-      for (int i = 0; i < n; ++i) z[i] /= nn;
+      const double in2 = 1.0 / sqrt(nn);
+      for (int i = 0; i < n; ++i) z[i] *= in2;
     }
     if (z[0] < 0.0)
       for (int i = 0; i < n; ++i) z[i] = -z[i];
@@ -233,7 +260,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
   __shared__ double s_red[kWarpsCta];
   __shared__ double s_work[2 * kMaxM];
   __shared__ double s_theta, s_resid;
-  __shared__ int s_flag;
+  __shared__ int s_flag, s_zwarm;
   const SmallUnit U = units[blockIdx.x];
   const SmallProblem P = probs[U.prob];
   const int N = P.N;
@@ -270,6 +297,8 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
   for (int cycle = 0;; ++cycle) {
     n = 0;
     bool exhausted = false;
+    if (tid == 0) s_zwarm = 0;
+    __syncthreads();
     for (int j = 0; j < m; ++j) {
       const S* vj = V + size_t(j) * N;
       // w = H v_j (matvec in the storage precision)
@@ -290,42 +319,78 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
           w[i] = 0.0;
         }
       }
-      // classical Gram-Schmidt against V_0..V_j, prm.reorth passes
+      // Classical Gram-Schmidt against the whole basis V_0..V_j (which also
+      // performs the three-term recurrence), four basis vectors per round so
+      // four independent FP64 chains are in flight.  A further pass (up to
+      // prm.reorth) runs only when a pass cancels more than two digits,
+      // ||w_after|| < 1e-2 ||w_before||: the rounding error it leaves along the
+      // basis is then above eps * 100 relative to w.
+      double nb;
+      {
+        double s0 = 0.0;
+#pragma unroll
+        for (int i = 0; i < R; ++i) s0 = fma(w[i], w[i], s0);
+        nb = block_sum(s0, s_red);
+      }
+      double ss = nb;
       for (int pass = 0; pass < prm.reorth; ++pass) {
-        for (int b = 0; b <= j; ++b) {
-          const S* vb = V + size_t(b) * N;
-          double p = 0.0;
+        for (int b0 = 0; b0 <= j; b0 += 4) {
+          double p[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
           for (int i = 0; i < R; ++i) {
             const int r = tid + i * kCta;
-            if (r < N) p = fma(double(vb[r]), w[i], p);
+            if (r < N) {
+#pragma unroll
+              for (int q = 0; q < 4; ++q)
+                if (b0 + q <= j) p[q] = fma(double(V[size_t(b0 + q) * N + r]), w[i], p[q]);
+            }
           }
-          p = warp_sum(p);
-          if (lane == 0) s_part[b][wid] = p;
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) p[q] += __shfl_xor_sync(0xffffffffu, p[q], o);
+          }
+          if (lane < 4 && b0 + lane <= j) {
+            const double mine = (lane == 0) ? p[0] : (lane == 1) ? p[1] : (lane == 2) ? p[2] : p[3];
+            s_part[b0 + lane][wid] = mine;
+          }
         }
         __syncthreads();
         if (tid <= j) {
-          double s = 0.0;
-          for (int ww = 0; ww < kWarpsCta; ++ww) s += s_part[tid][ww];
-          s_h[tid] = s;
-          if (tid == j) s_alpha[j] = (pass == 0) ? s : s_alpha[j] + s;
+          double s0 = 0.0, s1 = 0.0;
+          for (int ww = 0; ww < kWarpsCta; ww += 2) {
+            s0 += s_part[tid][ww];
+            s1 += s_part[tid][ww + 1];
+          }
+          const double sum = s0 + s1;
+          s_h[tid] = sum;
+          if (tid == j) s_alpha[j] = (pass == 0) ? sum : s_alpha[j] + sum;
         }
         __syncthreads();
-        for (int b = 0; b <= j; ++b) {
-          const double hb = s_h[b];
-          const S* vb = V + size_t(b) * N;
+        for (int b0 = 0; b0 <= j; b0 += 4) {
+          double h4[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) h4[q] = (b0 + q <= j) ? s_h[b0 + q] : 0.0;
 #pragma unroll
           for (int i = 0; i < R; ++i) {
             const int r = tid + i * kCta;
-            if (r < N) w[i] = fma(-hb, double(vb[r]), w[i]);
+            if (r < N) {
+              double t[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+              for (int q = 0; q < 4; ++q)
+                if (b0 + q <= j) t[q] = h4[q] * double(V[size_t(b0 + q) * N + r]);
+              w[i] -= (t[0] + t[1]) + (t[2] + t[3]);
+            }
           }
         }
-        __syncthreads();
-      }
-      double ss = 0.0;
+        double s1 = 0.0;
 #pragma unroll
-      for (int i = 0; i < R; ++i) ss = fma(w[i], w[i], ss);
-      const double beta = sqrt(block_sum(ss, s_red));
+        for (int i = 0; i < R; ++i) s1 = fma(w[i], w[i], s1);
+        ss = block_sum(s1, s_red);
+        if (!(ss < 1e-4 * nb)) break;
+        nb = ss;
+      }
+      const double beta = sqrt(ss);
       if (tid == 0) s_beta[j] = beta;
       n = j + 1;
       ++steps;
@@ -341,11 +406,13 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
           if (r < N) vn[r] = S(w[i] / beta);
         }
       }
-      const bool check = exhausted || ((j + 1) % prm.check_every == 0) || (j + 1 == m);
+      // first check after 2 * check_every steps, then every check_every
+      const bool check = exhausted || (j + 1 == m) ||
+                         (j + 1 >= 2 * prm.check_every && (j + 1) % prm.check_every == 0);
       if (check) {
         __syncthreads();
         if (wid == 0) {
-          const double th = warp_lowest_eig(s_alpha, s_beta, n, s_z, s_work);
+          const double th = warp_lowest_eig(s_alpha, s_beta, n, s_z, s_work, s_zwarm != 0);
           if (lane == 0) {
             const double rr = exhausted ? 0.0 : fabs(s_beta[n - 1] * s_z[n - 1]);
             // FP32 panels resolve residuals to ~1e-6 |H|: relative floor
@@ -353,6 +420,8 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
             s_flag = (exhausted || rr <= tl) ? 1 : 0;
             s_theta = th;
             s_resid = rr;
+            s_zwarm = 1;
+            for (int i = n; i < kMaxM; ++i) s_z[i] = 0.0;
           }
         }
         __syncthreads();
