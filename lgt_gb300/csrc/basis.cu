@@ -265,6 +265,106 @@ __global__ void k_rank_order_keys(Geom G, RankView R, const uint64_t* in, int64_
   out[i] = idx;
 }
 
+
+// ---- rank tables ---------------------------------------------------------------
+//
+// Within the segment of a fermion mask, states are ordered lexicographically
+// by their e_U rows u_0, u_1, ..., u_{ny-2}, each row by its free digits
+// (all but the last, which the row sum fixes).  So the index of a state is
+//     segc(mask) + sum_r T_r(mask rows >= r, u_{r-1}, u_r),
+//     T_r = sum over v < u_r valid at row r given u_{r-1} of
+//           Cnt_{r+1}(v) = number of valid completions of rows r+1.. given u_r = v.
+// Validity at row r needs only q on row r, the row sum S_r (which depends on
+// the mask rows below... above r: S_r = -sum_{j>r} R_j) and u_{r-1}, u_r, so
+// every term is a table lookup.  Tables are built bottom-up; entry [F] of the
+// last axis holds the total Cnt_r.  T_0 is indexed by the whole mask and
+// carries segc folded in.  A state's rank is then ny-1 independent loads.
+
+// digits of a row from its free-digit index f (first most significant) and
+// row sum S; returns false if the determined last digit is out of range
+__device__ __forceinline__ bool row_digits(int nx, int dg, int B, uint32_t f, int S, int* d) {
+  int sum = 0;
+  for (int ix = nx - 2; ix >= 0; --ix) {
+    d[ix] = int(f % uint32_t(B)) - dg;
+    f /= uint32_t(B);
+    sum += d[ix];
+  }
+  d[nx - 1] = S - sum;
+  return d[nx - 1] >= -dg && d[nx - 1] <= dg;
+}
+
+// e_R row validity: acc over ix < nx-1 of q(ix) - u(ix) + uprev(ix) within [-dg, dg]
+__device__ __forceinline__ bool eR_row_ok(int nx, int dg, uint32_t rowbits, const int8_t* g,
+                                          const int* u, const int* uprev) {
+  int acc = 0;
+  for (int ix = 0; ix < nx - 1; ++ix) {
+    acc += int((rowbits >> ix) & 1u) + g[ix] - (u ? u[ix] : 0) + (uprev ? uprev[ix] : 0);
+    if (acc < -dg || acc > dg) return false;
+  }
+  return true;
+}
+
+// Cnt_{ny-1}(u_{ny-2}): the last e_R row, for every bit pattern m of the last
+// site row and every free index fp of u_{ny-2}.
+__global__ void k_tab_last(Geom G, int F, uint32_t* L) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (1 << G.nx) * F) return;
+  const uint32_t m = uint32_t(idx / F), fp = uint32_t(idx % F);
+  const int r = G.ny - 1;
+  const int Rl = __popc(m) + G.grow[r];
+  int up[kMaxSites];
+  const bool okp = row_digits(G.nx, G.dg, 2 * G.dg + 1, fp, -Rl, up);
+  L[idx] = (okp && eR_row_ok(G.nx, G.dg, m, G.gq + r * G.nx, nullptr, up)) ? 1u : 0u;
+}
+
+// T_r for e_U row r (0 <= r <= ny-2): m = site rows >= r (nx*(ny-r) bits),
+// fp = free index of u_{r-1} (Fp = 1 for r = 0).  `next` is Cnt_{r+1}:
+// L when r = ny-2, else T_{r+1} (its entry [F]).
+__global__ void k_tab_row(Geom G, int F, int r, const uint32_t* next, int next_is_last,
+                          uint32_t* T, int Fp, int64_t nm) {
+  const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= nm * Fp) return;
+  const uint32_t m = uint32_t(idx / Fp), fp = uint32_t(idx % Fp);
+  const int B = 2 * G.dg + 1;
+  const uint32_t rowmask = (1u << G.nx) - 1u;
+  int Sr = 0;  // S_r = -sum_{j>r} R_j
+  for (int j = r + 1; j < G.ny; ++j) Sr -= __popc((m >> ((j - r) * G.nx)) & rowmask) + G.grow[j];
+  const int Rr = __popc(m & rowmask) + G.grow[r];
+  int up[kMaxSites], u[kMaxSites];
+  if (r > 0) row_digits(G.nx, G.dg, B, fp, Sr - Rr, up);
+  uint32_t run = 0;
+  uint32_t* out = T + (uint64_t(m) * Fp + fp) * uint64_t(F + 1);
+  for (int v = 0; v < F; ++v) {
+    out[v] = run;
+    if (!row_digits(G.nx, G.dg, B, uint32_t(v), Sr, u)) continue;
+    if (!eR_row_ok(G.nx, G.dg, m & rowmask, G.gq + r * G.nx, u, r > 0 ? up : nullptr)) continue;
+    const uint64_t mn = uint64_t(m >> G.nx);
+    run += next_is_last ? next[mn * F + v] : next[(mn * F + v) * uint64_t(F + 1) + F];
+  }
+  out[F] = run;
+}
+
+// T_0 += segc of the mask's segment (masks with the sector's particle number)
+__global__ void k_tab_seg(Geom G, const uint32_t* masks, const uint32_t* segc, int nmasks, int F,
+                          uint32_t* T0) {
+  const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= int64_t(nmasks) * (F + 1)) return;
+  const int cr = int(idx / (F + 1)), v = int(idx % (F + 1));
+  T0[uint64_t(masks[cr]) * (F + 1) + v] += segc[cr];
+}
+
+// every basis key must rank to its own index through the tables
+__global__ void k_tab_check(RankView R, int* bad) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= R.dim) return;
+  const uint64_t key = R.keys[i];
+  const uint64_t digits = key & ((1ull << R.ushift) - 1);
+  uint32_t f[kMaxTabRows];
+#pragma unroll
+  for (int r = 0; r < kMaxTabRows; ++r) f[r] = (r < R.nrows) ? row_index(R, digits, r) : 0u;
+  if (rank_rows(R, uint32_t(key >> R.ushift), f, -1, 0) != i) atomicOr(bad, 1);
+}
+
 #define CK(call)                                                                 \
   do {                                                                           \
     cudaError_t e_ = (call);                                                     \
@@ -366,6 +466,62 @@ std::string make_geom(int nx, int ny, int dg, const int32_t* g, Geom* Gp) {
   return std::string();
 }
 
+// Builds the row-count rank tables when they fit (at most 2^25 entries) and
+// keeps them only if every basis key ranks to its own index through them.
+std::string build_rank_tables(BasisDev* B) {
+  const Geom& G = B->G;
+  cudaStream_t s = B->stream;
+  const int nrows = G.ny - 1;
+  if (B->dim == 0 || nrows < 1 || nrows > kMaxTabRows || G.nx < 2) return std::string();
+  const int Bd = 2 * G.dg + 1;
+  long double Fl = 1;
+  for (int i = 0; i < G.nx - 1; ++i) Fl *= Bd;
+  if (Fl > 4096) return std::string();
+  const int F = int(Fl);
+  int64_t off[kMaxTabRows] = {};
+  long double tot = (long double)(1ull << G.ns) * (F + 1);
+  for (int r = 1; r < nrows; ++r) {
+    off[r] = int64_t(tot);
+    tot += (long double)(1ull << (G.nx * (G.ny - r))) * F * (F + 1);
+  }
+  const int64_t nlast = int64_t(1) << G.nx;
+  if (tot + nlast * F > (long double)(int64_t(1) << 25)) return std::string();
+  uint32_t* tab = nullptr;
+  uint32_t* L = nullptr;
+  int* bad = nullptr;
+  CK(cudaMalloc(&tab, sizeof(uint32_t) * size_t(tot)));
+  CK(cudaMalloc(&L, sizeof(uint32_t) * size_t(nlast * F)));
+  CK(cudaMalloc(&bad, sizeof(int)));
+  CK(cudaMemsetAsync(bad, 0, sizeof(int), s));
+  k_tab_last<<<unsigned((nlast * F + 255) / 256), 256, 0, s>>>(G, F, L), lgt::note_launch();
+  for (int r = nrows - 1; r >= 0; --r) {
+    const int64_t nm = int64_t(1) << (G.nx * (G.ny - r));
+    const int Fp = (r == 0) ? 1 : F;
+    const uint32_t* next = (r == nrows - 1) ? L : tab + off[r + 1];
+    k_tab_row<<<unsigned((nm * Fp + 255) / 256), 256, 0, s>>>(G, F, r, next, r == nrows - 1,
+                                                              tab + off[r], Fp, nm), lgt::note_launch();
+  }
+  k_tab_seg<<<unsigned((int64_t(B->nmasks) * (F + 1) + 255) / 256), 256, 0, s>>>(
+      G, B->masks, B->segc, B->nmasks, F, tab), lgt::note_launch();
+  CK(cudaGetLastError());
+  B->tab = tab;
+  B->tab_F = F;
+  for (int r = 0; r < kMaxTabRows; ++r) B->tab_off[r] = off[r];
+  k_tab_check<<<unsigned((B->dim + 255) / 256), 256, 0, s>>>(B->view(), bad), lgt::note_launch();
+  int hbad = 0;
+  CK(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  cudaFree(L);
+  cudaFree(bad);
+  if (hbad) {  // keep the binary-search ranking
+    cudaFree(B->tab);
+    B->tab = nullptr;
+    B->tab_F = 0;
+    return "rank tables failed their self-check";
+  }
+  return std::string();
+}
+
 std::string build_basis_device(BasisDev* B) {
   const Geom& G = B->G;
   cudaStream_t s = B->stream;
@@ -426,10 +582,14 @@ std::string build_basis_device(BasisDev* B) {
     CK(cudaGetLastError());
   }
   CK(cudaStreamSynchronize(s));
+  err = build_rank_tables(B);
+  if (!err.empty()) return err;
   return std::string();
 }
 
 void free_basis_device(BasisDev* B) {
+  cudaFree(B->tab);
+  B->tab = nullptr;
   cudaFree(B->keys);
   cudaFree(B->low);
   cudaFree(B->segc);

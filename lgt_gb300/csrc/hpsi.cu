@@ -126,14 +126,31 @@ __global__ void __launch_bounds__(kThreads) k_hpsi(HpsiArgs<T> a) {
       const Config c = decode(G, __ldg(a.R.keys + row));
       diag_parts(G, c, &e2, &stag);
       uint32_t* my = nbr + lane * G.max_moves;
-      for_each_move<PLAQ, JW>(G, c, [&](uint64_t nkey, uint32_t kind) {
-        const int64_t j = rank_key(a.R, segc, s_binom, nkey);
-        if (j < 0) {
-          raise_err(a.err, kDevErrRank);
-          return;
-        }
-        if (cnt < G.max_moves) my[cnt++] = (uint32_t(j) << 2) | kind;
-      });
+      if (a.R.tab) {
+        // rank tables: each neighbour's index is nrows independent loads
+        uint32_t fidx[kMaxTabRows];
+#pragma unroll
+        for (int r = 0; r < kMaxTabRows; ++r)
+          fidx[r] = (r < a.R.nrows) ? row_index(a.R, c.digits, r) : 0u;
+        for_each_move_rows<PLAQ, JW>(G, c, fidx, a.R.pw,
+                                     [&](uint32_t nmask, int rc, uint32_t frc, uint32_t kind) {
+          const int64_t j = rank_rows(a.R, nmask, fidx, rc, frc);
+          if (j < 0 || j >= a.N) {
+            raise_err(a.err, kDevErrBounds);
+            return;
+          }
+          if (cnt < G.max_moves) my[cnt++] = (uint32_t(j) << 2) | kind;
+        });
+      } else {
+        for_each_move<PLAQ, JW>(G, c, [&](uint64_t nkey, uint32_t kind) {
+          const int64_t j = rank_key(a.R, segc, s_binom, nkey);
+          if (j < 0) {
+            raise_err(a.err, kDevErrRank);
+            return;
+          }
+          if (cnt < G.max_moves) my[cnt++] = (uint32_t(j) << 2) | kind;
+        });
+      }
     }
     meta[lane * 4 + 0] = int16_t(cnt);
     meta[lane * 4 + 1] = int16_t(e2);

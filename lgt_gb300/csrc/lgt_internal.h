@@ -21,6 +21,8 @@ namespace lgt {
 // positions p_1 < ... < p_k).  segc[r] is the first index of mask r's
 // segment.  The hop kernels stage this level in shared memory when it fits.
 // The bottom level is a binary search over the segment's low key parts.
+constexpr int kMaxTabRows = 8;
+
 struct RankView {
   const uint64_t* keys;   // sorted order keys [dim]
   const uint32_t* low;    // low (e_U) parts of the keys [dim] (when ushift <= 32)
@@ -30,6 +32,15 @@ struct RankView {
   int nmasks;
   int ushift;
   int low32;              // 1 when `low` is valid
+  // Row-count tables (tab != null): the index of a state is a sum of one
+  // table entry per e_U row (see basis.cu, "rank tables").
+  const uint32_t* tab;
+  int64_t tab_off[kMaxTabRows];  // start of the table of e_U row r in `tab`
+  int nrows;              // e_U rows with a table (ny - 1)
+  int F;                  // free-digit strings per e_U row, B^(nx-1)
+  int B, nx, w, nU;       // digit base, lattice width, bits per digit, up links
+  int ns, nf;             // sites, fermions
+  int pw[kMaxSites];      // weight of free digit ix in a row's index (0 for the last)
 };
 
 struct BasisDev {
@@ -41,6 +52,9 @@ struct BasisDev {
   uint32_t* segc = nullptr;
   uint32_t* masks = nullptr;
   uint32_t* binom = nullptr;
+  uint32_t* tab = nullptr;      // rank tables (null when they would not fit)
+  int64_t tab_off[kMaxTabRows] = {};
+  int tab_F = 0;
   int* err = nullptr;           // device error word (DevErr bits)
   cudaStream_t stream = nullptr;
   RankView view() const {
@@ -53,6 +67,22 @@ struct BasisDev {
     v.nmasks = nmasks;
     v.ushift = G.ushift;
     v.low32 = (G.ushift <= 32) ? 1 : 0;
+    v.tab = tab;
+    for (int r = 0; r < kMaxTabRows; ++r) v.tab_off[r] = tab_off[r];
+    v.nrows = G.ny - 1;
+    v.F = tab_F;
+    v.B = 2 * G.dg + 1;
+    v.nx = G.nx;
+    v.w = G.w;
+    v.nU = G.nU;
+    v.ns = G.ns;
+    v.nf = G.nf_target;
+    int p = 1;
+    for (int ix = kMaxSites - 1; ix >= 0; --ix) v.pw[ix] = 0;
+    for (int ix = G.nx - 2; ix >= 0; --ix) {
+      v.pw[ix] = p;
+      p *= v.B;
+    }
     return v;
   }
 };
