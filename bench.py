@@ -255,11 +255,12 @@ def gpu_workloads(args, rank, world):
 
     # ---- roofline: H*psi on the 4x4 lattice (working set > L2) ---------------
     rf = roofline(L, C, lib, torch, stream, dev)
+    qn = quench(L, C, lib, torch, stream, dev, n_steps=args.quench_steps)
     states.close()
     return dict(t_mix=t_mix, dE_mix=dE_mix, launches=launches, clocks=clocks, info_mix=info_mix,
                 t_b64=t_b64, dE_b64=dE_b64, plain_times=plain_times, dE_plain=dE_plain,
                 t_pjw=t_pjw, dE_pjw=dE_pjw, e2e_times=e2e_times, h2d=h2d, d2h=d2h,
-                dE_e2e=dE_e2e, basis_ms=basis_ms, N=N, rf=rf,
+                dE_e2e=dE_e2e, basis_ms=basis_ms, N=N, rf=rf, quench=qn,
                 matvecs_mix=info_mix.matvecs, restarts_mix=info_mix.restarts)
 
 
@@ -298,6 +299,53 @@ def gs_only(args):
     H.close()
     states.close()
     return {"gs_per_s": KPTS / statistics.mean(ts), "ms_per_step": 1e3 * statistics.mean(ts)}
+
+
+def quench(L, C, lib, torch, stream, dev, n_steps=5):
+    """4x4 real-time quench panel: K = 8 points g ~ U[0.5, 1.5] (seed 0), m = 0.5,
+    t = 1, from the staggered product state, dt = 0.05; n_steps Krylov
+    exp(-iH dt) steps with observables every step, FP64 and FP32-mixed."""
+    b, _ = L.build_basis(RF_NX, RF_NY, DG, L.staggered_charges(RF_NX, RF_NY), device=dev)
+    C.check(lib.lgt_basis_set_stream(b.handle, ctypes_ptr(stream.cuda_stream)))
+    N = len(b)
+    gs = np.random.default_rng(0).uniform(0.5, 1.5, RF_K)
+    H = L.build_hamiltonian(b, g=gs, t=1.0, m=0.5, model="ref")
+    v0 = L.staggered_product_state(b)
+    i0 = int(np.argmax(np.abs(v0)))
+    out = {"N": N, "K": RF_K, "dt": 0.05, "steps_timed": n_steps}
+    for prec, code in (("fp64", C.LGT_FP64), ("fp32_mixed", C.LGT_FP32_MIXED)):
+        psi = torch.zeros((N, RF_K, 2), dtype=torch.float64, device="cuda")
+        psi[i0, :, 0] = 1.0
+        torch.cuda.synchronize()  # the library runs on `stream`
+        e_before = np.zeros(RF_K)
+        C.check(lib.lgt_energy(H.handle, psi.data_ptr(), 2, C.LGT_DEVICE_PTRS, e_before.ctypes.data))
+        o = C.defaults(True)
+        o.precision = code
+        obs = (C.Obs * ((n_steps + 1) * RF_K))()
+        drift = np.zeros(RF_K)
+        info = C.Info()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            C.check(lib.lgt_expm_steps(H.handle, o, 0.05, n_steps, psi.data_ptr(), obs,
+                                       drift.ctypes.data, C.LGT_DEVICE_PTRS, info))
+            e1.record(stream)
+        e1.synchronize()
+        t = e0.elapsed_time(e1) * 1e-3
+        e_after = np.zeros(RF_K)
+        C.check(lib.lgt_energy(H.handle, psi.data_ptr(), 2, C.LGT_DEVICE_PTRS, e_after.ctypes.data))
+        out[prec] = {"quench_steps_per_s": n_steps / t, "s_per_step": t / n_steps,
+                     "matvecs_per_step": info.matvecs / n_steps,
+                     "max_norm_drift": float(drift.max()),
+                     "max_rel_energy_drift": float(np.max(np.abs(e_after - e_before) /
+                                                         np.abs(e_before))),
+                     "E2_mean_t_end_point0": obs[n_steps * RF_K].E2_mean}
+        del psi
+    H.close()
+    b.close()
+    return out
 
 
 def ctypes_ptr(v):
@@ -358,7 +406,9 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--part", default="all", choices=["all", "hpsi", "gs"],
+    ap.add_argument("--quench-steps", type=int, default=4,
+                    help="timed 4x4 quench steps (dt = 0.05; t = 5 needs 100)")
+    ap.add_argument("--part", default="all", choices=["all", "hpsi", "gs", "quench"],
                     help="hpsi: only the 4x4 H*psi roofline loop; gs: only the headline "
                          "ground-state loop (both for profiling: no child processes)")
     args = ap.parse_args()
@@ -398,6 +448,16 @@ def main():
 
     if args.part == "gs":
         print(json.dumps({"part": "gs", **gs_only(args)}))
+        return
+
+    if args.part == "quench":
+        import torch
+
+        import lgt_gb300 as L
+        from lgt_gb300 import _capi as C
+        torch.cuda.set_device(0)
+        q = quench(L, C, C.load(), torch, torch.cuda.Stream(), 0, n_steps=args.quench_steps)
+        print(json.dumps({"part": "quench", "quench": q}))
         return
 
     if args.part == "hpsi":
@@ -469,6 +529,7 @@ def main():
                      "peak_source": rf["peak_src"] + " (MEASURED_PEAKS.json hbm_gbs)",
                      "algo_bytes_per_launch": dom["algo_bytes"], "ms_per_launch": dom["ms"],
                      "variants": {k: v for k, v in rf.items() if isinstance(v, dict)}},
+        "quench_4x4": r["quench"],
         "cpu_baseline": {"value": cpu_val, "unit": "GS/s", "cores": ncores, "kind": "port",
                          "sample": "one step: all 64 points, one point per host process; oracle "
                                    "port of finite_ed.jl (C basis + H, scipy eigsh tol 1e-10 ncv 50)"},

@@ -89,11 +89,18 @@ __host__ __device__ inline SmemLayout smem_layout(int nmasks, int seg_smem, int 
   return L;
 }
 
+// Off-diagonal entries a row can have: one per bond, plus W and W^dagger
+// per plaquette when the model has them.
+__host__ __device__ inline int row_moves(const Geom& G, bool plaq) {
+  return G.nR + G.nU + (plaq ? 2 * G.nP : 0);
+}
+
 template <typename T, int V, bool PLAQ, bool JW>
 __global__ void __launch_bounds__(kThreads) k_hpsi(HpsiArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const Geom& G = a.G;
-  const SmemLayout L = smem_layout<T>(a.R.nmasks, a.seg_smem, a.K, G.max_moves);
+  const int MM = row_moves(G, PLAQ);
+  const SmemLayout L = smem_layout<T>(a.R.nmasks, a.seg_smem, a.K, MM);
   uint32_t* s_binom = reinterpret_cast<uint32_t*>(smem + L.binom_off);
   uint32_t* s_segc = reinterpret_cast<uint32_t*>(smem + L.segc_off);
   T* s_coef = reinterpret_cast<T*>(smem + L.coef_off);  // [4][K]: cE, cm, ch, cp
@@ -116,7 +123,7 @@ __global__ void __launch_bounds__(kThreads) k_hpsi(HpsiArgs<T> a) {
   const int64_t warp_row0 = (int64_t(blockIdx.x) * kWarps + wid) * 32;
   if (warp_row0 >= a.N) return;
   int16_t* meta = s_meta + (wid * 32) * 4;
-  uint32_t* nbr = s_nbr + size_t(wid * 32) * G.max_moves;
+  uint32_t* nbr = s_nbr + size_t(wid * 32) * MM;
 
   // ---- phase 1: one lane per row: moves + ranks -------------------------
   {
@@ -125,7 +132,7 @@ __global__ void __launch_bounds__(kThreads) k_hpsi(HpsiArgs<T> a) {
     if (row < a.N) {
       const Config c = decode(G, __ldg(a.R.keys + row));
       diag_parts(G, c, &e2, &stag);
-      uint32_t* my = nbr + lane * G.max_moves;
+      uint32_t* my = nbr + lane * MM;
       if (a.R.tab) {
         // rank tables: each neighbour's index is nrows independent loads
         uint32_t fidx[kMaxTabRows];
@@ -139,7 +146,7 @@ __global__ void __launch_bounds__(kThreads) k_hpsi(HpsiArgs<T> a) {
             raise_err(a.err, kDevErrBounds);
             return;
           }
-          if (cnt < G.max_moves) my[cnt++] = (uint32_t(j) << 2) | kind;
+          if (cnt < MM) my[cnt++] = (uint32_t(j) << 2) | kind;
         });
       } else {
         for_each_move<PLAQ, JW>(G, c, [&](uint64_t nkey, uint32_t kind) {
@@ -148,7 +155,7 @@ __global__ void __launch_bounds__(kThreads) k_hpsi(HpsiArgs<T> a) {
             raise_err(a.err, kDevErrRank);
             return;
           }
-          if (cnt < G.max_moves) my[cnt++] = (uint32_t(j) << 2) | kind;
+          if (cnt < MM) my[cnt++] = (uint32_t(j) << 2) | kind;
         });
       }
     }
@@ -185,7 +192,7 @@ __global__ void __launch_bounds__(kThreads) k_hpsi(HpsiArgs<T> a) {
     vload<T, V>(x + size_t(row) * C + col0, xv);
 #pragma unroll
     for (int e = 0; e < V; ++e) acc[e] = cd[e] * xv[e];
-    const uint32_t* lst = nbr + rl * G.max_moves;
+    const uint32_t* lst = nbr + rl * MM;
     for (int n = 0; n < cnt; ++n) {
       const uint32_t ent = lst[n];
       const size_t j = ent >> 2;
@@ -203,7 +210,7 @@ __global__ void __launch_bounds__(kThreads) k_hpsi(HpsiArgs<T> a) {
 
 template <typename T, int V, bool PLAQ, bool JW>
 cudaError_t launch_t(const HpsiArgs<T>& a, cudaStream_t s) {
-  const SmemLayout L = smem_layout<T>(a.R.nmasks, a.seg_smem, a.K, a.G.max_moves);
+  const SmemLayout L = smem_layout<T>(a.R.nmasks, a.seg_smem, a.K, row_moves(a.G, PLAQ));
   auto kern = k_hpsi<T, V, PLAQ, JW>;
   // raise the dynamic shared-memory limit once per kernel (outside any graph
   // capture: the first launch of a configuration is always eager)

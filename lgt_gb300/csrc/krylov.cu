@@ -181,19 +181,35 @@ __global__ void __launch_bounds__(kT) k_update(const S* __restrict__ V, size_t v
   if (act) {
     for (int64_t row = r0 + rg; row < r1; row += RG) {
       const size_t off = size_t(row) * C;
-      double w = double(W[off + c]);
-      for (int i = 0; i < Ju; ++i) {
-        const double hr = h[(size_t(i) * K + k) * 2 + 0];
-        const double v = double(V[size_t(i) * vstride + off + c]);
-        if (NC == 1) {
-          w = fma(-hr, v, w);
-        } else {
-          const double hi = h[(size_t(i) * K + k) * 2 + 1];
-          const double vp = double(V[size_t(i) * vstride + off + (c ^ 1)]);
+      // two independent chains (even / odd basis vectors)
+      double w0 = double(W[off + c]), w1 = 0.0;
+      int i = 0;
+      for (; i + 1 < Ju; i += 2) {
+        const double hr0 = h[(size_t(i) * K + k) * 2 + 0];
+        const double hr1 = h[(size_t(i + 1) * K + k) * 2 + 0];
+        const double v0 = double(V[size_t(i) * vstride + off + c]);
+        const double v1 = double(V[size_t(i + 1) * vstride + off + c]);
+        w0 = fma(-hr0, v0, w0);
+        w1 = fma(-hr1, v1, w1);
+        if (NC == 2) {
           // (hr + i hi)(v_re + i v_im): re = hr v_re - hi v_im, im = hr v_im + hi v_re
-          w = (c & 1) ? (w - (hr * v + hi * vp)) : (w - (hr * v - hi * vp));
+          const double hi0 = h[(size_t(i) * K + k) * 2 + 1];
+          const double hi1 = h[(size_t(i + 1) * K + k) * 2 + 1];
+          const double vp0 = double(V[size_t(i) * vstride + off + (c ^ 1)]);
+          const double vp1 = double(V[size_t(i + 1) * vstride + off + (c ^ 1)]);
+          w0 = fma((c & 1) ? -hi0 : hi0, vp0, w0);
+          w1 = fma((c & 1) ? -hi1 : hi1, vp1, w1);
         }
       }
+      if (i < Ju) {
+        const double hr = h[(size_t(i) * K + k) * 2 + 0];
+        w0 = fma(-hr, double(V[size_t(i) * vstride + off + c]), w0);
+        if (NC == 2) {
+          const double hi = h[(size_t(i) * K + k) * 2 + 1];
+          w0 = fma((c & 1) ? -hi : hi, double(V[size_t(i) * vstride + off + (c ^ 1)]), w0);
+        }
+      }
+      const double w = w0 + w1;
       if (Ju > 0) W[off + c] = S(w);
       const double ws = double(S(w));
       nrm = fma(ws, ws, nrm);
@@ -245,20 +261,28 @@ __global__ void k_finish_norm(const double* npart, int nblk, int K, int C, int n
 }
 
 // dst = src / bnorm per column for points with status == sel.  dst is panel
-// (*jstate + dst_off) of `dstbase` when jstate is given.
+// (*jstate + dst_off) of `dstbase` when jstate is given.  Each thread owns one
+// column (one reciprocal, no per-element division or modulo); launched with
+// kT threads per block.
 template <typename SI, typename SO>
 __global__ void k_scale(const SI* src, SO* dstbase, size_t vstride, const int* jstate, int dst_off,
                         int64_t N, int C, int ncomp, const double* bnorm, const int* status,
                         int sel) {
   SO* dst = dstbase + size_t((jstate ? *jstate : 0) + dst_off) * vstride;
-  const int64_t n = N * C;
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
-       i += int64_t(gridDim.x) * blockDim.x) {
-    const int c = int(i % C);
-    const int k = c / ncomp;
-    if (status && status[k] != sel) continue;
-    const double b = bnorm[k];
-    dst[i] = SO(b > 0.0 ? double(src[i]) / b : 0.0);
+  const int RG = kT / C;
+  const int c = threadIdx.x % C, rg = threadIdx.x / C;
+  if (rg >= RG) return;
+  const int k = c / ncomp;
+  if (status && status[k] != sel) return;
+  const double b = bnorm[k];
+  const double inv = (b > 0.0) ? 1.0 / b : 0.0;
+  const float invf = float(inv);
+  for (int64_t row = int64_t(blockIdx.x) * RG + rg; row < N; row += int64_t(gridDim.x) * RG) {
+    const size_t i = size_t(row) * C + c;
+    if (sizeof(SI) == 4 && sizeof(SO) == 4)
+      dst[i] = SO(float(src[i]) * invf);
+    else
+      dst[i] = SO(double(src[i]) * inv);
   }
 }
 

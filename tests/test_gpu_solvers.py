@@ -84,3 +84,29 @@ def test_string_sector_and_start_vector(oracle, lgt):
     E0o = oracle.ground_state(oracle.build_hamiltonian(ob, g=1.0, t=1.0, m=2.0))[0]
     assert abs(E0 - E0o) <= 1e-10 * abs(E0o)
     H.close()
+
+
+@pytest.mark.parametrize("precision,tol_state", [("fp64", 1e-9), ("fp32_mixed", 2e-5)])
+@pytest.mark.parametrize("model", ["ref", "pjw"])
+def test_quench_4x3_batched(oracle, lgt, precision, tol_state, model):
+    """Real-time quench on the 4x3 lattice (N = 72211), two coupling points
+    in one panel, from the staggered product state: states after 5 steps of
+    dt = 0.05 against exp(-iHt) of the oracle; norm drift and energy
+    conservation."""
+    ob, gb = _basis(oracle, lgt, 4, 3)
+    gs = np.array([0.7, 1.3])
+    H = lgt.build_hamiltonian(gb, g=gs, t=1.0, m=0.5, model=model)
+    v0 = lgt.staggered_product_state(gb)
+    p0 = np.stack([v0, v0], axis=1)
+    data, psi, drift = lgt.evolve_ED(p0, H, dt=0.05, n_steps=5, tol=1e-12, precision=precision,
+                                     return_state=True)
+    for k in range(2):
+        Ho = oracle.build_hamiltonian(ob, g=gs[k], t=1.0, m=0.5, model=model)
+        po, do = oracle.evolve(v0, Ho, ob, dt=0.05, n_steps=5)
+        assert np.linalg.norm(psi[:, k] - po) <= tol_state
+        assert abs(data[-1][k]["E2_mean"] - do[-1]["E2_mean"]) <= 10 * tol_state
+        e0 = np.vdot(v0, Ho @ v0).real
+        e1 = np.vdot(psi[:, k], Ho @ psi[:, k]).real
+        assert abs(e1 - e0) <= 100 * tol_state * abs(e0)
+    assert np.all(drift < (1e-12 if precision == "fp64" else 1e-5))
+    H.close()
