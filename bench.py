@@ -372,10 +372,13 @@ def roofline(L, C, lib, torch, stream, dev, reps=10):
     out = {"N": N, "basis_build_s": basis_s}
     for model in ("ref", "pjw"):
         H = L.build_hamiltonian(b, g=gs, t=1.0, m=0.5, model=model)
-        for prec, dtype, s in (("fp64", torch.float64, 16), ("fp32", torch.float32, 8)):
+        for prec, dtype, s, generic in (("fp64", torch.float64, 16, False),
+                                        ("fp32", torch.float32, 8, False),
+                                        ("fp64", torch.float64, 16, True),
+                                        ("fp32", torch.float32, 8, True)):
             x = torch.randn((N, RF_K, 2), dtype=dtype, device="cuda")
             y = torch.empty_like(x)
-            flags = C.LGT_DEVICE_PTRS | C.LGT_ASYNC
+            flags = C.LGT_DEVICE_PTRS | C.LGT_ASYNC | (C.LGT_GENERIC_KERNELS if generic else 0)
             code = C.LGT_FP64 if prec == "fp64" else C.LGT_FP32
             ts = []
             for it in range(reps + 2):
@@ -390,7 +393,8 @@ def roofline(L, C, lib, torch, stream, dev, reps=10):
                     ts.append(e0.elapsed_time(e1) * 1e-3)
             t = statistics.mean(ts)
             algo = N * 8 + 2 * RF_K * N * s   # key table + x + y, neighbour gathers 0
-            out["%s_%s" % (model, prec)] = {"ms": t * 1e3, "algo_bytes": algo,
+            out["%s_%s%s" % (model, prec, "_generic" if generic else "")] = {
+                                            "ms": t * 1e3, "algo_bytes": algo,
                                             "gbs": algo / t / 1e9, "frac": algo / t / 1e9 / peak}
             del x, y
         H.close()

@@ -75,8 +75,10 @@ enum {
 
 enum {
   LGT_DEVICE_PTRS = 1, /* amplitude pointers are device pointers                  */
-  LGT_ASYNC = 2        /* with LGT_DEVICE_PTRS: lgt_matvec returns without waiting
+  LGT_ASYNC = 2,       /* with LGT_DEVICE_PTRS: lgt_matvec returns without waiting
                           for the kernel (stream-ordered; no self-check read)   */
+  LGT_GENERIC_KERNELS = 4 /* lgt_matvec: use the run-time-geometry H*psi kernel
+                          even where a fixed-shape one exists (cross-checks)    */
 };
 
 typedef struct lgt_basis lgt_basis;

@@ -37,6 +37,7 @@ LGT_SOLVER_CTA = 2
 
 LGT_DEVICE_PTRS = 1
 LGT_ASYNC = 2
+LGT_GENERIC_KERNELS = 4
 
 # every symbol include/lgt_ed.h declares
 EXPORTS = (

@@ -409,7 +409,8 @@ lgt_status lgt_matvec(const lgt_ham* hc, const void* x, void* y, int32_t ncomp, 
     dx = h->x.p;
     dy = h->y.p;
   }
-  const OpDev op = h->op();
+  OpDev op = h->op();
+  op.force_generic = (flags & LGT_GENERIC_KERNELS) ? 1 : 0;
   cudaError_t e = (precision == LGT_FP64)
                       ? apply_h_d(op, static_cast<const double*>(dx), static_cast<double*>(dy), ncomp, s)
                       : apply_h_f(op, static_cast<const float*>(dx), static_cast<float*>(dy), ncomp, s);

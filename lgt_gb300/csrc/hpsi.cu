@@ -240,16 +240,35 @@ cudaError_t launch_v(const HpsiArgs<T>& a, uint32_t model, cudaStream_t s) {
 int hpsi_seg_smem_default(int nmasks) { return (nmasks + 1) * 4 <= 16 * 1024 ? 1 : 0; }
 
 template <typename T>
-cudaError_t launch_hpsi(HpsiArgs<T> a, uint32_t model, cudaStream_t s) {
+bool vec_ok(const HpsiArgs<T>& a) {
   constexpr int VW = 16 / int(sizeof(T));
-  const bool vec_ok = (a.C % VW == 0) && ((reinterpret_cast<uintptr_t>(a.x) & 15) == 0) &&
-                      ((reinterpret_cast<uintptr_t>(a.y) & 15) == 0);
-  if (vec_ok) return launch_v<T, VW>(a, model, s);
+  const size_t xs = a.xsel ? a.xstride * sizeof(T) : 0;
+  return (a.C % VW == 0) && ((reinterpret_cast<uintptr_t>(a.x) & 15) == 0) &&
+         ((reinterpret_cast<uintptr_t>(a.y) & 15) == 0) && (xs % 16 == 0);
+}
+
+template <typename T>
+cudaError_t launch_hpsi_generic(HpsiArgs<T> a, uint32_t model, cudaStream_t s) {
+  constexpr int VW = 16 / int(sizeof(T));
+  if (vec_ok(a)) return launch_v<T, VW>(a, model, s);
   return launch_v<T, 1>(a, model, s);
+}
+
+template <typename T>
+cudaError_t launch_hpsi(HpsiArgs<T> a, uint32_t model, cudaStream_t s) {
+  const Geom& G = a.G;
+  if (!a.force_generic && G.dg == 1 && a.R.tab && a.N < (int64_t(1) << 31) && vec_ok(a)) {
+    if (G.nx == 4 && G.ny == 4) return launch_hpsi_4x4(a, model, s);
+    if (G.nx == 4 && G.ny == 3) return launch_hpsi_4x3(a, model, s);
+    if (G.nx == 3 && G.ny == 4) return launch_hpsi_3x4(a, model, s);
+  }
+  return launch_hpsi_generic(a, model, s);
 }
 
 template cudaError_t launch_hpsi<double>(HpsiArgs<double>, uint32_t, cudaStream_t);
 template cudaError_t launch_hpsi<float>(HpsiArgs<float>, uint32_t, cudaStream_t);
+template cudaError_t launch_hpsi_generic<double>(HpsiArgs<double>, uint32_t, cudaStream_t);
+template cudaError_t launch_hpsi_generic<float>(HpsiArgs<float>, uint32_t, cudaStream_t);
 
 // ----------------------------------------------------------------------------
 // CSR export (parity checks and the reference's nnz(H), finite_ed.jl:355)

@@ -1,0 +1,15 @@
+// hpsi_3x4.cu -- fixed-shape H*psi for the 3x4 lattice (one translation
+// unit per shape so the unrolled kernels compile in parallel).
+#include "lgt_hpsi_fixed.cuh"
+
+namespace lgt {
+
+cudaError_t launch_hpsi_3x4(const HpsiArgs<float>& a, uint32_t model, cudaStream_t s) {
+  return fixed::launch_shape<3, 4, float>(a, model, s);
+}
+
+cudaError_t launch_hpsi_3x4(const HpsiArgs<double>& a, uint32_t model, cudaStream_t s) {
+  return fixed::launch_shape<3, 4, double>(a, model, s);
+}
+
+}  // namespace lgt

@@ -735,6 +735,7 @@ cudaError_t apply_h<double>(const OpDev& op, const double* x, const int* xsel, s
   a.seg_smem = op.seg_smem;
   a.xsel = xsel;
   a.xstride = xstride;
+  a.force_generic = op.force_generic;
   return launch_hpsi<double>(a, op.model, s);
 }
 
@@ -758,6 +759,7 @@ cudaError_t apply_h<float>(const OpDev& op, const float* x, const int* xsel, siz
   a.seg_smem = op.seg_smem;
   a.xsel = xsel;
   a.xstride = xstride;
+  a.force_generic = op.force_generic;
   return launch_hpsi<float>(a, op.model, s);
 }
 

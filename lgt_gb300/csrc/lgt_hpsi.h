@@ -25,13 +25,30 @@ struct HpsiArgs {
   // Lets one captured CUDA graph apply H to "the current Krylov vector".
   const int* xsel;
   size_t xstride;
+  int force_generic = 0;  // 1: run-time-geometry kernel even for a fixed shape
 };
 
 // Default staging decision for the top-level rank table.
 int hpsi_seg_smem_default(int nmasks);
 
+// y = H x.  Lattices with a compile-time kernel (4x4, 4x3, 3x4 at dg = 1,
+// rank tables present, vector-aligned panels) use it; all others the
+// run-time-geometry kernel.  Both give the same product.
 template <typename T>
 cudaError_t launch_hpsi(HpsiArgs<T> a, uint32_t model, cudaStream_t s);
+
+// The run-time-geometry kernel alone (tests compare the two paths).
+template <typename T>
+cudaError_t launch_hpsi_generic(HpsiArgs<T> a, uint32_t model, cudaStream_t s);
+
+// Fixed-shape kernels, one translation unit each (hpsi_<nx>x<ny>.cu).
+#define LGT_DECLARE_FIXED_SHAPE(NX, NY)                                                   \
+  cudaError_t launch_hpsi_##NX##x##NY(const HpsiArgs<float>& a, uint32_t model, cudaStream_t s); \
+  cudaError_t launch_hpsi_##NX##x##NY(const HpsiArgs<double>& a, uint32_t model, cudaStream_t s);
+LGT_DECLARE_FIXED_SHAPE(4, 4)
+LGT_DECLARE_FIXED_SHAPE(4, 3)
+LGT_DECLARE_FIXED_SHAPE(3, 4)
+#undef LGT_DECLARE_FIXED_SHAPE
 
 cudaError_t launch_row_nnz(const Geom& G, const RankView& R, uint32_t model, int64_t* counts,
                            cudaStream_t s);

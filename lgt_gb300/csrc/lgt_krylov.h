@@ -19,6 +19,7 @@ struct OpDev {
   int seg_smem;
   const double *cE_d, *cm_d, *ch_d, *cp_d;
   const float *cE_f, *cm_f, *ch_f, *cp_f;
+  int force_generic = 0;  // H*psi through the run-time-geometry kernel only
 };
 
 struct KrylovParams {

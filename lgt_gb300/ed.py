@@ -323,25 +323,29 @@ class Hamiltonian:
             return np.ascontiguousarray(p), 2
         return np.ascontiguousarray(x, dtype=dtype), 1
 
-    def matvec(self, x, precision="fp64"):
+    def matvec(self, x, precision="fp64", generic=False):
         """y = H x for host arrays: x of shape (N,) (K = 1) or (N, K), real or
-        complex; precision "fp64" or "fp32"."""
+        complex; precision "fp64" or "fp32".  ``generic`` forces the
+        run-time-geometry kernel where a fixed-shape one exists."""
         prec = _PREC[precision]
         dtype = np.float64 if prec == C.LGT_FP64 else np.float32
         xin = np.asarray(x)
         px, nc = self._panel(xin, dtype)
         py = np.empty_like(px)
-        C.check(C.load().lgt_matvec(self._h, _p(px), _p(py), nc, prec, 0))
+        flags = C.LGT_GENERIC_KERNELS if generic else 0
+        C.check(C.load().lgt_matvec(self._h, _p(px), _p(py), nc, prec, flags))
         if nc == 2:
             y = py[..., 0] + 1j * py[..., 1]
         else:
             y = py
         return y.reshape(xin.shape)
 
-    def matvec_device(self, x_ptr: int, y_ptr: int, ncomp: int = 1, precision="fp64"):
+    def matvec_device(self, x_ptr: int, y_ptr: int, ncomp: int = 1, precision="fp64",
+                      generic=False):
         """y = H x on device panels [N][K][ncomp] (raw device pointers)."""
+        flags = C.LGT_DEVICE_PTRS | (C.LGT_GENERIC_KERNELS if generic else 0)
         C.check(C.load().lgt_matvec(self._h, ctypes.c_void_p(x_ptr), ctypes.c_void_p(y_ptr),
-                                    ncomp, _PREC[precision], C.LGT_DEVICE_PTRS))
+                                    ncomp, _PREC[precision], flags))
 
     def energy(self, psi) -> np.ndarray:
         """<psi|H|psi> / <psi|psi> per point, FP64."""
