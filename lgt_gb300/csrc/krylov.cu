@@ -560,6 +560,36 @@ __global__ void k_combine(const S* __restrict__ V, size_t vstride, const double*
   }
 }
 
+// Split exponential (real Krylov columns 2k = Re psi_k and 2k+1 = Im psi_k,
+// each with complex coefficients c = rho exp(-i tau T) e_0 from its own
+// tridiagonal): psi_k = sum_i c^re_i V_i[2k] + i sum_i c^im_i V_i[2k+1].
+template <typename S>
+__global__ void k_combine_split(const S* __restrict__ V, size_t vstride, const double* coef,
+                                int ldT, const int* len, double* out, int64_t N, int K) {
+  const int C = 2 * K;
+  const int64_t n = N * C;
+  for (int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; idx < n;
+       idx += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t row = idx / C;
+    const int c = int(idx - row * C);
+    const int comp = c & 1, ca = c & ~1, cb = ca + 1;
+    const size_t off = size_t(row) * C;
+    double acc = 0.0;
+    const int na = len[ca], nb = len[cb];
+    // the real column contributes (Re c) v to Re psi and (Im c) v to Im psi
+    for (int i = 0; i < na; ++i)
+      acc = fma(coef[(size_t(ca) * ldT + i) * 2 + comp], double(V[size_t(i) * vstride + off + ca]),
+                acc);
+    // i (cr + i ci) v = -ci v + i cr v
+    for (int i = 0; i < nb; ++i) {
+      const double cf = comp ? coef[(size_t(cb) * ldT + i) * 2 + 0]
+                             : -coef[(size_t(cb) * ldT + i) * 2 + 1];
+      acc = fma(cf, double(V[size_t(i) * vstride + off + cb]), acc);
+    }
+    out[off + c] = acc;
+  }
+}
+
 __global__ void k_residual_parts(const double* X, const double* HX, const double* E, int64_t N,
                                  int C, int ncomp, int64_t rpb, double* npart) {
   __shared__ double red[kT];
@@ -619,6 +649,11 @@ template <typename S>
 struct Work {
   int64_t N = -1;
   int C = 0, K = 0, ncomp = 1, m = 0, ldT = 0;
+  // Components per coupling point seen by H*psi: equal to ncomp, except in
+  // the split exponential, where the Krylov columns are real (ncomp = 1)
+  // and H*psi pairs them as (re, im) of one point (hcomp = 2).
+  int hcomp = 1;
+  bool lite = false;  // reduction buffers only (no Krylov panels)
   size_t vstride = 0;
   S* V = nullptr;        // m+1 Krylov panels
   S* W = nullptr;        // H V_j, then the new residual vector
@@ -646,20 +681,28 @@ struct Work {
   double graph_tiny = 0.0;
   int graph_nodes = 0;
 
-  std::string ensure(int64_t N_, int C_, int K_, int ncomp_, int m_) {
-    if (N_ == N && C_ == C && K_ == K && ncomp_ == ncomp && m_ == m && V) return std::string();
+  std::string ensure(int64_t N_, int C_, int K_, int ncomp_, int m_, int hcomp_ = 0,
+                     bool lite_ = false) {
+    if (hcomp_ <= 0) hcomp_ = ncomp_;
+    if (N_ == N && C_ == C && K_ == K && ncomp_ == ncomp && m_ == m && hcomp_ == hcomp &&
+        lite_ == lite && part)
+      return std::string();
     release();
     N = N_;
     C = C_;
     K = K_;
     ncomp = ncomp_;
     m = m_;
+    hcomp = hcomp_;
+    lite = lite_;
     ldT = m + 1;
     vstride = size_t(N) * C;
     red.plan(N, C);
-    KCK(cudaMalloc(&V, sizeof(S) * vstride * (m + 1)));
-    KCK(cudaMalloc(&W, sizeof(S) * vstride));
-    KCK(cudaMalloc(&R, sizeof(double) * vstride));
+    if (!lite) {
+      KCK(cudaMalloc(&V, sizeof(S) * vstride * (m + 1)));
+      KCK(cudaMalloc(&W, sizeof(S) * vstride));
+      KCK(cudaMalloc(&R, sizeof(double) * vstride));
+    }
     KCK(cudaMalloc(&part, sizeof(double) * size_t(red.nblk) * ldT * 2 * C));
     KCK(cudaMalloc(&npart, sizeof(double) * size_t(red.nblk) * C));
     KCK(cudaMalloc(&h, sizeof(double) * size_t(ldT) * K * 2));
@@ -797,7 +840,7 @@ cudaError_t launch_update(Work<S>& w, S* Wp, cudaStream_t s, const int* need = n
 template <typename S>
 cudaError_t lanczos_step(const OpDev& op, Work<S>& w, int reorth, double tiny_rel,
                          cudaStream_t s) {
-  cudaError_t e = apply_h<S>(op, w.V, w.jstate, w.vstride, w.W, w.ncomp, s);
+  cudaError_t e = apply_h<S>(op, w.V, w.jstate, w.vstride, w.W, w.hcomp, s);
   if (e != cudaSuccess) return e;
   const int fdb = (w.ldT * w.K + 127) / 128;
   // Classical Gram-Schmidt against the whole basis (this also performs the
@@ -1059,25 +1102,33 @@ std::string ground_state_impl(const OpDev& op, const KrylovParams& p, Work<S>& w
   return std::string();
 }
 
+// Krylov exp(-i dt H) steps.  H is real, so exp(-i tau H)(a + i b) =
+// exp(-i tau H) a + i exp(-i tau H) b: the real and imaginary parts of each
+// point's state are propagated as two real Krylov columns (real
+// Gram-Schmidt: half the FP64 work of complex columns) and recombined with
+// complex coefficients.  Each column's error estimate must meet tol / sqrt 2,
+// so the point's combined error meets tol.
 template <typename S>
 std::string expm_impl(const OpDev& op, const KrylovParams& p, Work<S>& w, double dt, int n_steps,
                       double* X, double* drift, StepObserver* obs, cudaStream_t s,
                       KrylovReport* rep) {
   const int64_t N = op.R.dim;
-  const int K = op.K;
-  const int ncomp = 2, C = 2 * K;
+  const int K = op.K;       // coupling points (complex columns of X)
+  const int C = 2 * K;      // real Krylov columns
+  const int Kc = C;         // Krylov "points": one per real column
   int m = p.krylovdim;
   if (m > N) m = int(N);
   if (m > kMaxDim - 1) m = kMaxDim - 1;
   if (m < 1) m = 1;
-  std::string err = w.ensure(N, C, K, ncomp, m);
+  std::string err = w.ensure(N, C, Kc, 1, m, 2);
   if (!err.empty()) {
     w.release();
     return err;
   }
   const double tiny_rel = (sizeof(S) == 8) ? 1e-12 : 1e-6;
-  std::vector<int> st(K);
-  std::vector<double> errs(K, 0.0), nrm(K);
+  const double tol = p.tol / sqrt(2.0);
+  std::vector<int> st(Kc);
+  std::vector<double> errs(Kc, 0.0), nrm(K);
   if (drift)
     for (int k = 0; k < K; ++k) drift[k] = 0.0;
   int64_t matvecs = 0;
@@ -1092,14 +1143,24 @@ std::string expm_impl(const OpDev& op, const KrylovParams& p, Work<S>& w, double
     err = obs->on_step(0, X);
     if (!err.empty()) return err;
   }
+  auto all_converged = [&](bool* out) -> std::string {
+    KCK(cudaMemcpyAsync(st.data(), w.status, sizeof(int) * Kc, cudaMemcpyDeviceToHost, s));
+    KCK(cudaStreamSynchronize(s));
+    bool a = true;
+    for (int k = 0; k < Kc; ++k) a = a && (st[k] >= kConverged);
+    *out = a;
+    return std::string();
+  };
   for (int step = 1; step <= n_steps; ++step) {
     double remaining = dt;
     int guard_sub = 0;
     while (remaining > 0.0) {
-      KCK(cudaMemsetAsync(w.status, 0, sizeof(int) * K, s));
-      KCK(cudaMemsetAsync(w.len, 0, sizeof(int) * K, s));
+      KCK(cudaMemsetAsync(w.status, 0, sizeof(int) * Kc, s));
+      KCK(cudaMemsetAsync(w.len, 0, sizeof(int) * Kc, s));
       err = reset_cycle<S>(w, s);
       if (!err.empty()) return err;
+      // V_0 = column / ||column|| (a zero column, e.g. Im psi = 0, spans an
+      // empty Krylov space: it is exhausted at once and contributes 0)
       err = start_from<S>(w, X, s);
       if (!err.empty()) return err;
       int j = 0;
@@ -1109,53 +1170,53 @@ std::string expm_impl(const OpDev& op, const KrylovParams& p, Work<S>& w, double
         err = run_steps<S>(op, w, p, steps, tiny_rel, s, &matvecs);
         if (!err.empty()) return err;
         j += steps;
-        k_check_expm<<<K, 64, 0, s>>>(w.alpha, w.beta, w.ldT, w.status, w.len, w.rho, remaining,
-                                      w.resid, w.coef, p.tol, 0, w.fail), lgt::note_launch();
+        k_check_expm<<<Kc, 64, 0, s>>>(w.alpha, w.beta, w.ldT, w.status, w.len, w.rho, remaining,
+                                       w.resid, w.coef, tol, 0, w.fail), lgt::note_launch();
         KCK(cudaGetLastError());
-        KCK(cudaMemcpyAsync(st.data(), w.status, sizeof(int) * K, cudaMemcpyDeviceToHost, s));
-        KCK(cudaStreamSynchronize(s));
-        all = true;
-        for (int k = 0; k < K; ++k) all = all && (st[k] >= kConverged);
+        err = all_converged(&all);
+        if (!err.empty()) return err;
         if (all) break;
       }
       double tau = remaining;
       if (!all) {
         // The Krylov space is too small for the whole interval: take the
         // largest tau = remaining / 2^q meeting the tolerance (scaled to the
-        // sub-interval) for every point, then continue from there.
+        // sub-interval) for every column, then continue from there.
         double t = remaining;
         for (int q = 0; q < 40; ++q) {
           t *= 0.5;
-          k_check_expm<<<K, 64, 0, s>>>(w.alpha, w.beta, w.ldT, w.status, w.len, w.rho, t,
-                                        w.resid, w.coef, p.tol * (t / dt), 0, w.fail), lgt::note_launch();
-          KCK(cudaMemcpyAsync(st.data(), w.status, sizeof(int) * K, cudaMemcpyDeviceToHost, s));
-          KCK(cudaStreamSynchronize(s));
-          bool ok = true;
-          for (int k = 0; k < K; ++k) ok = ok && (st[k] >= kConverged);
+          k_check_expm<<<Kc, 64, 0, s>>>(w.alpha, w.beta, w.ldT, w.status, w.len, w.rho, t,
+                                         w.resid, w.coef, tol * (t / dt), 0, w.fail), lgt::note_launch();
+          bool ok = false;
+          err = all_converged(&ok);
+          if (!err.empty()) return err;
           if (ok) break;
         }
         tau = t;
-        KCK(cudaMemsetAsync(w.status, 0, sizeof(int) * K, s));
-        k_check_expm<<<K, 64, 0, s>>>(w.alpha, w.beta, w.ldT, w.status, w.len, w.rho, tau,
-                                      w.resid, w.coef, p.tol, 1, w.fail), lgt::note_launch();
+        KCK(cudaMemsetAsync(w.status, 0, sizeof(int) * Kc, s));
+        k_check_expm<<<Kc, 64, 0, s>>>(w.alpha, w.beta, w.ldT, w.status, w.len, w.rho, tau,
+                                       w.resid, w.coef, tol, 1, w.fail), lgt::note_launch();
         KCK(cudaGetLastError());
         ++substeps;
         if (++guard_sub > 4096) return std::string("NOCONV: exponential step could not be split");
       }
-      KCK(cudaMemcpyAsync(errs.data(), w.resid, sizeof(double) * K, cudaMemcpyDeviceToHost, s));
-      k_combine<S, 2><<<grid_for(N * C), kT, 0, s>>>(w.V, w.vstride, w.coef, w.ldT, w.len,
-                                                     w.status, kConverged, X, N, C, ncomp), lgt::note_launch();
+      KCK(cudaMemcpyAsync(errs.data(), w.resid, sizeof(double) * Kc, cudaMemcpyDeviceToHost, s));
+      k_combine_split<S><<<grid_for(N * C), kT, 0, s>>>(w.V, w.vstride, w.coef, w.ldT, w.len, X, N,
+                                                        K), lgt::note_launch();
       KCK(cudaGetLastError());
       KCK(cudaStreamSynchronize(s));
-      for (int k = 0; k < K; ++k) maxerr = fmax(maxerr, errs[k]);
+      for (int k = 0; k < K; ++k) maxerr = fmax(maxerr, hypot(errs[2 * k], errs[2 * k + 1]));
       remaining -= tau;
       if (remaining < 1e-15 * dt) remaining = 0.0;
     }
-    // psi ./= norm(psi)   (finite_ed.jl:420)
-    KCK(cudaMemsetAsync(w.status, 0, sizeof(int) * K, s));
-    err = colnorms_double<S>(w, X, w.rho, s);
-    if (!err.empty()) return err;
-    k_scale<double, double><<<grid_for(N * C), kT, 0, s>>>(X, X, 0, nullptr, 0, N, C, ncomp, w.rho,
+    // psi ./= norm(psi) per point (finite_ed.jl:420): the point view of the
+    // panel, K complex columns
+    k_residual_parts<<<w.red.nblk, kT, 0, s>>>(X, X, w.zeros, N, C, 2, w.red.rpb,
+                                               w.npart), lgt::note_launch();
+    k_finish_norm<<<(K + 63) / 64, 64, 0, s>>>(w.npart, w.red.nblk, K, C, 2, w.jstate, w.beta,
+                                               w.alpha, w.ldT, w.status, w.len, w.rho, 0.0,
+                                               0), lgt::note_launch();
+    k_scale<double, double><<<grid_for(N * C), kT, 0, s>>>(X, X, 0, nullptr, 0, N, C, 2, w.rho,
                                                             nullptr, 0), lgt::note_launch();
     KCK(cudaGetLastError());
     if (drift) {
@@ -1194,11 +1255,13 @@ struct KrylovCache {
   Work<float> gs_f;
   Work<double> ex_d;
   Work<float> ex_f;
+  Work<double> dots;  // reduction buffers of panel_dots only
   ~KrylovCache() {
     gs_d.release();
     gs_f.release();
     ex_d.release();
     ex_f.release();
+    dots.release();
   }
 };
 
@@ -1215,9 +1278,8 @@ cudaError_t apply_h_f(const OpDev& op, const float* x, float* y, int ncomp, cuda
 
 std::string panel_dots(KrylovCache* cache, const double* x, const double* y, int64_t N, int K,
                        int ncomp, double* out, cudaStream_t s) {
-  Work<double>& w = cache->ex_d;
-  // any workspace of matching shape serves; (re)shape the exponential one
-  std::string err = w.ensure(N, K * ncomp, K, ncomp, w.m > 0 ? w.m : 1);
+  Work<double>& w = cache->dots;
+  std::string err = w.ensure(N, K * ncomp, K, ncomp, 1, ncomp, true);
   if (!err.empty()) return err;
   return dots_ws<double>(w, x, y, out, s);
 }

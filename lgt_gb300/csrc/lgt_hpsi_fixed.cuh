@@ -15,8 +15,9 @@
 //
 // Phase 1 (lane = row) writes the row's neighbour indices into shared
 // memory, hops first, then plaquette moves; bit 31 of a hop entry is its
-// Jordan-Wigner parity.  Phase 2 (lanes over (row, W-column slice)) gathers
-// x rows with VPL vector loads of V elements per neighbour.
+// Jordan-Wigner parity.  Phase 2 (lanes over (row, column slice)) gathers
+// x rows: each of a row's lanes loads VPL vectors of V elements per
+// neighbour.
 #pragma once
 
 #include "lgt_hpsi.h"
@@ -292,7 +293,10 @@ __global__ void __launch_bounds__(kThreads, PLAQ ? LGT_FIXED_MINB_PLAQ : LGT_FIX
     const int rl = it / lpr;
     const int64_t row = warp_row0 + rl;
     if (row >= a.N) continue;
+    // lane slice: W contiguous columns (interleaving the row's lanes so that
+    // one load instruction covers whole sectors measured slower)
     const int col0 = (it - rl * lpr) * W;
+    constexpr int qstep = V;
     const uint32_t m = s_meta[wid * 32 + rl];
     const int cnt = int(m & 255u), nh = int((m >> 8) & 255u);
     const T e2 = T(int((m >> 16) & 255u)), stag = T(int(m >> 24) - 128);
@@ -300,7 +304,7 @@ __global__ void __launch_bounds__(kThreads, PLAQ ? LGT_FIXED_MINB_PLAQ : LGT_FIX
     T ah[W], ap[W], xd[W], xs[LGT_FIXED_UNROLL][W];
     const T* px = x + size_t(row) * C + col0;
 #pragma unroll
-    for (int q = 0; q < VPL; ++q) ld<T, V>(px + q * V, xd + q * V);
+    for (int q = 0; q < VPL; ++q) ld<T, V>(px + q * qstep, xd + q * V);
 #pragma unroll
     for (int e = 0; e < W; ++e) {
       ah[e] = T(0);
@@ -316,7 +320,7 @@ __global__ void __launch_bounds__(kThreads, PLAQ ? LGT_FIXED_MINB_PLAQ : LGT_FIX
         if (n + u < nh) {
           const T* p = x + size_t(ent[u] & 0x7fffffffu) * C + col0;
 #pragma unroll
-          for (int q = 0; q < VPL; ++q) ld<T, V>(p + q * V, xs[u] + q * V);
+          for (int q = 0; q < VPL; ++q) ld<T, V>(p + q * qstep, xs[u] + q * V);
         } else {
 #pragma unroll
           for (int e = 0; e < W; ++e) xs[u][e] = T(0);
@@ -341,7 +345,7 @@ __global__ void __launch_bounds__(kThreads, PLAQ ? LGT_FIXED_MINB_PLAQ : LGT_FIX
           if (n + u < cnt) {
             const T* p = x + size_t(lst[n + u]) * C + col0;
 #pragma unroll
-            for (int q = 0; q < VPL; ++q) ld<T, V>(p + q * V, xs[u] + q * V);
+            for (int q = 0; q < VPL; ++q) ld<T, V>(p + q * qstep, xs[u] + q * V);
           } else {
 #pragma unroll
             for (int e = 0; e < W; ++e) xs[u][e] = T(0);
@@ -355,7 +359,8 @@ __global__ void __launch_bounds__(kThreads, PLAQ ? LGT_FIXED_MINB_PLAQ : LGT_FIX
     }
 #pragma unroll
     for (int e = 0; e < W; ++e) {
-      const int k = (ncomp == 2) ? ((col0 + e) >> 1) : (col0 + e);
+      const int col = col0 + (e / V) * qstep + (e % V);
+      const int k = (ncomp == 2) ? (col >> 1) : col;
       const T cd = s_coef[k] * e2 + s_coef[K + k] * stag;  // (g^2/2) e2 + m stag
       T v = fma(s_coef[2 * K + k], ah[e], cd * xd[e]);
       if (PLAQ) v = fma(s_coef[3 * K + k], ap[e], v);
@@ -363,7 +368,7 @@ __global__ void __launch_bounds__(kThreads, PLAQ ? LGT_FIXED_MINB_PLAQ : LGT_FIX
     }
     T* py = y + size_t(row) * C + col0;
 #pragma unroll
-    for (int q = 0; q < VPL; ++q) st<T, V>(py + q * V, xd + q * V);
+    for (int q = 0; q < VPL; ++q) st<T, V>(py + q * qstep, xd + q * V);
   }
 }
 
