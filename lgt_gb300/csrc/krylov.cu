@@ -31,6 +31,12 @@ namespace {
 constexpr int kT = 256;   // threads of the panel kernels
 constexpr int kIC = 8;    // Krylov vectors per multidot pass
 constexpr int kMaxDim = 64;
+#ifndef LGT_MD_ROWS
+#define LGT_MD_ROWS 1  // rows per trip of the Gram-Schmidt dot kernel (2 measured slower)
+#endif
+#ifndef LGT_UPD_CHAINS
+#define LGT_UPD_CHAINS 2  // independent FMA chains of the update (4 measured slower)
+#endif
 
 #define KCK(call)                                                                  \
   do {                                                                             \
@@ -91,16 +97,30 @@ __global__ void __launch_bounds__(kT) k_multidot(const S* __restrict__ V, size_t
 #pragma unroll
     for (int q = 0; q < kIC; ++q) a[q] = b[q] = 0.0;
     if (act) {
-      for (int64_t row = r0 + rg; row < r1; row += RG) {
-        const size_t off = size_t(row) * C;
-        const double w = double(W[off + c]);
-        const double wx = (NC == 2) ? double(W[off + (c ^ 1)]) : 0.0;
+      // LGT_MD_ROWS rows per trip: more independent loads in flight
+      for (int64_t row = r0 + rg; row < r1; row += int64_t(RG) * LGT_MD_ROWS) {
+        double w[LGT_MD_ROWS], wx[LGT_MD_ROWS];
+        size_t off[LGT_MD_ROWS];
+        bool ok[LGT_MD_ROWS];
+#pragma unroll
+        for (int u = 0; u < LGT_MD_ROWS; ++u) {
+          const int64_t r = row + int64_t(u) * RG;
+          ok[u] = r < r1;
+          off[u] = size_t(ok[u] ? r : row) * C;
+          w[u] = ok[u] ? double(W[off[u] + c]) : 0.0;
+          wx[u] = (NC == 2 && ok[u]) ? double(W[off[u] + (c ^ 1)]) : 0.0;
+        }
 #pragma unroll
         for (int q = 0; q < kIC; ++q) {
           if (i0 + q < J) {
-            const double v = (i0 + q < Jv) ? double(V[size_t(i0 + q) * vstride + off + c]) : w;
-            a[q] = fma(v, w, a[q]);
-            if (NC == 2) b[q] = fma(v, wx, b[q]);
+#pragma unroll
+            for (int u = 0; u < LGT_MD_ROWS; ++u) {
+              const double v =
+                  (i0 + q < Jv) ? (ok[u] ? double(V[size_t(i0 + q) * vstride + off[u] + c]) : 0.0)
+                                : w[u];
+              a[q] = fma(v, w[u], a[q]);
+              if (NC == 2) b[q] = fma(v, wx[u], b[q]);
+            }
           }
         }
       }
@@ -181,9 +201,23 @@ __global__ void __launch_bounds__(kT) k_update(const S* __restrict__ V, size_t v
   if (act) {
     for (int64_t row = r0 + rg; row < r1; row += RG) {
       const size_t off = size_t(row) * C;
-      // two independent chains (even / odd basis vectors)
       double w0 = double(W[off + c]), w1 = 0.0;
       int i = 0;
+      if (NC == 1) {
+        // LGT_UPD_CHAINS independent chains over consecutive basis vectors
+        double wc[LGT_UPD_CHAINS];
+#pragma unroll
+        for (int u = 0; u < LGT_UPD_CHAINS; ++u) wc[u] = 0.0;
+        for (; i + LGT_UPD_CHAINS <= Ju; i += LGT_UPD_CHAINS) {
+#pragma unroll
+          for (int u = 0; u < LGT_UPD_CHAINS; ++u)
+            wc[u] = fma(-h[(size_t(i + u) * K + k) * 2 + 0],
+                        double(V[size_t(i + u) * vstride + off + c]), wc[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < LGT_UPD_CHAINS; ++u) w1 += wc[u];
+      }
+      // two independent chains (even / odd basis vectors)
       for (; i + 1 < Ju; i += 2) {
         const double hr0 = h[(size_t(i) * K + k) * 2 + 0];
         const double hr1 = h[(size_t(i + 1) * K + k) * 2 + 0];
@@ -627,14 +661,17 @@ int grid_for(int64_t n) {
 }
 
 // Row partition of the two-stage reductions: enough rows per block to keep
-// its threads busy, at most two blocks per SM.
+// its threads busy, at most LGT_RED_BLOCKS blocks.
+#ifndef LGT_RED_BLOCKS
+#define LGT_RED_BLOCKS 608  // 4 blocks per SM: the reductions are latency-bound
+#endif
 struct Reducer {
   int nblk = 1;
   int64_t rpb = 1;
   void plan(int64_t N, int C) {
     const int RG = kT / C;
     int64_t want = (N * C + 4095) / 4096;
-    if (want > 304) want = 304;
+    if (want > LGT_RED_BLOCKS) want = LGT_RED_BLOCKS;
     if (want < 1) want = 1;
     rpb = (N + want - 1) / want;
     if (rpb < RG) rpb = RG;
