@@ -37,6 +37,9 @@ import numpy as np  # noqa: E402
 NX, NY, DG, KPTS = 4, 2, 1, 64
 G_LO, G_HI, T_HOP, MASS = 0.5, 2.0, 1.0, 0.5
 RF_NX, RF_NY, RF_K = 4, 4, 8          # roofline panel (4x4 quench, K = 8 complex)
+# DRAM bytes of one such launch (FP32, reference model), measured by ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum, --set full, one launch)
+RF_TRAFFIC_BYTES = int((2.904194 + 0.533047) * 1e9)
 L2_FLUSH_BYTES = 512 << 20            # > 129 MB L2
 
 
@@ -348,6 +351,110 @@ def quench(L, C, lib, torch, stream, dev, n_steps=5):
     return out
 
 
+def _oracle_point(args):
+    """FP64 oracle ground state of one (lattice, g, m, model) point: E0 and,
+    when asked, <E^2> and <n_stag> (pool worker)."""
+    nx, ny, g, m, model, want_obs = args
+    from oracle import oracle as O
+    b = O.build_basis(nx, ny, 1, O.staggered_charges(nx, ny))
+    E0, psi = O.ground_state(O.build_hamiltonian(b, g=g, t=1.0, m=m, model=model))
+    if not want_obs:
+        return (E0,)
+    mo = O.measure(psi, b)
+    return E0, mo["E2_mean"], mo["n_stag"]
+
+
+C4_LATTICES = [(3, 2), (4, 2), (3, 3), (4, 3)]
+
+
+def c4_points():
+    """16 (g, m) points per lattice: g log-uniform on [0.3, 3], m uniform on
+    [0, 1], seed 0, drawn lattice by lattice (g then m)."""
+    rng = np.random.default_rng(0)
+    out = []
+    for _ in C4_LATTICES:
+        g = np.exp(rng.uniform(np.log(0.3), np.log(3.0), 16))
+        m = rng.uniform(0.0, 1.0, 16)
+        out.append((g, m))
+    return out
+
+
+def extra_configs(L, pool, dev, reps=3):
+    """The other configurations as parity cases with their own timings:
+    3x2 plain FP64 at tol 1e-12; 4x3 (g = 0.8, m = 0.3) FP32-mixed against
+    FP64, errors of E0, <E^2>, <n_stag> against the FP64 oracle, both model
+    flags; the uneven batch 3x2 + 4x2 + 3x3 + 4x3 x 16 points in one call."""
+    jobs = [(3, 2, 1.0, 0.5, "ref", False)]
+    jobs += [(4, 3, 0.8, 0.3, model, True) for model in ("ref", "pjw")]
+    pts = c4_points()
+    for (nx, ny), (g, m) in zip(C4_LATTICES, pts):
+        jobs += [(nx, ny, float(g[i]), float(m[i]), "ref", False) for i in range(16)]
+    pending = pool.map_async(_oracle_point, jobs)
+    out = {}
+    # C1: 3x2, FP64, tol 1e-12, start normal(seed 0)
+    b, kd = L.build_basis(3, 2, 1, L.staggered_charges(3, 2), device=dev)
+    H = L.build_hamiltonian(b, kd, 3, 2, 1, g=1.0, t=1.0, m=0.5)
+    ts = []
+    for it in range(2 + reps):
+        t0 = time.perf_counter()
+        E1, _ = L.find_ground_state(H, tol=1e-12, seed=0)
+        if it >= 2:
+            ts.append(time.perf_counter() - t0)
+    H.close()
+    b.close()
+    # C3: 4x3, g = 0.8, m = 0.3, FP32-mixed vs FP64, both models
+    b, kd = L.build_basis(4, 3, 1, L.staggered_charges(4, 3), device=dev)
+    c3 = {}
+    for model in ("ref", "pjw"):
+        H = L.build_hamiltonian(b, kd, 4, 3, 1, g=0.8, t=1.0, m=0.3, model=model)
+        for prec in ("fp64", "fp32_mixed"):
+            t0 = time.perf_counter()
+            E, psi = L.find_ground_state(H, precision=prec, as_complex=False)
+            o = L.measure_ED(psi, b, 4, 3, 1, 0.0)
+            c3["%s_%s" % (model, prec)] = {"E0": E, "E2_mean": o["E2_mean"],
+                                           "n_stag": o["n_stag"],
+                                           "s_incl_host_copies": time.perf_counter() - t0}
+        H.close()
+    b.close()
+    # C4: uneven batch, FP32-mixed, one call
+    bases, Hs = [], []
+    for (nx, ny), (g, m) in zip(C4_LATTICES, pts):
+        bb, kk = L.build_basis(nx, ny, 1, L.staggered_charges(nx, ny), device=dev)
+        bases.append(bb)
+        Hs.append(L.build_hamiltonian(bb, kk, nx, ny, 1, g=g, t=1.0, m=m))
+    ts4 = []
+    for it in range(1 + reps):
+        t0 = time.perf_counter()
+        res4 = L.find_ground_states(Hs, precision="fp32_mixed")
+        if it >= 1:
+            ts4.append(time.perf_counter() - t0)
+    for H in Hs:
+        H.close()
+    for bb in bases:
+        bb.close()
+    ref = pending.get()
+    out["c1_3x2_fp64_tol1e-12"] = {"N": 90, "E0": E1, "rel_dE": abs(E1 - ref[0][0]) / abs(ref[0][0]),
+                                   "ms_per_solve_incl_host_copies": 1e3 * min(ts)}
+    c3e = {}
+    for q, model in enumerate(("ref", "pjw")):
+        E0o, E2o, nso = ref[1 + q]
+        for prec in ("fp64", "fp32_mixed"):
+            r = c3["%s_%s" % (model, prec)]
+            c3e["%s_%s" % (model, prec)] = {
+                "rel_dE0": abs(r["E0"] - E0o) / abs(E0o), "abs_dE2": abs(r["E2_mean"] - E2o),
+                "abs_dn_stag": abs(r["n_stag"] - nso),
+                "s_incl_host_copies": r["s_incl_host_copies"]}
+    out["c3_4x3_mixed_vs_fp64"] = {"N": 72211, "g": 0.8, "m": 0.3, "errors_vs_fp64_oracle": c3e}
+    e4 = np.array([r[0] for r in ref[3:]])
+    got = np.concatenate([E for E, _ in res4])
+    out["c4_uneven_batch"] = {
+        "lattices": ["%dx%d" % l for l in C4_LATTICES], "points_per_lattice": 16,
+        "rows_total": int(sum(16 * bb for bb in (90, 645, 2443, 72211))),
+        "gs_per_s_incl_host_copies": 64 / statistics.mean(ts4),
+        "max_rel_dE_fp32_mixed": float(np.max(np.abs(got - e4) / np.abs(e4)))}
+    return out
+
+
 def ctypes_ptr(v):
     import ctypes
     return ctypes.c_void_p(v)
@@ -500,11 +607,13 @@ def main():
     if rank != 0:
         return
     cpu_s, E_cpu = cpu_step(pool, points(0))
-    pool.close()
     cpu_val = KPTS / cpu_s
 
+    import lgt_gb300 as L
+    extra = extra_configs(L, pool, int(os.environ.get("LOCAL_RANK", "0")))
+    pool.close()
     rf = r["rf"]
-    dom = rf["ref_fp64"]
+    dom = rf["ref_fp32"]
     e2e_val = KPTS / statistics.mean(r["e2e_times"])
     line = {
         "metric": "ground states/s, batched FP32-mixed Lanczos at |dE|/|E|<=1e-10",
@@ -527,13 +636,18 @@ def main():
             "pjw_fp32_mixed_batched_gs_per_s": KPTS / statistics.mean(r["t_pjw"]),
             "matvecs_per_solve_mixed": r["matvecs_mix"], "restarts_mixed": r["restarts_mix"],
         },
-        "roofline": {"kernel": "k_hpsi (H*psi), 4x4 N=8563545, K=8 complex FP64, reference model",
+        "roofline": {"kernel": "k_hpsi_fixed (H*psi), 4x4 N=8563545, K=8 complex FP32 (the "
+                               "FP32-mixed quench panel), reference model",
                      "bound": "hbm", "achieved": dom["gbs"], "peak": rf["peak"], "unit": "GB/s",
-                     "frac": dom["frac"], "traffic": None,
+                     "frac": dom["frac"], "traffic": RF_TRAFFIC_BYTES,
+                     "traffic_note": "ncu DRAM bytes per launch; 3.0x the algorithmic bytes: "
+                                     "neighbour gathers re-read x from HBM (LRU model of a "
+                                     "100 MB L2: 4.4 misses per row)",
                      "peak_source": rf["peak_src"] + " (MEASURED_PEAKS.json hbm_gbs)",
                      "algo_bytes_per_launch": dom["algo_bytes"], "ms_per_launch": dom["ms"],
                      "variants": {k: v for k, v in rf.items() if isinstance(v, dict)}},
         "quench_4x4": r["quench"],
+        "configs": extra,
         "cpu_baseline": {"value": cpu_val, "unit": "GS/s", "cores": ncores, "kind": "port",
                          "sample": "one step: all 64 points, one point per host process; oracle "
                                    "port of finite_ed.jl (C basis + H, scipy eigsh tol 1e-10 ncv 50)"},
