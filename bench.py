@@ -322,6 +322,8 @@ def quench(L, C, lib, torch, stream, dev, n_steps=5):
         torch.cuda.synchronize()  # the library runs on `stream`
         e_before = np.zeros(RF_K)
         C.check(lib.lgt_energy(H.handle, psi.data_ptr(), 2, C.LGT_DEVICE_PTRS, e_before.ctypes.data))
+        tune = C.Tuning()  # the autotuner's one-time timing runs here, not in the timed step
+        C.check(lib.lgt_autotune(H.handle, 2, code, ctypes_byref(tune)))
         o = C.defaults(True)
         o.precision = code
         obs = (C.Obs * ((n_steps + 1) * RF_K))()
@@ -344,7 +346,11 @@ def quench(L, C, lib, torch, stream, dev, n_steps=5):
                      "max_norm_drift": float(drift.max()),
                      "max_rel_energy_drift": float(np.max(np.abs(e_after - e_before) /
                                                          np.abs(e_before))),
-                     "E2_mean_t_end_point0": obs[n_steps * RF_K].E2_mean}
+                     "E2_mean_t_end_point0": obs[n_steps * RF_K].E2_mean,
+                     "autotune": {"hpsi_kernel": ["rule", "generic", "fixed_vpl1",
+                                                  "fixed_vpl2"][tune.hpsi_kernel],
+                                  "reduce_blocks": tune.reduce_blocks,
+                                  "measured": bool(tune.measured)}}
         del psi
     H.close()
     b.close()
@@ -458,6 +464,11 @@ def extra_configs(L, pool, dev, reps=3):
 def ctypes_ptr(v):
     import ctypes
     return ctypes.c_void_p(v)
+
+
+def ctypes_byref(v):
+    import ctypes
+    return ctypes.byref(v)
 
 
 def roofline(L, C, lib, torch, stream, dev, reps=10):

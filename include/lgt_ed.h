@@ -265,6 +265,28 @@ LGT_API lgt_status lgt_observe_noalloc(const lgt_ham* h, const void* psi, int32_
 LGT_API lgt_status lgt_energy(const lgt_ham* h, const void* psi, int32_t ncomp, uint32_t flags,
                       double* energy);
 
+/* Autotuner report (no counterpart in the reference).  The Krylov drivers
+   time their kernel candidates at the first solve of each operator shape
+   (lattice, model, storage precision, panel width) and keep the fastest for
+   the process: the H*psi kernel (run-time geometry, or the fixed-shape
+   kernel with one or two vector loads per lane) and the block count of the
+   Gram-Schmidt reductions.  LGT_AUTOTUNE=0 in the environment keeps the
+   built-in rules. */
+typedef struct lgt_tuning {
+  int32_t hpsi_kernel;    /* 0 built-in rule, 1 run-time geometry,
+                             2 fixed shape 1 vector/lane, 3 fixed shape 2    */
+  int32_t reduce_blocks;  /* block-count cap of the panel reductions         */
+  double hpsi_ms;         /* one H*psi with the chosen kernel                */
+  double reduce_ms;       /* one 8-vector Gram-Schmidt pass, chosen blocks   */
+  int32_t measured;       /* 1 timed on this device, 0 built-in rules        */
+} lgt_tuning;
+
+/* Runs (or looks up) the autotuner for h's Krylov panels: ncomp 1 is the
+   ground-state shape (K real columns), 2 the exponential's (2K real
+   columns); precision LGT_FP64, or LGT_FP32 / LGT_FP32_MIXED (FP32
+   storage).  Tuning allocates a temporary workspace and synchronises. */
+LGT_API lgt_status lgt_autotune(lgt_ham* h, int32_t ncomp, int32_t precision, lgt_tuning* out);
+
 LGT_API void lgt_ham_destroy(lgt_ham* h);
 
 #ifdef __cplusplus

@@ -46,9 +46,19 @@ EXPORTS = (
     "lgt_basis_lookup", "lgt_basis_rank", "lgt_basis_destroy", "lgt_basis_set_stream",
     "lgt_launch_count",
     "lgt_ham_create", "lgt_ham_set_couplings", "lgt_ham_nnz", "lgt_ham_export_csr",
-    "lgt_matvec", "lgt_ground_state", "lgt_ground_state_batch", "lgt_expm_steps", "lgt_observe", "lgt_observe_noalloc", "lgt_energy",
-    "lgt_ham_destroy",
+    "lgt_matvec", "lgt_ground_state", "lgt_ground_state_batch", "lgt_expm_steps", "lgt_observe",
+    "lgt_observe_noalloc", "lgt_energy", "lgt_autotune", "lgt_ham_destroy",
 )
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [
+        ("hpsi_kernel", ctypes.c_int32),
+        ("reduce_blocks", ctypes.c_int32),
+        ("hpsi_ms", ctypes.c_double),
+        ("reduce_ms", ctypes.c_double),
+        ("measured", ctypes.c_int32),
+    ]
 
 
 class KrylovOpts(ctypes.Structure):
@@ -151,6 +161,7 @@ def load(build_if_missing: bool = True):
         "lgt_observe": (i32, [vp, vp, i32, i32, u32, dbl, vp, vp, vp, vp]),
         "lgt_observe_noalloc": (i32, [vp, vp, i32, i32, dbl, vp, vp, vp, vp]),
         "lgt_energy": (i32, [vp, vp, i32, u32, vp]),
+        "lgt_autotune": (i32, [vp, i32, i32, ctypes.POINTER(Tuning)]),
         "lgt_ham_destroy": (None, [vp]),
     }
     for name in EXPORTS:

@@ -853,6 +853,25 @@ lgt_status lgt_energy(const lgt_ham* hc, const void* psi, int32_t ncomp, uint32_
   return check_device_errors(h->b);
 }
 
+lgt_status lgt_autotune(lgt_ham* h, int32_t ncomp, int32_t precision, lgt_tuning* out) {
+  if (!h || !out) return fail(LGT_ERR_ARG, "null argument");
+  if (ncomp != 1 && ncomp != 2) return fail(LGT_ERR_ARG, "ncomp must be 1 or 2");
+  if (precision != LGT_FP64 && precision != LGT_FP32 && precision != LGT_FP32_MIXED)
+    return fail(LGT_ERR_ARG, "unknown precision");
+  lgt_status st = set_device(h->b);
+  if (st) return st;
+  TuneChoice c;
+  std::string m = krylov_autotune(h->op(), h->cache, ncomp, precision != LGT_FP64 ? 1 : 0,
+                                  h->b->B.stream, &c);
+  if (!m.empty()) return from_msg(m);
+  out->hpsi_kernel = c.hpsi_variant;
+  out->reduce_blocks = c.red_blocks;
+  out->hpsi_ms = c.hpsi_ms;
+  out->reduce_ms = c.red_ms;
+  out->measured = c.measured;
+  return check_device_errors(h->b);
+}
+
 void lgt_ham_destroy(lgt_ham* h) {
   if (!h) return;
   if (h->b) {

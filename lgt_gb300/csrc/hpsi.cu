@@ -255,15 +255,28 @@ cudaError_t launch_hpsi_generic(HpsiArgs<T> a, uint32_t model, cudaStream_t s) {
 }
 
 template <typename T>
+bool hpsi_fixed_applies(const HpsiArgs<T>& a, int* max_vpl) {
+  const Geom& G = a.G;
+  const bool shape = (G.nx == 4 && G.ny == 4) || (G.nx == 4 && G.ny == 3) ||
+                     (G.nx == 3 && G.ny == 4);
+  const bool ok = shape && G.dg == 1 && a.R.tab && a.N < (int64_t(1) << 31) && vec_ok(a);
+  if (max_vpl) *max_vpl = ok ? ((a.C % (2 * (16 / int(sizeof(T)))) == 0) ? 2 : 1) : 0;
+  return ok;
+}
+
+template <typename T>
 cudaError_t launch_hpsi(HpsiArgs<T> a, uint32_t model, cudaStream_t s) {
   const Geom& G = a.G;
-  if (!a.force_generic && G.dg == 1 && a.R.tab && a.N < (int64_t(1) << 31) && vec_ok(a)) {
+  if (!a.force_generic && hpsi_fixed_applies(a, nullptr)) {
     if (G.nx == 4 && G.ny == 4) return launch_hpsi_4x4(a, model, s);
     if (G.nx == 4 && G.ny == 3) return launch_hpsi_4x3(a, model, s);
     if (G.nx == 3 && G.ny == 4) return launch_hpsi_3x4(a, model, s);
   }
   return launch_hpsi_generic(a, model, s);
 }
+
+template bool hpsi_fixed_applies<double>(const HpsiArgs<double>&, int*);
+template bool hpsi_fixed_applies<float>(const HpsiArgs<float>&, int*);
 
 template cudaError_t launch_hpsi<double>(HpsiArgs<double>, uint32_t, cudaStream_t);
 template cudaError_t launch_hpsi<float>(HpsiArgs<float>, uint32_t, cudaStream_t);

@@ -18,8 +18,12 @@
 // eigendecomposition by implicit QL (exponential).
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "lgt_krylov.h"
@@ -665,13 +669,14 @@ int grid_for(int64_t n) {
 #ifndef LGT_RED_BLOCKS
 #define LGT_RED_BLOCKS 608  // 4 blocks per SM: the reductions are latency-bound
 #endif
+constexpr int kRedMaxBlocks = 1216;  // 8 per SM: the largest candidate of the tuner
 struct Reducer {
   int nblk = 1;
   int64_t rpb = 1;
-  void plan(int64_t N, int C) {
+  void plan(int64_t N, int C, int cap = LGT_RED_BLOCKS) {
     const int RG = kT / C;
     int64_t want = (N * C + 4095) / 4096;
-    if (want > LGT_RED_BLOCKS) want = LGT_RED_BLOCKS;
+    if (want > cap) want = cap;
     if (want < 1) want = 1;
     rpb = (N + want - 1) / want;
     if (rpb < RG) rpb = RG;
@@ -734,14 +739,16 @@ struct Work {
     lite = lite_;
     ldT = m + 1;
     vstride = size_t(N) * C;
+    red.plan(N, C, kRedMaxBlocks);  // partial-sum buffers for the largest block count
+    const int nblk_max = red.nblk;
     red.plan(N, C);
     if (!lite) {
       KCK(cudaMalloc(&V, sizeof(S) * vstride * (m + 1)));
       KCK(cudaMalloc(&W, sizeof(S) * vstride));
       KCK(cudaMalloc(&R, sizeof(double) * vstride));
     }
-    KCK(cudaMalloc(&part, sizeof(double) * size_t(red.nblk) * ldT * 2 * C));
-    KCK(cudaMalloc(&npart, sizeof(double) * size_t(red.nblk) * C));
+    KCK(cudaMalloc(&part, sizeof(double) * size_t(nblk_max) * ldT * 2 * C));
+    KCK(cudaMalloc(&npart, sizeof(double) * size_t(nblk_max) * C));
     KCK(cudaMalloc(&h, sizeof(double) * size_t(ldT) * K * 2));
     KCK(cudaMalloc(&alpha, sizeof(double) * size_t(K) * ldT));
     KCK(cudaMalloc(&beta, sizeof(double) * size_t(K) * ldT));
@@ -759,6 +766,13 @@ struct Work {
     KCK(cudaMalloc(&jstate, sizeof(int) * 4));
     KCK(cudaMalloc(&fail, sizeof(int)));
     return std::string();
+  }
+  // Re-partition the reductions (the captured graph holds the old one).
+  void replan(int cap) {
+    red.plan(N, C, cap);
+    if (graph) cudaGraphExecDestroy(graph);
+    graph = nullptr;
+    graph_steps = 0;
   }
   void release() {
     if (graph) cudaGraphExecDestroy(graph);
@@ -816,6 +830,7 @@ cudaError_t apply_h<double>(const OpDev& op, const double* x, const int* xsel, s
   a.xsel = xsel;
   a.xstride = xstride;
   a.force_generic = op.force_generic;
+  a.vpl = op.vpl;
   return launch_hpsi<double>(a, op.model, s);
 }
 
@@ -840,6 +855,7 @@ cudaError_t apply_h<float>(const OpDev& op, const float* x, const int* xsel, siz
   a.xsel = xsel;
   a.xstride = xstride;
   a.force_generic = op.force_generic;
+  a.vpl = op.vpl;
   return launch_hpsi<float>(a, op.model, s);
 }
 
@@ -937,6 +953,146 @@ std::string dots_ws(Work<S>& w, const double* x, const double* y, double* out_ho
   return std::string();
 }
 
+// ---- autotuner ---------------------------------------------------------------
+//
+// Per operator shape (lattice, model, storage precision, panel width) the
+// first solve times the candidates on its own workspace and keeps the
+// fastest for the process:
+//   * the H*psi kernel: run-time geometry, or (where one exists) the
+//     fixed-shape kernel with one or two vector loads per lane;
+//   * the block count of the panel reductions (Gram-Schmidt dots and
+//     updates): 2, 4, 6 or 8 blocks per SM.
+// LGT_AUTOTUNE=0 in the environment keeps the built-in rules.
+struct TuneKey {
+  int nx, ny, dg, model, bytes, C, hcomp;
+  int64_t N;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(nx, ny, dg, model, bytes, C, hcomp, N) <
+           std::tie(o.nx, o.ny, o.dg, o.model, o.bytes, o.C, o.hcomp, o.N);
+  }
+};
+
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneChoice> g_tune;
+
+bool autotune_enabled() {
+  const char* e = getenv("LGT_AUTOTUNE");
+  return !(e && e[0] == '0');
+}
+
+void apply_variant(OpDev* op, int v) {
+  op->force_generic = (v == kHpsiGeneric) ? 1 : 0;
+  op->vpl = (v == kHpsiFixed1) ? 1 : ((v == kHpsiFixed2) ? 2 : 0);
+}
+
+template <typename S>
+std::string autotune(OpDev* op, Work<S>& w, cudaStream_t s, TuneChoice* out) {
+  const TuneKey key{op->G.nx, op->G.ny, op->G.dg, int(op->model), int(sizeof(S)),
+                    w.C, w.hcomp, w.N};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      apply_variant(op, it->second.hpsi_variant);
+      if (w.red.nblk != it->second.red_nblk) w.replan(it->second.red_blocks);
+      if (out) *out = it->second;
+      return std::string();
+    }
+  }
+  TuneChoice c;
+  c.hpsi_variant = kHpsiDefault;
+  c.red_blocks = LGT_RED_BLOCKS;
+  if (autotune_enabled() && !w.lite && w.V) {
+    const int J = (w.m + 1 < 8) ? w.m + 1 : 8;
+    KCK(cudaMemsetAsync(w.V, 0, sizeof(S) * w.vstride * J, s));
+    KCK(cudaMemsetAsync(w.W, 0, sizeof(S) * w.vstride, s));
+    cudaEvent_t e0, e1;
+    KCK(cudaEventCreate(&e0));
+    KCK(cudaEventCreate(&e1));
+    std::string err;
+    auto timed = [&](auto&& launch) -> double {  // one warm-up, mean of three
+      cudaError_t e = launch();
+      if (e == cudaSuccess) e = cudaEventRecord(e0, s);
+      for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = launch();
+      if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      float ms = 0.f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (e != cudaSuccess) {
+        err = std::string("autotune: ") + cudaGetErrorString(e);
+        return 1e30;
+      }
+      return double(ms) / 3.0;
+    };
+    // H*psi variants
+    HpsiArgs<S> probe;
+    probe.G = op->G;
+    probe.R = op->R;
+    probe.x = w.V;
+    probe.y = w.W;
+    probe.N = w.N;
+    probe.C = w.C;
+    probe.xsel = nullptr;
+    probe.xstride = 0;
+    int max_vpl = 0;
+    std::vector<int> cand{kHpsiGeneric};
+    if (hpsi_fixed_applies(probe, &max_vpl)) {
+      cand.push_back(kHpsiFixed1);
+      if (max_vpl >= 2) cand.push_back(kHpsiFixed2);
+    }
+    double best = 1e30;
+    for (int v : cand) {
+      OpDev o = *op;
+      apply_variant(&o, v);
+      const double t =
+          timed([&] { return apply_h<S>(o, w.V, nullptr, 0, w.W, w.hcomp, s); });
+      if (!err.empty()) break;
+      if (t < best) {
+        best = t;
+        c.hpsi_variant = v;
+      }
+    }
+    c.hpsi_ms = best;
+    // reduction block counts: one Gram-Schmidt pass (dots and update)
+    // against J vectors (step index J - 1, all points active, h = 0)
+    const int jm1 = J - 1;
+    KCK(cudaMemcpyAsync(w.jstate, &jm1, sizeof(int), cudaMemcpyHostToDevice, s));
+    KCK(cudaMemsetAsync(w.status, 0, sizeof(int) * w.K, s));
+    KCK(cudaMemsetAsync(w.h, 0, sizeof(double) * size_t(w.ldT) * w.K * 2, s));
+    best = 1e30;
+    int last_nblk = -1;
+    for (int cap : {304, 608, 912, kRedMaxBlocks}) {
+      if (!err.empty()) break;
+      w.red.plan(w.N, w.C, cap);
+      if (w.red.nblk == last_nblk) continue;
+      last_nblk = w.red.nblk;
+      const double t = timed([&] {
+        cudaError_t e = launch_multidot<S, S>(w, w.V, w.vstride, w.jstate, 0, w.W, s);
+        if (e == cudaSuccess) e = launch_update<S>(w, w.W, s);
+        return e;
+      });
+      if (t < best) {
+        best = t;
+        c.red_blocks = cap;
+      }
+    }
+    c.red_ms = best;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (!err.empty()) return err;
+    c.measured = 1;
+  }
+  w.replan(c.red_blocks);
+  c.red_nblk = w.red.nblk;
+  apply_variant(op, c.hpsi_variant);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[key] = c;
+  }
+  if (out) *out = c;
+  return std::string();
+}
+
 template <typename S>
 std::string capture_steps(const OpDev& op, Work<S>& w, int steps, int reorth, double tiny_rel,
                           cudaStream_t s) {
@@ -1011,8 +1167,9 @@ std::string reset_cycle(Work<S>& w, cudaStream_t s) {
 }
 
 template <typename S>
-std::string ground_state_impl(const OpDev& op, const KrylovParams& p, Work<S>& w, double* X,
+std::string ground_state_impl(const OpDev& op_in, const KrylovParams& p, Work<S>& w, double* X,
                               double* E0, double* resid_out, cudaStream_t s, KrylovReport* rep) {
+  OpDev op = op_in;  // carries the autotuner's H*psi variant
   const int64_t N = op.R.dim;
   const int K = op.K;
   const int ncomp = 1, C = K;
@@ -1025,6 +1182,8 @@ std::string ground_state_impl(const OpDev& op, const KrylovParams& p, Work<S>& w
     w.release();
     return err;
   }
+  err = autotune<S>(&op, w, s, nullptr);
+  if (!err.empty()) return err;
   const bool fp32 = sizeof(S) == 4;
   const double tiny_rel = fp32 ? 1e-6 : 1e-12;
   // FP32 panels cannot resolve residuals much below 1e-6 |H|: the inner
@@ -1146,9 +1305,10 @@ std::string ground_state_impl(const OpDev& op, const KrylovParams& p, Work<S>& w
 // complex coefficients.  Each column's error estimate must meet tol / sqrt 2,
 // so the point's combined error meets tol.
 template <typename S>
-std::string expm_impl(const OpDev& op, const KrylovParams& p, Work<S>& w, double dt, int n_steps,
-                      double* X, double* drift, StepObserver* obs, cudaStream_t s,
+std::string expm_impl(const OpDev& op_in, const KrylovParams& p, Work<S>& w, double dt,
+                      int n_steps, double* X, double* drift, StepObserver* obs, cudaStream_t s,
                       KrylovReport* rep) {
+  OpDev op = op_in;  // carries the autotuner's H*psi variant
   const int64_t N = op.R.dim;
   const int K = op.K;       // coupling points (complex columns of X)
   const int C = 2 * K;      // real Krylov columns
@@ -1162,6 +1322,8 @@ std::string expm_impl(const OpDev& op, const KrylovParams& p, Work<S>& w, double
     w.release();
     return err;
   }
+  err = autotune<S>(&op, w, s, nullptr);
+  if (!err.empty()) return err;
   const double tiny_rel = (sizeof(S) == 8) ? 1e-12 : 1e-6;
   const double tol = p.tol / sqrt(2.0);
   std::vector<int> st(Kc);
@@ -1293,14 +1455,38 @@ struct KrylovCache {
   Work<double> ex_d;
   Work<float> ex_f;
   Work<double> dots;  // reduction buffers of panel_dots only
+  Work<double> tune_d;  // explicit autotuning (lgt_autotune), released after use
+  Work<float> tune_f;
   ~KrylovCache() {
     gs_d.release();
     gs_f.release();
     ex_d.release();
     ex_f.release();
     dots.release();
+    tune_d.release();
+    tune_f.release();
   }
 };
+
+std::string krylov_autotune(const OpDev& op_in, KrylovCache* cache, int ncomp, int mixed,
+                            cudaStream_t s, TuneChoice* out) {
+  OpDev op = op_in;
+  const int64_t N = op.R.dim;
+  const int C = (ncomp == 2) ? 2 * op.K : op.K;
+  if (C > kT) return "at most 256 real columns per panel";
+  const int m = int(N < 8 ? N : 8);
+  std::string err;
+  if (mixed) {
+    err = cache->tune_f.ensure(N, C, C, 1, m, ncomp == 2 ? 2 : 1);
+    if (err.empty()) err = autotune<float>(&op, cache->tune_f, s, out);
+    cache->tune_f.release();
+  } else {
+    err = cache->tune_d.ensure(N, C, C, 1, m, ncomp == 2 ? 2 : 1);
+    if (err.empty()) err = autotune<double>(&op, cache->tune_d, s, out);
+    cache->tune_d.release();
+  }
+  return err;
+}
 
 KrylovCache* krylov_cache_new() { return new KrylovCache(); }
 void krylov_cache_free(KrylovCache* c) { delete c; }

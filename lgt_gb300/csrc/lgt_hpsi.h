@@ -26,7 +26,13 @@ struct HpsiArgs {
   const int* xsel;
   size_t xstride;
   int force_generic = 0;  // 1: run-time-geometry kernel even for a fixed shape
+  int vpl = 0;            // fixed-shape kernels: vector loads per lane (0: by C)
 };
+
+// Whether a fixed-shape kernel serves these arguments, and the vector loads
+// per lane it may use (1, or 2 when C is a multiple of two vectors).
+template <typename T>
+bool hpsi_fixed_applies(const HpsiArgs<T>& a, int* max_vpl);
 
 // Default staging decision for the top-level rank table.
 int hpsi_seg_smem_default(int nmasks);

@@ -403,7 +403,7 @@ cudaError_t launch_shape_v(const HpsiArgs<T>& a, cudaStream_t s) {
 template <int NX, int NY, typename T, bool PLAQ, bool JW>
 cudaError_t launch_shape_m(const HpsiArgs<T>& a, cudaStream_t s) {
   constexpr int V = 16 / int(sizeof(T));
-  if (a.C % (2 * V) == 0) return launch_shape_v<NX, NY, T, 2, PLAQ, JW>(a, s);
+  if (a.vpl != 1 && a.C % (2 * V) == 0) return launch_shape_v<NX, NY, T, 2, PLAQ, JW>(a, s);
   return launch_shape_v<NX, NY, T, 1, PLAQ, JW>(a, s);
 }
 

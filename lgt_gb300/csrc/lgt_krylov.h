@@ -20,6 +20,7 @@ struct OpDev {
   const double *cE_d, *cm_d, *ch_d, *cp_d;
   const float *cE_f, *cm_f, *ch_f, *cp_f;
   int force_generic = 0;  // H*psi through the run-time-geometry kernel only
+  int vpl = 0;            // fixed-shape H*psi: vector loads per lane (0: by width)
 };
 
 struct KrylovParams {
@@ -34,6 +35,25 @@ struct KrylovParams {
   int use_graph;
   int start_given;
 };
+
+struct KrylovCache;
+
+// Autotuner choice for one operator shape (see krylov.cu).
+enum HpsiVariant : int { kHpsiDefault = 0, kHpsiGeneric = 1, kHpsiFixed1 = 2, kHpsiFixed2 = 3 };
+struct TuneChoice {
+  int hpsi_variant = kHpsiDefault;
+  int red_blocks = 0;
+  int red_nblk = 0;
+  double hpsi_ms = 0.0;  // one H*psi of the chosen variant
+  double red_ms = 0.0;   // one 8-vector Gram-Schmidt pass (dots + update), chosen blocks
+  int measured = 0;      // 0: built-in rules (tuning disabled)
+};
+
+// Runs (or looks up) the autotuner for the Krylov panels of this operator:
+// ncomp = 1 the ground-state shape, 2 the exponential's (two real columns
+// per point); mixed = FP32 storage.
+std::string krylov_autotune(const OpDev& op, KrylovCache* cache, int ncomp, int mixed,
+                            cudaStream_t s, TuneChoice* out);
 
 struct KrylovReport {
   int64_t matvecs = 0;

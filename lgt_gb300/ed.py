@@ -347,6 +347,16 @@ class Hamiltonian:
         C.check(C.load().lgt_matvec(self._h, ctypes.c_void_p(x_ptr), ctypes.c_void_p(y_ptr),
                                     ncomp, _PREC[precision], flags))
 
+    def autotune(self, ncomp: int = 1, precision="fp64") -> dict:
+        """Autotuner choice for this operator's Krylov panels (ncomp 1:
+        ground states, 2: exponential steps); tunes on first use."""
+        t = C.Tuning()
+        C.check(C.load().lgt_autotune(self._h, int(ncomp), _PREC[precision], ctypes.byref(t)))
+        names = {0: "rule", 1: "generic", 2: "fixed_vpl1", 3: "fixed_vpl2"}
+        return {"hpsi_kernel": names.get(t.hpsi_kernel, str(t.hpsi_kernel)),
+                "reduce_blocks": t.reduce_blocks, "hpsi_ms": t.hpsi_ms,
+                "reduce_ms": t.reduce_ms, "measured": bool(t.measured)}
+
     def energy(self, psi) -> np.ndarray:
         """<psi|H|psi> / <psi|psi> per point, FP64."""
         px, nc = self._panel(np.asarray(psi), np.float64)
