@@ -10,10 +10,13 @@ energy is checked against the FP64 oracle (|dE|/|E| <= 1e-10).
 
 Beside it: the same workload in plain (one point per solve) FP64 and in
 batched FP64; the H*psi roofline on the 4x4 lattice (N = 8,563,545, K = 8
-complex FP64 points, the real-time quench panel) whose working set exceeds
-L2; an end-to-end number through the public Python API with host buffers;
-and the oracle port (the reference's algorithm on the host cores) as CPU
-baseline.
+complex points, the real-time quench panel, FP32 as in the mixed path, FP64
+and run-time-geometry variants alongside) whose working set exceeds L2; the
+4x4 quench steps/s (FP64 and FP32-mixed); the other configurations as
+parity cases (3x2 FP64 at tol 1e-12; 4x3 mixed-vs-FP64 errors of E0, <E^2>,
+<n_stag>; the uneven 3x2/4x2/3x3/4x3 batch); an end-to-end number through
+the public Python API with host buffers; and the oracle port (the
+reference's algorithm on the host cores) as CPU baseline.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
