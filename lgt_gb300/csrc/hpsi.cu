@@ -95,11 +95,17 @@ __host__ __device__ inline int row_moves(const Geom& G, bool plaq) {
   return G.nR + G.nU + (plaq ? 2 * G.nP : 0);
 }
 
+// Shared-memory stride of a row's neighbour list: odd, so that the lists of
+// the rows a warp touches at once fall in distinct banks.
+__host__ __device__ inline int row_stride(const Geom& G, bool plaq) {
+  return row_moves(G, plaq) | 1;
+}
+
 template <typename T, int V, bool PLAQ, bool JW>
 __global__ void __launch_bounds__(kThreads) k_hpsi(HpsiArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const Geom& G = a.G;
-  const int MM = row_moves(G, PLAQ);
+  const int MM = row_stride(G, PLAQ);
   const SmemLayout L = smem_layout<T>(a.R.nmasks, a.seg_smem, a.K, MM);
   uint32_t* s_binom = reinterpret_cast<uint32_t*>(smem + L.binom_off);
   uint32_t* s_segc = reinterpret_cast<uint32_t*>(smem + L.segc_off);
@@ -210,7 +216,7 @@ __global__ void __launch_bounds__(kThreads) k_hpsi(HpsiArgs<T> a) {
 
 template <typename T, int V, bool PLAQ, bool JW>
 cudaError_t launch_t(const HpsiArgs<T>& a, cudaStream_t s) {
-  const SmemLayout L = smem_layout<T>(a.R.nmasks, a.seg_smem, a.K, row_moves(a.G, PLAQ));
+  const SmemLayout L = smem_layout<T>(a.R.nmasks, a.seg_smem, a.K, row_stride(a.G, PLAQ));
   auto kern = k_hpsi<T, V, PLAQ, JW>;
   // raise the dynamic shared-memory limit once per kernel (outside any graph
   // capture: the first launch of a configuration is always eager)

@@ -73,6 +73,13 @@ __host__ __device__ constexpr int max_moves() {
   return Shape<NX, NY>::NR + Shape<NX, NY>::NU + (PLAQ ? 2 * Shape<NX, NY>::NP : 0);
 }
 
+// Shared-memory stride of a row's neighbour list: odd, so the lists of the
+// rows a warp touches at once fall in distinct banks.
+template <int NX, int NY, bool PLAQ>
+__host__ __device__ constexpr int list_stride() {
+  return max_moves<NX, NY, PLAQ>() | 1;
+}
+
 template <typename T>
 __host__ __device__ inline int coef_bytes(int K) {
   return (4 * K * int(sizeof(T)) + 15) / 16 * 16;
@@ -80,7 +87,7 @@ __host__ __device__ inline int coef_bytes(int K) {
 
 template <int NX, int NY, bool PLAQ, typename T>
 __host__ __device__ inline int smem_bytes(int K) {
-  return coef_bytes<T>(K) + kThreads * 4 + kThreads * max_moves<NX, NY, PLAQ>() * 4;
+  return coef_bytes<T>(K) + kThreads * 4 + kThreads * list_stride<NX, NY, PLAQ>() * 4;
 }
 
 // Index of the state (nm, rows f) with row rc's index replaced by frc
@@ -143,7 +150,7 @@ __global__ void __launch_bounds__(kThreads, PLAQ ? LGT_FIXED_MINB_PLAQ : LGT_FIX
   using S = Shape<NX, NY>;
   constexpr int V = 16 / int(sizeof(T));
   constexpr int W = V * VPL;  // columns per lane
-  constexpr int MM = max_moves<NX, NY, PLAQ>();
+  constexpr int MM = list_stride<NX, NY, PLAQ>();
   extern __shared__ __align__(16) unsigned char smem[];
   const int K = a.K;
   T* s_coef = reinterpret_cast<T*>(smem);  // [4][K]: cE, cm, ch, cp
