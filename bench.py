@@ -351,7 +351,7 @@ def quench(L, C, lib, torch, stream, dev, n_steps=5):
                                                          np.abs(e_before))),
                      "E2_mean_t_end_point0": obs[n_steps * RF_K].E2_mean,
                      "autotune": {"hpsi_kernel": ["rule", "generic", "fixed_vpl1",
-                                                  "fixed_vpl2"][tune.hpsi_kernel],
+                                                  "fixed_vpl2", "fixed_wide"][tune.hpsi_kernel],
                                   "reduce_blocks": tune.reduce_blocks,
                                   "measured": bool(tune.measured)}}
         del psi
@@ -514,9 +514,14 @@ def roofline(L, C, lib, torch, stream, dev, reps=10):
                     ts.append(e0.elapsed_time(e1) * 1e-3)
             t = statistics.mean(ts)
             algo = N * 8 + 2 * RF_K * N * s   # key table + x + y, neighbour gathers 0
-            out["%s_%s%s" % (model, prec, "_generic" if generic else "")] = {
-                                            "ms": t * 1e3, "algo_bytes": algo,
-                                            "gbs": algo / t / 1e9, "frac": algo / t / 1e9 / peak}
+            row = {"ms": t * 1e3, "algo_bytes": algo, "gbs": algo / t / 1e9,
+                   "frac": algo / t / 1e9 / peak}
+            if not generic:  # the autotuner's kernel for this shape (chosen at the first call)
+                tune = C.Tuning()
+                C.check(lib.lgt_autotune(H.handle, 2, code, ctypes_byref(tune)))
+                row["kernel"] = ["rule", "generic", "fixed_vpl1", "fixed_vpl2",
+                                 "fixed_wide"][tune.hpsi_kernel]
+            out["%s_%s%s" % (model, prec, "_generic" if generic else "")] = row
             del x, y
         H.close()
     b.close()

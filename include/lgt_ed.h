@@ -269,12 +269,15 @@ LGT_API lgt_status lgt_energy(const lgt_ham* h, const void* psi, int32_t ncomp, 
    time their kernel candidates at the first solve of each operator shape
    (lattice, model, storage precision, panel width) and keep the fastest for
    the process: the H*psi kernel (run-time geometry, or the fixed-shape
-   kernel with one or two vector loads per lane) and the block count of the
+   kernel with one of its load modes; lgt_matvec uses and, on its first call
+   for a shape, makes the same choice) and the block count of the
    Gram-Schmidt reductions.  LGT_AUTOTUNE=0 in the environment keeps the
-   built-in rules. */
+   built-in rules; LGT_HPSI_VARIANT=1..4 forces one H*psi kernel (the
+   hpsi_kernel codes below) for cross-checks. */
 typedef struct lgt_tuning {
-  int32_t hpsi_kernel;    /* 0 built-in rule, 1 run-time geometry,
-                             2 fixed shape 1 vector/lane, 3 fixed shape 2    */
+  int32_t hpsi_kernel;    /* 0 built-in rule, 1 run-time geometry, fixed
+                             shape with 2 one / 3 two 16-byte vectors per
+                             lane, 4 two vectors as one 32-byte access      */
   int32_t reduce_blocks;  /* block-count cap of the panel reductions         */
   double hpsi_ms;         /* one H*psi with the chosen kernel                */
   double reduce_ms;       /* one 8-vector Gram-Schmidt pass, chosen blocks   */

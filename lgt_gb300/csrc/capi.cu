@@ -411,6 +411,13 @@ lgt_status lgt_matvec(const lgt_ham* hc, const void* x, void* y, int32_t ncomp, 
   }
   OpDev op = h->op();
   op.force_generic = (flags & LGT_GENERIC_KERNELS) ? 1 : 0;
+  if (!op.force_generic) {  // the autotuner's kernel for this shape (timed on first use)
+    std::string m =
+        (precision == LGT_FP64)
+            ? hpsi_choose_d(&op, static_cast<const double*>(dx), static_cast<double*>(dy), ncomp, s)
+            : hpsi_choose_f(&op, static_cast<const float*>(dx), static_cast<float*>(dy), ncomp, s);
+    if (!m.empty()) return from_msg(m);
+  }
   cudaError_t e = (precision == LGT_FP64)
                       ? apply_h_d(op, static_cast<const double*>(dx), static_cast<double*>(dy), ncomp, s)
                       : apply_h_f(op, static_cast<const float*>(dx), static_cast<float*>(dy), ncomp, s);

@@ -266,7 +266,11 @@ bool hpsi_fixed_applies(const HpsiArgs<T>& a, int* max_vpl) {
   const bool shape = (G.nx == 4 && G.ny == 4) || (G.nx == 4 && G.ny == 3) ||
                      (G.nx == 3 && G.ny == 4);
   const bool ok = shape && G.dg == 1 && a.R.tab && a.N < (int64_t(1) << 31) && vec_ok(a);
-  if (max_vpl) *max_vpl = ok ? ((a.C % (2 * (16 / int(sizeof(T)))) == 0) ? 2 : 1) : 0;
+  const bool two = a.C % (2 * (16 / int(sizeof(T)))) == 0;
+  const bool wide = two && (reinterpret_cast<uintptr_t>(a.x) & 31) == 0 &&
+                    (reinterpret_cast<uintptr_t>(a.y) & 31) == 0 &&
+                    (a.xsel == nullptr || (a.xstride * sizeof(T)) % 32 == 0);
+  if (max_vpl) *max_vpl = ok ? (wide ? 3 : (two ? 2 : 1)) : 0;
   return ok;
 }
 

@@ -982,7 +982,101 @@ bool autotune_enabled() {
 
 void apply_variant(OpDev* op, int v) {
   op->force_generic = (v == kHpsiGeneric) ? 1 : 0;
-  op->vpl = (v == kHpsiFixed1) ? 1 : ((v == kHpsiFixed2) ? 2 : 0);
+  op->vpl = (v == kHpsiFixed1) ? 1 : (v == kHpsiFixed2) ? 2 : (v == kHpsiFixed2w) ? 3 : 0;
+}
+
+struct HpsiKey {
+  int nx, ny, dg, model, bytes, C;
+  int64_t N;
+  bool operator<(const HpsiKey& o) const {
+    return std::tie(nx, ny, dg, model, bytes, C, N) <
+           std::tie(o.nx, o.ny, o.dg, o.model, o.bytes, o.C, o.N);
+  }
+};
+std::map<HpsiKey, std::pair<int, double>> g_hpsi_tune;  // variant, ms per launch
+
+// Times the H*psi candidates on (x, y) for this shape once per process.
+template <typename S>
+std::string tune_hpsi(OpDev* op, const S* x, S* y, int C, int hcomp, cudaStream_t s,
+                      int* variant_out, double* ms_out) {
+  // LGT_HPSI_VARIANT=1..4 forces one variant (cross-checks of every kernel)
+  if (const char* fv = getenv("LGT_HPSI_VARIANT")) {
+    const int v = atoi(fv);
+    if (v >= kHpsiGeneric && v <= kHpsiFixed2w) {
+      apply_variant(op, v);
+      if (variant_out) *variant_out = v;
+      if (ms_out) *ms_out = 0.0;
+      return std::string();
+    }
+  }
+  const HpsiKey key{op->G.nx, op->G.ny, op->G.dg, int(op->model), int(sizeof(S)), C, op->R.dim};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_hpsi_tune.find(key);
+    if (it != g_hpsi_tune.end()) {
+      apply_variant(op, it->second.first);
+      if (variant_out) *variant_out = it->second.first;
+      if (ms_out) *ms_out = it->second.second;
+      return std::string();
+    }
+  }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) cap = cudaStreamCaptureStatusActive;
+  if (!autotune_enabled() || cap != cudaStreamCaptureStatusNone) {
+    apply_variant(op, kHpsiDefault);
+    if (variant_out) *variant_out = kHpsiDefault;
+    if (ms_out) *ms_out = 0.0;
+    return std::string();  // rule (not cached: a later eager call may tune)
+  }
+  HpsiArgs<S> probe;
+  probe.G = op->G;
+  probe.R = op->R;
+  probe.x = x;
+  probe.y = y;
+  probe.N = op->R.dim;
+  probe.C = C;
+  probe.xsel = nullptr;
+  probe.xstride = 0;
+  int mode = 0;
+  std::vector<int> cand{kHpsiGeneric};
+  if (hpsi_fixed_applies(probe, &mode)) {
+    cand.push_back(kHpsiFixed1);
+    if (mode >= 2) cand.push_back(kHpsiFixed2);
+    if (mode >= 3) cand.push_back(kHpsiFixed2w);
+  }
+  cudaEvent_t e0, e1;
+  KCK(cudaEventCreate(&e0));
+  KCK(cudaEventCreate(&e1));
+  int best_v = kHpsiDefault;
+  double best = 1e30;
+  cudaError_t e = cudaSuccess;
+  for (int v : cand) {
+    OpDev o = *op;
+    apply_variant(&o, v);
+    e = apply_h<S>(o, x, nullptr, 0, y, hcomp, s);  // warm-up
+    if (e == cudaSuccess) e = cudaEventRecord(e0, s);
+    for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = apply_h<S>(o, x, nullptr, 0, y, hcomp, s);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e != cudaSuccess) break;
+    if (ms / 3.0 < best) {
+      best = ms / 3.0;
+      best_v = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (e != cudaSuccess) return std::string("autotune: ") + cudaGetErrorString(e);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_hpsi_tune[key] = {best_v, best};
+  }
+  apply_variant(op, best_v);
+  if (variant_out) *variant_out = best_v;
+  if (ms_out) *ms_out = best;
+  return std::string();
 }
 
 template <typename S>
@@ -1006,10 +1100,12 @@ std::string autotune(OpDev* op, Work<S>& w, cudaStream_t s, TuneChoice* out) {
     const int J = (w.m + 1 < 8) ? w.m + 1 : 8;
     KCK(cudaMemsetAsync(w.V, 0, sizeof(S) * w.vstride * J, s));
     KCK(cudaMemsetAsync(w.W, 0, sizeof(S) * w.vstride, s));
+    // H*psi variant (shared with lgt_matvec's choice for this shape)
+    std::string err = tune_hpsi<S>(op, w.V, w.W, w.C, w.hcomp, s, &c.hpsi_variant, &c.hpsi_ms);
+    if (!err.empty()) return err;
     cudaEvent_t e0, e1;
     KCK(cudaEventCreate(&e0));
     KCK(cudaEventCreate(&e1));
-    std::string err;
     auto timed = [&](auto&& launch) -> double {  // one warm-up, mean of three
       cudaError_t e = launch();
       if (e == cudaSuccess) e = cudaEventRecord(e0, s);
@@ -1024,42 +1120,13 @@ std::string autotune(OpDev* op, Work<S>& w, cudaStream_t s, TuneChoice* out) {
       }
       return double(ms) / 3.0;
     };
-    // H*psi variants
-    HpsiArgs<S> probe;
-    probe.G = op->G;
-    probe.R = op->R;
-    probe.x = w.V;
-    probe.y = w.W;
-    probe.N = w.N;
-    probe.C = w.C;
-    probe.xsel = nullptr;
-    probe.xstride = 0;
-    int max_vpl = 0;
-    std::vector<int> cand{kHpsiGeneric};
-    if (hpsi_fixed_applies(probe, &max_vpl)) {
-      cand.push_back(kHpsiFixed1);
-      if (max_vpl >= 2) cand.push_back(kHpsiFixed2);
-    }
-    double best = 1e30;
-    for (int v : cand) {
-      OpDev o = *op;
-      apply_variant(&o, v);
-      const double t =
-          timed([&] { return apply_h<S>(o, w.V, nullptr, 0, w.W, w.hcomp, s); });
-      if (!err.empty()) break;
-      if (t < best) {
-        best = t;
-        c.hpsi_variant = v;
-      }
-    }
-    c.hpsi_ms = best;
     // reduction block counts: one Gram-Schmidt pass (dots and update)
     // against J vectors (step index J - 1, all points active, h = 0)
     const int jm1 = J - 1;
     KCK(cudaMemcpyAsync(w.jstate, &jm1, sizeof(int), cudaMemcpyHostToDevice, s));
     KCK(cudaMemsetAsync(w.status, 0, sizeof(int) * w.K, s));
     KCK(cudaMemsetAsync(w.h, 0, sizeof(double) * size_t(w.ldT) * w.K * 2, s));
-    best = 1e30;
+    double best = 1e30;
     int last_nblk = -1;
     for (int cap : {304, 608, 912, kRedMaxBlocks}) {
       if (!err.empty()) break;
@@ -1497,6 +1564,14 @@ cudaError_t apply_h_d(const OpDev& op, const double* x, double* y, int ncomp, cu
 
 cudaError_t apply_h_f(const OpDev& op, const float* x, float* y, int ncomp, cudaStream_t s) {
   return apply_h<float>(op, x, nullptr, 0, y, ncomp, s);
+}
+
+std::string hpsi_choose_d(OpDev* op, const double* x, double* y, int ncomp, cudaStream_t s) {
+  return tune_hpsi<double>(op, x, y, op->K * ncomp, ncomp, s, nullptr, nullptr);
+}
+
+std::string hpsi_choose_f(OpDev* op, const float* x, float* y, int ncomp, cudaStream_t s) {
+  return tune_hpsi<float>(op, x, y, op->K * ncomp, ncomp, s, nullptr, nullptr);
 }
 
 std::string panel_dots(KrylovCache* cache, const double* x, const double* y, int64_t N, int K,

@@ -26,11 +26,13 @@ struct HpsiArgs {
   const int* xsel;
   size_t xstride;
   int force_generic = 0;  // 1: run-time-geometry kernel even for a fixed shape
-  int vpl = 0;            // fixed-shape kernels: vector loads per lane (0: by C)
+  int vpl = 0;            // fixed-shape load mode: 1 one vector per lane, 2 two,
+                          // 3 two as one 32-byte access; 0 the built-in rule
 };
 
-// Whether a fixed-shape kernel serves these arguments, and the vector loads
-// per lane it may use (1, or 2 when C is a multiple of two vectors).
+// Whether a fixed-shape kernel serves these arguments, and the widest load
+// mode it may use (1, 2 when C is a multiple of two vectors, 3 when the
+// panels are also 32-byte aligned).
 template <typename T>
 bool hpsi_fixed_applies(const HpsiArgs<T>& a, int* max_vpl);
 

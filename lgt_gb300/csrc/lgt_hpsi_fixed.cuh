@@ -16,8 +16,8 @@
 // Phase 1 (lane = row) writes the row's neighbour indices into shared
 // memory, hops first, then plaquette moves; bit 31 of a hop entry is its
 // Jordan-Wigner parity.  Phase 2 (lanes over (row, column slice)) gathers
-// x rows: each of a row's lanes loads VPL vectors of V elements per
-// neighbour.
+// x rows: each of a row's lanes loads one or two vectors of V elements per
+// neighbour (LD = 1, 2), or two vectors as one 32-byte access (LD = 4).
 #pragma once
 
 #include "lgt_hpsi.h"
@@ -144,12 +144,60 @@ __device__ __forceinline__ void st(T* p, const T* r) {
   __stcs(reinterpret_cast<VT*>(p), v);
 }
 
-template <int NX, int NY, typename T, int VPL, bool PLAQ, bool JW>
+// 32-byte loads and streaming stores (sm_100+ 256-bit global accesses);
+// the address must be 32-byte aligned, which the host checks.
+__device__ __forceinline__ void ld32(const float* p, float* r) {
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(r[0]), "=f"(r[1]), "=f"(r[2]), "=f"(r[3]), "=f"(r[4]), "=f"(r[5]), "=f"(r[6]),
+        "=f"(r[7])
+      : "l"(p));
+}
+__device__ __forceinline__ void ld32(const double* p, double* r) {
+  asm("ld.global.nc.v4.f64 {%0, %1, %2, %3}, [%4];"
+      : "=d"(r[0]), "=d"(r[1]), "=d"(r[2]), "=d"(r[3])
+      : "l"(p));
+}
+__device__ __forceinline__ void st32(float* p, const float* r) {
+  asm volatile("st.global.cs.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};"
+               :
+               : "l"(p), "f"(r[0]), "f"(r[1]), "f"(r[2]), "f"(r[3]), "f"(r[4]), "f"(r[5]),
+                 "f"(r[6]), "f"(r[7])
+               : "memory");
+}
+__device__ __forceinline__ void st32(double* p, const double* r) {
+  asm volatile("st.global.cs.v4.f64 [%0], {%1, %2, %3, %4};"
+               :
+               : "l"(p), "d"(r[0]), "d"(r[1]), "d"(r[2]), "d"(r[3])
+               : "memory");
+}
+
+// A lane's columns of one row: LD = 1 one vector, 2 two vectors, 4 two
+// vectors as one 32-byte access.
+template <typename T, int V, int LD>
+__device__ __forceinline__ void ld_slice(const T* p, T* r) {
+  if (LD == 4) {
+    ld32(p, r);
+  } else {
+#pragma unroll
+    for (int q = 0; q < LD; ++q) ld<T, V>(p + q * V, r + q * V);
+  }
+}
+template <typename T, int V, int LD>
+__device__ __forceinline__ void st_slice(T* p, const T* r) {
+  if (LD == 4) {
+    st32(p, r);
+  } else {
+#pragma unroll
+    for (int q = 0; q < LD; ++q) st<T, V>(p + q * V, r + q * V);
+  }
+}
+
+template <int NX, int NY, typename T, int LD, bool PLAQ, bool JW>
 __global__ void __launch_bounds__(kThreads, PLAQ ? LGT_FIXED_MINB_PLAQ : LGT_FIXED_MINB)
     k_hpsi_fixed(HpsiArgs<T> a) {
   using S = Shape<NX, NY>;
   constexpr int V = 16 / int(sizeof(T));
-  constexpr int W = V * VPL;  // columns per lane
+  constexpr int W = V * (LD == 1 ? 1 : 2);  // columns per lane
   constexpr int MM = list_stride<NX, NY, PLAQ>();
   extern __shared__ __align__(16) unsigned char smem[];
   const int K = a.K;
@@ -303,15 +351,13 @@ __global__ void __launch_bounds__(kThreads, PLAQ ? LGT_FIXED_MINB_PLAQ : LGT_FIX
     // lane slice: W contiguous columns (interleaving the row's lanes so that
     // one load instruction covers whole sectors measured slower)
     const int col0 = (it - rl * lpr) * W;
-    constexpr int qstep = V;
     const uint32_t m = s_meta[wid * 32 + rl];
     const int cnt = int(m & 255u), nh = int((m >> 8) & 255u);
     const T e2 = T(int((m >> 16) & 255u)), stag = T(int(m >> 24) - 128);
     const uint32_t* lst = nbr + rl * MM;
     T ah[W], ap[W], xd[W], xs[LGT_FIXED_UNROLL][W];
     const T* px = x + size_t(row) * C + col0;
-#pragma unroll
-    for (int q = 0; q < VPL; ++q) ld<T, V>(px + q * qstep, xd + q * V);
+    ld_slice<T, V, LD>(px, xd);
 #pragma unroll
     for (int e = 0; e < W; ++e) {
       ah[e] = T(0);
@@ -325,9 +371,7 @@ __global__ void __launch_bounds__(kThreads, PLAQ ? LGT_FIXED_MINB_PLAQ : LGT_FIX
       for (int u = 0; u < LGT_FIXED_UNROLL; ++u) {
         ent[u] = (n + u < nh) ? lst[n + u] : 0u;
         if (n + u < nh) {
-          const T* p = x + size_t(ent[u] & 0x7fffffffu) * C + col0;
-#pragma unroll
-          for (int q = 0; q < VPL; ++q) ld<T, V>(p + q * qstep, xs[u] + q * V);
+          ld_slice<T, V, LD>(x + size_t(ent[u] & 0x7fffffffu) * C + col0, xs[u]);
         } else {
 #pragma unroll
           for (int e = 0; e < W; ++e) xs[u][e] = T(0);
@@ -350,9 +394,7 @@ __global__ void __launch_bounds__(kThreads, PLAQ ? LGT_FIXED_MINB_PLAQ : LGT_FIX
 #pragma unroll
         for (int u = 0; u < LGT_FIXED_UNROLL; ++u) {
           if (n + u < cnt) {
-            const T* p = x + size_t(lst[n + u]) * C + col0;
-#pragma unroll
-            for (int q = 0; q < VPL; ++q) ld<T, V>(p + q * qstep, xs[u] + q * V);
+            ld_slice<T, V, LD>(x + size_t(lst[n + u]) * C + col0, xs[u]);
           } else {
 #pragma unroll
             for (int e = 0; e < W; ++e) xs[u][e] = T(0);
@@ -366,25 +408,23 @@ __global__ void __launch_bounds__(kThreads, PLAQ ? LGT_FIXED_MINB_PLAQ : LGT_FIX
     }
 #pragma unroll
     for (int e = 0; e < W; ++e) {
-      const int col = col0 + (e / V) * qstep + (e % V);
+      const int col = col0 + e;
       const int k = (ncomp == 2) ? (col >> 1) : col;
       const T cd = s_coef[k] * e2 + s_coef[K + k] * stag;  // (g^2/2) e2 + m stag
       T v = fma(s_coef[2 * K + k], ah[e], cd * xd[e]);
       if (PLAQ) v = fma(s_coef[3 * K + k], ap[e], v);
       xd[e] = v;
     }
-    T* py = y + size_t(row) * C + col0;
-#pragma unroll
-    for (int q = 0; q < VPL; ++q) st<T, V>(py + q * qstep, xd + q * V);
+    st_slice<T, V, LD>(y + size_t(row) * C + col0, xd);
   }
 }
 
 // Launches the fixed-shape kernel for (NX, NY); the caller has checked
 // dg == 1, rank tables present, N < 2^31, C % (16 / sizeof(T)) == 0 and
 // 16-byte aligned panels.
-template <int NX, int NY, typename T, int VPL, bool PLAQ, bool JW>
+template <int NX, int NY, typename T, int LD, bool PLAQ, bool JW>
 cudaError_t launch_shape_v(const HpsiArgs<T>& a, cudaStream_t s) {
-  auto kern = k_hpsi_fixed<NX, NY, T, VPL, PLAQ, JW>;
+  auto kern = k_hpsi_fixed<NX, NY, T, LD, PLAQ, JW>;
   const int bytes = smem_bytes<NX, NY, PLAQ, T>(a.K);
   static int attr_bytes = 48 * 1024;  // raised once, outside any capture (first launch is eager)
 #ifdef LGT_FIXED_CARVEOUT
@@ -407,10 +447,20 @@ cudaError_t launch_shape_v(const HpsiArgs<T>& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// Load mode: a.vpl = 1 one vector per lane, 2 two vectors, 3 two vectors as
+// one 32-byte access; 0 the built-in rule (two vectors when C allows).  A mode
+// the panel cannot take falls back to the next narrower one.
 template <int NX, int NY, typename T, bool PLAQ, bool JW>
 cudaError_t launch_shape_m(const HpsiArgs<T>& a, cudaStream_t s) {
   constexpr int V = 16 / int(sizeof(T));
-  if (a.vpl != 1 && a.C % (2 * V) == 0) return launch_shape_v<NX, NY, T, 2, PLAQ, JW>(a, s);
+  const bool two = a.C % (2 * V) == 0;
+  // 32-byte accesses: panels and the Krylov panel stride keep every row
+  // slice 32-byte aligned
+  const bool wide = two && (reinterpret_cast<uintptr_t>(a.x) & 31) == 0 &&
+                    (reinterpret_cast<uintptr_t>(a.y) & 31) == 0 &&
+                    (a.xsel == nullptr || (a.xstride * sizeof(T)) % 32 == 0);
+  if (a.vpl == 3 && wide) return launch_shape_v<NX, NY, T, 4, PLAQ, JW>(a, s);
+  if (a.vpl != 1 && two) return launch_shape_v<NX, NY, T, 2, PLAQ, JW>(a, s);
   return launch_shape_v<NX, NY, T, 1, PLAQ, JW>(a, s);
 }
 

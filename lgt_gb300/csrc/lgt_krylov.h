@@ -39,7 +39,13 @@ struct KrylovParams {
 struct KrylovCache;
 
 // Autotuner choice for one operator shape (see krylov.cu).
-enum HpsiVariant : int { kHpsiDefault = 0, kHpsiGeneric = 1, kHpsiFixed1 = 2, kHpsiFixed2 = 3 };
+enum HpsiVariant : int {
+  kHpsiDefault = 0,   // built-in rule
+  kHpsiGeneric = 1,   // run-time geometry
+  kHpsiFixed1 = 2,    // fixed shape, one 16-byte vector per lane
+  kHpsiFixed2 = 3,    // fixed shape, two 16-byte vectors per lane
+  kHpsiFixed2w = 4,   // fixed shape, two vectors as one 32-byte access
+};
 struct TuneChoice {
   int hpsi_variant = kHpsiDefault;
   int red_blocks = 0;
@@ -54,6 +60,12 @@ struct TuneChoice {
 // per point); mixed = FP32 storage.
 std::string krylov_autotune(const OpDev& op, KrylovCache* cache, int ncomp, int mixed,
                             cudaStream_t s, TuneChoice* out);
+
+// H*psi variant for this operator and panel width, timed on (x, y) at the
+// first call of each shape (x is only read; y is overwritten); sets op's
+// kernel selection.  No timing while `s` is capturing or LGT_AUTOTUNE=0.
+std::string hpsi_choose_d(OpDev* op, const double* x, double* y, int ncomp, cudaStream_t s);
+std::string hpsi_choose_f(OpDev* op, const float* x, float* y, int ncomp, cudaStream_t s);
 
 struct KrylovReport {
   int64_t matvecs = 0;

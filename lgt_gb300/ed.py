@@ -352,7 +352,7 @@ class Hamiltonian:
         ground states, 2: exponential steps); tunes on first use."""
         t = C.Tuning()
         C.check(C.load().lgt_autotune(self._h, int(ncomp), _PREC[precision], ctypes.byref(t)))
-        names = {0: "rule", 1: "generic", 2: "fixed_vpl1", 3: "fixed_vpl2"}
+        names = {0: "rule", 1: "generic", 2: "fixed_vpl1", 3: "fixed_vpl2", 4: "fixed_wide"}
         return {"hpsi_kernel": names.get(t.hpsi_kernel, str(t.hpsi_kernel)),
                 "reduce_blocks": t.reduce_blocks, "hpsi_ms": t.hpsi_ms,
                 "reduce_ms": t.reduce_ms, "measured": bool(t.measured)}

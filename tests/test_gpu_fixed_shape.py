@@ -1,8 +1,9 @@
 """GPU parity of the fixed-shape H*psi kernels (4x3, 3x4 and 4x4 at dg = 1).
 
 Panels with C = K * ncomp a multiple of the vector width run the
-compile-time kernels; every column width that selects a different variant
-(one or two vector loads per lane) is covered, for all four model flags.
+compile-time kernels; every load mode (one or two 16-byte vectors per lane,
+two vectors as one 32-byte access; forced with LGT_HPSI_VARIANT) and every
+column width that changes it is covered, for all four model flags.
 Bars: 1e-12 relative to max |y| (FP64) and 2e-6 (FP32) against the FP64
 oracle's CSR matrix for the reference and plaquette+JW models; against the
 run-time-geometry kernel (itself checked against the oracle in
@@ -44,10 +45,12 @@ WIDTHS = {"fp64": [(1, True), (2, True), (8, True), (4, False)],
           "fp32": [(2, True), (4, True), (8, True), (8, False)]}
 
 
+@pytest.mark.parametrize("variant", ["2", "3", "4"])  # one / two vectors, one 32-byte access
 @pytest.mark.parametrize("nx,ny,kind", [(4, 3, "stag"), (3, 4, "stag"), (3, 4, "string")])
 @pytest.mark.parametrize("model", ["ref", "pjw"])
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
-def test_fixed_vs_oracle(oracle, lgt, nx, ny, kind, model, prec):
+def test_fixed_vs_oracle(oracle, lgt, nx, ny, kind, model, prec, variant, monkeypatch):
+    monkeypatch.setenv("LGT_HPSI_VARIANT", variant)
     ob, gb = _pair(oracle, lgt, nx, ny, kind)
     rng = np.random.default_rng(nx * 10 + ny)
     Hos = {}
@@ -66,10 +69,12 @@ def test_fixed_vs_oracle(oracle, lgt, nx, ny, kind, model, prec):
         H.close()
 
 
+@pytest.mark.parametrize("variant", ["2", "3", "4"])
 @pytest.mark.parametrize("nx,ny", [(4, 3), (3, 4)])
 @pytest.mark.parametrize("model", ["jw", "plaq"])
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
-def test_fixed_vs_generic_models(oracle, lgt, nx, ny, model, prec):
+def test_fixed_vs_generic_models(oracle, lgt, nx, ny, model, prec, variant, monkeypatch):
+    monkeypatch.setenv("LGT_HPSI_VARIANT", variant)
     ob, gb = _pair(oracle, lgt, nx, ny, "stag")
     rng = np.random.default_rng(3)
     for K, cplx in WIDTHS[prec]:
@@ -83,10 +88,12 @@ def test_fixed_vs_generic_models(oracle, lgt, nx, ny, model, prec):
         H.close()
 
 
+@pytest.mark.parametrize("variant", ["3", "4"])
 @pytest.mark.parametrize("model", ["ref", "pjw"])
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
-def test_fixed_4x4_vs_generic(lgt, model, prec):
+def test_fixed_4x4_vs_generic(lgt, model, prec, variant, monkeypatch):
     """4x4 staggered sector (N = 8,563,545), K = 2 complex and K = 4 complex."""
+    monkeypatch.setenv("LGT_HPSI_VARIANT", variant)
     st, _ = lgt.build_basis(4, 4, 1, lgt.staggered_charges(4, 4))
     assert len(st) == 8563545
     rng = np.random.default_rng(44)
