@@ -38,9 +38,6 @@ constexpr int kMaxDim = 64;
 #ifndef LGT_MD_ROWS
 #define LGT_MD_ROWS 1  // rows per trip of the Gram-Schmidt dot kernel (2 measured slower)
 #endif
-#ifndef LGT_UPD_CHAINS
-#define LGT_UPD_CHAINS 2  // independent FMA chains of the update (4 measured slower)
-#endif
 
 #define KCK(call)                                                                  \
   do {                                                                             \
@@ -57,6 +54,21 @@ __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
   x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
   return x ^ (x >> 31);
 }
+
+// FP32 -> FP64 widening by integer operations on the bit pattern (IEEE-754
+// binary32 -> binary64: exponent rebiased by 1023 - 127, mantissa shifted
+// left by 29), so the mixed path's conversions stay off GB300's narrow FP64
+// pipe.  Exact for normal numbers; FP32 subnormals (below 1.2e-38) become
+// zero; infinities and NaNs stay infinities and NaNs.
+__device__ __forceinline__ double widen(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xffu;
+  const uint32_t m = (e == 0u) ? 0u : (u & 0x7fffffu);
+  const uint32_t ed = (e == 0u) ? 0u : ((e == 0xffu) ? 0x7ffu : e + 896u);
+  const uint32_t hi = (u & 0x80000000u) | (ed << 20) | (m >> 3);
+  return __hiloint2double(int(hi), int(m << 29));
+}
+__device__ __forceinline__ double widen(double d) { return d; }
 
 // Standard normal samples from a counter-based hash (Box-Muller).  Point k
 // of seed s draws the same vector whatever K is.
@@ -111,8 +123,8 @@ __global__ void __launch_bounds__(kT) k_multidot(const S* __restrict__ V, size_t
           const int64_t r = row + int64_t(u) * RG;
           ok[u] = r < r1;
           off[u] = size_t(ok[u] ? r : row) * C;
-          w[u] = ok[u] ? double(W[off[u] + c]) : 0.0;
-          wx[u] = (NC == 2 && ok[u]) ? double(W[off[u] + (c ^ 1)]) : 0.0;
+          w[u] = ok[u] ? widen(W[off[u] + c]) : 0.0;
+          wx[u] = (NC == 2 && ok[u]) ? widen(W[off[u] + (c ^ 1)]) : 0.0;
         }
 #pragma unroll
         for (int q = 0; q < kIC; ++q) {
@@ -120,7 +132,7 @@ __global__ void __launch_bounds__(kT) k_multidot(const S* __restrict__ V, size_t
 #pragma unroll
             for (int u = 0; u < LGT_MD_ROWS; ++u) {
               const double v =
-                  (i0 + q < Jv) ? (ok[u] ? double(V[size_t(i0 + q) * vstride + off[u] + c]) : 0.0)
+                  (i0 + q < Jv) ? (ok[u] ? widen(V[size_t(i0 + q) * vstride + off[u] + c]) : 0.0)
                                 : w[u];
               a[q] = fma(v, w[u], a[q]);
               if (NC == 2) b[q] = fma(v, wx[u], b[q]);
@@ -188,8 +200,9 @@ __global__ void k_finish_dots(const double* part, int nblk, int Jmax, const int*
 // sums of |W|^2 per column of every active point.
 template <typename S, int NC>
 __global__ void __launch_bounds__(kT) k_update(const S* __restrict__ V, size_t vstride,
-                                               const int* jstate, int jfixed, S* W, int64_t N,
-                                               int C, int ncomp, const double* h, int K,
+                                               const int* jstate, int jfixed, S* __restrict__ W,
+                                               int64_t N, int C, int ncomp,
+                                               const double* __restrict__ h, int K,
                                                const int* status, int64_t rpb, double* npart,
                                                const int* need) {
   __shared__ double red[kT];
@@ -205,51 +218,35 @@ __global__ void __launch_bounds__(kT) k_update(const S* __restrict__ V, size_t v
   if (act) {
     for (int64_t row = r0 + rg; row < r1; row += RG) {
       const size_t off = size_t(row) * C;
-      double w0 = double(W[off + c]), w1 = 0.0;
+      // two independent chains (even / odd basis vectors); the first starts
+      // from W itself
+      double w0 = widen(W[off + c]), w1 = 0.0;
       int i = 0;
-      if (NC == 1) {
-        // LGT_UPD_CHAINS independent chains over consecutive basis vectors
-        double wc[LGT_UPD_CHAINS];
-#pragma unroll
-        for (int u = 0; u < LGT_UPD_CHAINS; ++u) wc[u] = 0.0;
-        for (; i + LGT_UPD_CHAINS <= Ju; i += LGT_UPD_CHAINS) {
-#pragma unroll
-          for (int u = 0; u < LGT_UPD_CHAINS; ++u)
-            wc[u] = fma(-h[(size_t(i + u) * K + k) * 2 + 0],
-                        double(V[size_t(i + u) * vstride + off + c]), wc[u]);
-        }
-#pragma unroll
-        for (int u = 0; u < LGT_UPD_CHAINS; ++u) w1 += wc[u];
-      }
-      // two independent chains (even / odd basis vectors)
       for (; i + 1 < Ju; i += 2) {
-        const double hr0 = h[(size_t(i) * K + k) * 2 + 0];
-        const double hr1 = h[(size_t(i + 1) * K + k) * 2 + 0];
-        const double v0 = double(V[size_t(i) * vstride + off + c]);
-        const double v1 = double(V[size_t(i + 1) * vstride + off + c]);
-        w0 = fma(-hr0, v0, w0);
-        w1 = fma(-hr1, v1, w1);
+        const double hr0 = __ldg(h + (size_t(i) * K + k) * 2 + 0);
+        const double hr1 = __ldg(h + (size_t(i + 1) * K + k) * 2 + 0);
+        w0 = fma(-hr0, widen(V[size_t(i) * vstride + off + c]), w0);
+        w1 = fma(-hr1, widen(V[size_t(i + 1) * vstride + off + c]), w1);
         if (NC == 2) {
           // (hr + i hi)(v_re + i v_im): re = hr v_re - hi v_im, im = hr v_im + hi v_re
-          const double hi0 = h[(size_t(i) * K + k) * 2 + 1];
-          const double hi1 = h[(size_t(i + 1) * K + k) * 2 + 1];
-          const double vp0 = double(V[size_t(i) * vstride + off + (c ^ 1)]);
-          const double vp1 = double(V[size_t(i + 1) * vstride + off + (c ^ 1)]);
-          w0 = fma((c & 1) ? -hi0 : hi0, vp0, w0);
-          w1 = fma((c & 1) ? -hi1 : hi1, vp1, w1);
+          const double hi0 = __ldg(h + (size_t(i) * K + k) * 2 + 1);
+          const double hi1 = __ldg(h + (size_t(i + 1) * K + k) * 2 + 1);
+          w0 = fma((c & 1) ? -hi0 : hi0, widen(V[size_t(i) * vstride + off + (c ^ 1)]), w0);
+          w1 = fma((c & 1) ? -hi1 : hi1, widen(V[size_t(i + 1) * vstride + off + (c ^ 1)]), w1);
         }
       }
       if (i < Ju) {
-        const double hr = h[(size_t(i) * K + k) * 2 + 0];
-        w0 = fma(-hr, double(V[size_t(i) * vstride + off + c]), w0);
+        const double hr = __ldg(h + (size_t(i) * K + k) * 2 + 0);
+        w0 = fma(-hr, widen(V[size_t(i) * vstride + off + c]), w0);
         if (NC == 2) {
-          const double hi = h[(size_t(i) * K + k) * 2 + 1];
-          w0 = fma((c & 1) ? -hi : hi, double(V[size_t(i) * vstride + off + (c ^ 1)]), w0);
+          const double hi = __ldg(h + (size_t(i) * K + k) * 2 + 1);
+          w0 = fma((c & 1) ? -hi : hi, widen(V[size_t(i) * vstride + off + (c ^ 1)]), w0);
         }
       }
       const double w = w0 + w1;
-      if (Ju > 0) W[off + c] = S(w);
-      const double ws = double(S(w));
+      const S wst = S(w);
+      if (Ju > 0) W[off + c] = wst;
+      const double ws = widen(wst);
       nrm = fma(ws, ws, nrm);
     }
   }
@@ -585,12 +582,12 @@ __global__ void k_combine(const S* __restrict__ V, size_t vstride, const double*
     double acc = 0.0;
     for (int i = 0; i < nk; ++i) {
       const double cr = coef[(size_t(k) * ldT + i) * 2 + 0];
-      const double v = double(V[size_t(i) * vstride + off + c]);
+      const double v = widen(V[size_t(i) * vstride + off + c]);
       if (NC == 1) {
         acc = fma(cr, v, acc);
       } else {
         const double ci = coef[(size_t(k) * ldT + i) * 2 + 1];
-        const double vp = double(V[size_t(i) * vstride + off + (c ^ 1)]);
+        const double vp = widen(V[size_t(i) * vstride + off + (c ^ 1)]);
         acc += (c & 1) ? (cr * v + ci * vp) : (cr * v - ci * vp);
       }
     }
@@ -616,13 +613,13 @@ __global__ void k_combine_split(const S* __restrict__ V, size_t vstride, const d
     const int na = len[ca], nb = len[cb];
     // the real column contributes (Re c) v to Re psi and (Im c) v to Im psi
     for (int i = 0; i < na; ++i)
-      acc = fma(coef[(size_t(ca) * ldT + i) * 2 + comp], double(V[size_t(i) * vstride + off + ca]),
+      acc = fma(coef[(size_t(ca) * ldT + i) * 2 + comp], widen(V[size_t(i) * vstride + off + ca]),
                 acc);
     // i (cr + i ci) v = -ci v + i cr v
     for (int i = 0; i < nb; ++i) {
       const double cf = comp ? coef[(size_t(cb) * ldT + i) * 2 + 0]
                              : -coef[(size_t(cb) * ldT + i) * 2 + 1];
-      acc = fma(cf, double(V[size_t(i) * vstride + off + cb]), acc);
+      acc = fma(cf, widen(V[size_t(i) * vstride + off + cb]), acc);
     }
     out[off + c] = acc;
   }
