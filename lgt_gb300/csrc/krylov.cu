@@ -35,9 +35,6 @@ namespace {
 constexpr int kT = 256;   // threads of the panel kernels
 constexpr int kIC = 8;    // Krylov vectors per multidot pass
 constexpr int kMaxDim = 64;
-#ifndef LGT_MD_ROWS
-#define LGT_MD_ROWS 1  // rows per trip of the Gram-Schmidt dot kernel (2 measured slower)
-#endif
 
 #define KCK(call)                                                                  \
   do {                                                                             \
@@ -94,8 +91,20 @@ __global__ void k_randn(S* out, int64_t N, int C, int ncomp, uint64_t seed) {
 // part[blk][i][1][c] = sum_rows V_i[row][c] W[row][c^1]   (complex only)
 // With self = 1, index J holds W against itself (its squared norm).  Columns
 // of points with need[k] == 0 contribute zero (need may be null).
+// Measured on the 4x4 quench panel (K = 8 complex, FP64 and FP32 storage):
+// the dot kernel issues a chunk's loads before its FMAs and keeps 4 blocks
+// per SM; the update's plain two-chain loop beats hoisted loads.
+#ifndef LGT_MD_HOIST
+#define LGT_MD_HOIST 1
+#endif
+#ifndef LGT_UPD_HOIST
+#define LGT_UPD_HOIST 0
+#endif
+#ifndef LGT_MD_MINB
+#define LGT_MD_MINB 4  // resident blocks per SM the dot kernel's registers must allow
+#endif
 template <typename S, int NC>
-__global__ void __launch_bounds__(kT) k_multidot(const S* __restrict__ V, size_t vstride,
+__global__ void __launch_bounds__(kT, LGT_MD_MINB) k_multidot(const S* __restrict__ V, size_t vstride,
                                                  const int* jstate, int jfixed,
                                                  const S* __restrict__ W, int64_t N, int C,
                                                  int64_t rpb, double* part, int Jmax,
@@ -113,32 +122,38 @@ __global__ void __launch_bounds__(kT) k_multidot(const S* __restrict__ V, size_t
 #pragma unroll
     for (int q = 0; q < kIC; ++q) a[q] = b[q] = 0.0;
     if (act) {
-      // LGT_MD_ROWS rows per trip: more independent loads in flight
-      for (int64_t row = r0 + rg; row < r1; row += int64_t(RG) * LGT_MD_ROWS) {
-        double w[LGT_MD_ROWS], wx[LGT_MD_ROWS];
-        size_t off[LGT_MD_ROWS];
-        bool ok[LGT_MD_ROWS];
+      for (int64_t row = r0 + rg; row < r1; row += RG) {
+        const size_t off = size_t(row) * C;
+        const double w = widen(W[off + c]);
+        const double wx = (NC == 2) ? widen(W[off + (c ^ 1)]) : 0.0;
+#if LGT_MD_HOIST
+        // every load of the chunk is issued before the first use; slots past
+        // the basis read its last vector again (an L1 hit) and are skipped
+        double v[kIC];
+        const int ilast = (Jv > 0) ? Jv - 1 : 0;
 #pragma unroll
-        for (int u = 0; u < LGT_MD_ROWS; ++u) {
-          const int64_t r = row + int64_t(u) * RG;
-          ok[u] = r < r1;
-          off[u] = size_t(ok[u] ? r : row) * C;
-          w[u] = ok[u] ? widen(W[off[u] + c]) : 0.0;
-          wx[u] = (NC == 2 && ok[u]) ? widen(W[off[u] + (c ^ 1)]) : 0.0;
+        for (int q = 0; q < kIC; ++q) {
+          const int i = (i0 + q < Jv) ? i0 + q : ilast;
+          v[q] = widen(V[size_t(i) * vstride + off + c]);
         }
 #pragma unroll
         for (int q = 0; q < kIC; ++q) {
           if (i0 + q < J) {
-#pragma unroll
-            for (int u = 0; u < LGT_MD_ROWS; ++u) {
-              const double v =
-                  (i0 + q < Jv) ? (ok[u] ? widen(V[size_t(i0 + q) * vstride + off[u] + c]) : 0.0)
-                                : w[u];
-              a[q] = fma(v, w[u], a[q]);
-              if (NC == 2) b[q] = fma(v, wx[u], b[q]);
-            }
+            const double vq = (i0 + q < Jv) ? v[q] : w;
+            a[q] = fma(vq, w, a[q]);
+            if (NC == 2) b[q] = fma(vq, wx, b[q]);
           }
         }
+#else
+#pragma unroll
+        for (int q = 0; q < kIC; ++q) {
+          if (i0 + q < J) {
+            const double vq = (i0 + q < Jv) ? widen(V[size_t(i0 + q) * vstride + off + c]) : w;
+            a[q] = fma(vq, w, a[q]);
+            if (NC == 2) b[q] = fma(vq, wx, b[q]);
+          }
+        }
+#endif
       }
 #pragma unroll
       for (int q = 0; q < kIC; ++q) {
@@ -222,6 +237,23 @@ __global__ void __launch_bounds__(kT) k_update(const S* __restrict__ V, size_t v
       // from W itself
       double w0 = widen(W[off + c]), w1 = 0.0;
       int i = 0;
+      if (NC == 1 && LGT_UPD_HOIST) {
+        // four basis vectors per trip, loads first (clamped to the last
+        // vector, an L1 hit), FMAs only for the vectors that exist
+        for (; i < Ju; i += 4) {
+          double vv[4], hh[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int ii = (i + u < Ju) ? i + u : Ju - 1;
+            hh[u] = __ldg(h + (size_t(ii) * K + k) * 2);
+            vv[u] = widen(V[size_t(ii) * vstride + off + c]);
+          }
+          w0 = fma(-hh[0], vv[0], w0);
+          if (i + 1 < Ju) w1 = fma(-hh[1], vv[1], w1);
+          if (i + 2 < Ju) w0 = fma(-hh[2], vv[2], w0);
+          if (i + 3 < Ju) w1 = fma(-hh[3], vv[3], w1);
+        }
+      }
       for (; i + 1 < Ju; i += 2) {
         const double hr0 = __ldg(h + (size_t(i) * K + k) * 2 + 0);
         const double hr1 = __ldg(h + (size_t(i + 1) * K + k) * 2 + 0);
@@ -1117,10 +1149,8 @@ std::string autotune(OpDev* op, Work<S>& w, cudaStream_t s, TuneChoice* out) {
       }
       return double(ms) / 3.0;
     };
-    // reduction block counts: one Gram-Schmidt pass (dots and update)
-    // against J vectors (step index J - 1, all points active, h = 0)
-    const int jm1 = J - 1;
-    KCK(cudaMemcpyAsync(w.jstate, &jm1, sizeof(int), cudaMemcpyHostToDevice, s));
+    // reduction block counts: Gram-Schmidt passes (dots and update) against
+    // 2, 5 and 8 vectors (all points active, h = 0), summed
     KCK(cudaMemsetAsync(w.status, 0, sizeof(int) * w.K, s));
     KCK(cudaMemsetAsync(w.h, 0, sizeof(double) * size_t(w.ldT) * w.K * 2, s));
     double best = 1e30;
@@ -1130,11 +1160,16 @@ std::string autotune(OpDev* op, Work<S>& w, cudaStream_t s, TuneChoice* out) {
       w.red.plan(w.N, w.C, cap);
       if (w.red.nblk == last_nblk) continue;
       last_nblk = w.red.nblk;
-      const double t = timed([&] {
-        cudaError_t e = launch_multidot<S, S>(w, w.V, w.vstride, w.jstate, 0, w.W, s);
-        if (e == cudaSuccess) e = launch_update<S>(w, w.W, s);
-        return e;
-      });
+      double t = 0.0;
+      for (int jv : {2, 5, 8}) {
+        const int jj = (jv < J ? jv : J) - 1;  // step index: jj + 1 vectors
+        KCK(cudaMemcpyAsync(w.jstate, &jj, sizeof(int), cudaMemcpyHostToDevice, s));
+        t += timed([&] {
+          cudaError_t e = launch_multidot<S, S>(w, w.V, w.vstride, w.jstate, 0, w.W, s);
+          if (e == cudaSuccess) e = launch_update<S>(w, w.W, s);
+          return e;
+        });
+      }
       if (t < best) {
         best = t;
         c.red_blocks = cap;
