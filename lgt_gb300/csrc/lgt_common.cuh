@@ -160,6 +160,21 @@ __host__ __device__ inline int popc32(uint32_t v) {
 __device__ inline void raise_err(int* err, int bit) {
   if (err) atomicOr(err, bit);
 }
+
+// FP32 -> FP64 widening by integer operations on the bit pattern (IEEE-754
+// binary32 -> binary64: exponent rebiased by 1023 - 127, mantissa shifted
+// left by 29), so mixed-precision kernels keep conversions off GB300's
+// narrow FP64 pipe.  Exact for normal numbers; FP32 subnormals (below
+// 1.2e-38) become zero; infinities and NaNs stay infinities and NaNs.
+__device__ __forceinline__ double widen(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xffu;
+  const uint32_t m = (e == 0u) ? 0u : (u & 0x7fffffu);
+  const uint32_t ed = (e == 0u) ? 0u : ((e == 0xffu) ? 0x7ffu : e + 896u);
+  const uint32_t hi = (u & 0x80000000u) | (ed << 20) | (m >> 3);
+  return __hiloint2double(int(hi), int(m << 29));
+}
+__device__ __forceinline__ double widen(double d) { return d; }
 #endif
 
 }  // namespace lgt

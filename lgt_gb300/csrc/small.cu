@@ -148,26 +148,37 @@ __device__ double block_sum(double v, double* red) {
 
 // Number of eigenvalues of the tridiagonal (a, b) below x: sign changes of
 // the leading principal minors p_i = det(T_i - x I), from the three-term
-// recurrence p_i = (a_i - x) p_{i-1} - b_{i-1}^2 p_{i-2}.  Division-free (FP64
-// division is a long dependent chain on this part); the minors are rescaled
-// by 2^-600 when they grow past 2^600 and an exact zero takes the sign
-// opposite to its predecessor.
-__device__ int sturm_below(const double* a, const double* b, int n, double x) {
+// recurrence p_i = (a_i - x) p_{i-1} - b_{i-1}^2 p_{i-2} (bb holds b^2).
+// Division-free (FP64 division is a long dependent chain on this part); the
+// minors are rescaled by 2^-600 when they grow past 2^600; an exact zero
+// takes the sign opposite to its predecessor.  Signs, zeros and magnitudes
+// are read from the bit patterns (integer operations), so a step costs
+// three FP64 operations.
+__device__ __forceinline__ int sign_bit(double v) { return int(uint32_t(__double2hiint(v)) >> 31); }
+__device__ __forceinline__ bool is_zero(double v) {
+  return ((uint32_t(__double2hiint(v)) & 0x7fffffffu) | uint32_t(__double2loint(v))) == 0u;
+}
+__device__ __forceinline__ int exp_bits(double v) {
+  return int((uint32_t(__double2hiint(v)) >> 20) & 0x7ffu);
+}
+
+__device__ int sturm_below(const double* a, const double* bb, int n, double x) {
   double p0 = 1.0, p1 = a[0] - x;
-  int sp = 1;
-  int s1 = (p1 > 0.0) ? 1 : ((p1 < 0.0) ? -1 : -sp);
+  int sp = 0;  // sign bit of the previous minor (p_{-1} = 1 > 0)
+  int s1 = is_zero(p1) ? 1 - sp : sign_bit(p1);
   int cnt = (s1 != sp) ? 1 : 0;
   sp = s1;
   for (int i = 1; i < n; ++i) {
-    double p2 = fma(a[i] - x, p1, -(b[i - 1] * b[i - 1]) * p0);
-    if (fabs(p2) > 0x1.0p600) {
+    double p2 = fma(a[i] - x, p1, -bb[i - 1] * p0);
+    const int e2 = exp_bits(p2);
+    if (e2 > 1023 + 600) {
       p2 *= 0x1.0p-600;
       p1 *= 0x1.0p-600;
-    } else if (fabs(p2) < 0x1.0p-600 && fabs(p1) < 0x1.0p-600) {
+    } else if (e2 < 1023 - 600 && exp_bits(p1) < 1023 - 600) {
       p2 *= 0x1.0p600;
       p1 *= 0x1.0p600;
     }
-    const int s2 = (p2 > 0.0) ? 1 : ((p2 < 0.0) ? -1 : -sp);
+    const int s2 = is_zero(p2) ? 1 - sp : sign_bit(p2);
     cnt += (s2 != sp) ? 1 : 0;
     sp = s2;
     p0 = p1;
@@ -180,11 +191,18 @@ __device__ int sturm_below(const double* a, const double* b, int n, double x) {
 // multisection of the Sturm count (32 probes per round), then inverse
 // iteration on the positive-definite T - (theta - delta) I by lane 0,
 // starting from z when warm (z holds the previous eigenvector, padded with
-// zeros) or from ones.  Called by one full warp; z (n entries) is written by
-// lane 0.
+// zeros) or from ones.  When warm, the previous lowest Ritz value th_prev
+// (an upper bound: the lowest Ritz value only decreases as the Krylov space
+// grows) and its residual r_prev bracket the search, [th_prev - 2 r_prev,
+// th_prev], if the Sturm count confirms the lower end; otherwise the
+// Gershgorin interval is used.  Called by one full warp; bb (n entries of
+// work space after the first kMaxM) and z are written by lane 0 / the warp.
 __device__ double warp_lowest_eig(const double* a, const double* b, int n, double* z,
-                                  double* work, bool warm) {
+                                  double* work, bool warm, double th_prev, double r_prev) {
   const int lane = threadIdx.x & 31;
+  double* bb = work + 2 * kMaxM;
+  for (int i = lane; i < n - 1; i += 32) bb[i] = b[i] * b[i];
+  __syncwarp();
   double lo = a[0], hi = a[0];
   for (int i = 0; i < n; ++i) {
     const double r = ((i > 0) ? fabs(b[i - 1]) : 0.0) + ((i < n - 1) ? fabs(b[i]) : 0.0);
@@ -192,11 +210,23 @@ __device__ double warp_lowest_eig(const double* a, const double* b, int n, doubl
     hi = fmax(hi, a[i] + r);
   }
   const double scale = fmax(fmax(fabs(lo), fabs(hi)), 1e-300);
+  if (warm) {
+    const double whi = fmin(hi, th_prev + 8.0 * 2.2e-16 * scale);
+    const double wlo = fmax(lo, th_prev - fmax(2.0 * r_prev, 1e-9 * scale));
+    // lane 0 probes the lower end, lane 1 the upper end
+    const double xp = (lane == 0) ? wlo : whi;
+    const int c = sturm_below(a, bb, n, xp);
+    const int c_lo = __shfl_sync(0xffffffffu, c, 0), c_hi = __shfl_sync(0xffffffffu, c, 1);
+    if (c_lo == 0 && c_hi >= 1) {
+      lo = wlo;
+      hi = whi;
+    }
+  }
   for (int it = 0; it < 40; ++it) {
     if (hi - lo <= 2.2e-16 * scale) break;
     const double step = (hi - lo) / 33.0;
     const double x = lo + step * double(lane + 1);
-    const unsigned bal = __ballot_sync(0xffffffffu, sturm_below(a, b, n, x) >= 1);
+    const unsigned bal = __ballot_sync(0xffffffffu, sturm_below(a, bb, n, x) >= 1);
     if (bal) {
       const int L = __ffs(bal) - 1;
       const double nhi = lo + step * double(L + 1);
@@ -258,7 +288,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
   __shared__ double s_alpha[kMaxM + 1], s_beta[kMaxM + 1], s_h[kMaxM + 1], s_z[kMaxM + 1];
   __shared__ double s_part[kMaxM + 1][kWarpsCta];
   __shared__ double s_red[kWarpsCta];
-  __shared__ double s_work[2 * kMaxM];
+  __shared__ double s_work[3 * kMaxM];
   __shared__ double s_theta, s_resid;
   __shared__ int s_flag, s_zwarm;
   const SmallUnit U = units[blockIdx.x];
@@ -342,18 +372,23 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
             if (r < N) {
 #pragma unroll
               for (int q = 0; q < 4; ++q)
-                if (b0 + q <= j) p[q] = fma(double(V[size_t(b0 + q) * N + r]), w[i], p[q]);
+                if (b0 + q <= j) p[q] = fma(widen(V[size_t(b0 + q) * N + r]), w[i], p[q]);
             }
           }
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) p[q] += __shfl_xor_sync(0xffffffffu, p[q], o);
-          }
-          if (lane < 4 && b0 + lane <= j) {
-            const double mine = (lane == 0) ? p[0] : (lane == 1) ? p[1] : (lane == 2) ? p[2] : p[3];
-            s_part[b0 + lane][wid] = mine;
-          }
+          // reduce-scatter over the warp: after the xor-16 and xor-8 steps
+          // lane l holds value 2 * bit4(l) + bit3(l) summed over 4 lanes, the
+          // last three steps finish it (6 FP64 adds per lane instead of 20)
+          const bool b4 = lane & 16, b3 = lane & 8;
+          const double r0 = __shfl_xor_sync(0xffffffffu, b4 ? p[0] : p[2], 16);
+          const double r1 = __shfl_xor_sync(0xffffffffu, b4 ? p[1] : p[3], 16);
+          const double k0 = (b4 ? p[2] : p[0]) + r0, k1 = (b4 ? p[3] : p[1]) + r1;
+          const double r2 = __shfl_xor_sync(0xffffffffu, b3 ? k0 : k1, 8);
+          double kk = (b3 ? k1 : k0) + r2;
+          kk += __shfl_xor_sync(0xffffffffu, kk, 4);
+          kk += __shfl_xor_sync(0xffffffffu, kk, 2);
+          kk += __shfl_xor_sync(0xffffffffu, kk, 1);
+          const int qv = lane >> 3;  // lanes 0, 8, 16, 24 hold values 0..3
+          if ((lane & 7) == 0 && b0 + qv <= j) s_part[b0 + qv][wid] = kk;
         }
         __syncthreads();
         if (tid <= j) {
@@ -375,11 +410,9 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
           for (int i = 0; i < R; ++i) {
             const int r = tid + i * kCta;
             if (r < N) {
-              double t[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
               for (int q = 0; q < 4; ++q)
-                if (b0 + q <= j) t[q] = h4[q] * double(V[size_t(b0 + q) * N + r]);
-              w[i] -= (t[0] + t[1]) + (t[2] + t[3]);
+                if (b0 + q <= j) w[i] = fma(-h4[q], widen(V[size_t(b0 + q) * N + r]), w[i]);
             }
           }
         }
@@ -412,7 +445,8 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
       if (check) {
         __syncthreads();
         if (wid == 0) {
-          const double th = warp_lowest_eig(s_alpha, s_beta, n, s_z, s_work, s_zwarm != 0);
+          const double th =
+              warp_lowest_eig(s_alpha, s_beta, n, s_z, s_work, s_zwarm != 0, s_theta, s_resid);
           if (lane == 0) {
             const double rr = exhausted ? 0.0 : fabs(s_beta[n - 1] * s_z[n - 1]);
             // FP32 panels resolve residuals to ~1e-6 |H|: relative floor
@@ -442,7 +476,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
       const int r = tid + i * kCta;
       double xv = 0.0;
       if (r < N)
-        for (int b = 0; b < n; ++b) xv = fma(s_z[b], double(V[size_t(b) * N + r]), xv);
+        for (int b = 0; b < n; ++b) xv = fma(s_z[b], widen(V[size_t(b) * N + r]), xv);
       w[i] = xv;
     }
     if (converged || cycle >= prm.maxiter) break;
