@@ -5,6 +5,7 @@
 #include <cmath>
 #include <memory>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -476,6 +477,9 @@ SmallParams small_params(const KrylovParams& p) {
   q.check_every = p.check_every;
   q.seed = p.seed;
   q.start_given = p.start_given;
+  // launch shape of the per-CTA solver: rows held per thread (LGT_CTA_ROWS
+  // overrides the built-in choice, the smallest that fits 512 threads)
+  if (const char* e = getenv("LGT_CTA_ROWS")) q.rows_per_thread = atoi(e);
   return q;
 }
 

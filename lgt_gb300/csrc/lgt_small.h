@@ -51,6 +51,7 @@ struct SmallParams {
   int check_every;
   uint64_t seed;
   int start_given;
+  int rows_per_thread = 0;  // launch shape: 0 the smallest R with N <= 512 R
 };
 
 // One Hamiltonian's share of a batched launch.

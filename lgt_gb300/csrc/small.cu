@@ -28,7 +28,7 @@ namespace lgt {
 
 namespace {
 
-constexpr int kCta = 512;
+constexpr int kCta = 512;               // most threads per CTA
 constexpr int kWarpsCta = kCta / 32;
 constexpr int kMaxM = 64;
 
@@ -137,12 +137,12 @@ __device__ __forceinline__ double warp_sum(double v) {
 // Block-wide sum of one double per thread (all threads get the result).
 __device__ double block_sum(double v, double* red) {
   v = warp_sum(v);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   __syncthreads();
   if (lane == 0) red[wid] = v;
   __syncthreads();
   double s = 0.0;
-  for (int w = 0; w < kWarpsCta; ++w) s += red[w];
+  for (int w = 0; w < nw; ++w) s += red[w];
   return s;
 }
 
@@ -428,6 +428,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
   const SmallProblem P = probs[U.prob];
   const int N = P.N;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int nthr = blockDim.x, nwarps = nthr >> 5;  // rows r = tid + i * nthr, i < R
   const int m = (prm.m < N) ? prm.m : N;
   S* V = reinterpret_cast<S*>(U.V);
   const S cE = S(U.cE), cm = S(U.cm), ch = S(U.ch), cp = S(U.cp);
@@ -440,7 +441,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
   double nrm = 0.0;
 #pragma unroll
   for (int i = 0; i < R; ++i) {
-    const int r = tid + i * kCta;
+    const int r = tid + i * nthr;
     w[i] = (r < N) ? (prm.start_given ? U.psi[size_t(r) * U.psi_stride]
                                       : start_normal(prm.seed, U.k, r))
                    : 0.0;
@@ -449,7 +450,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
   nrm = sqrt(block_sum(nrm, s_red));
 #pragma unroll
   for (int i = 0; i < R; ++i) {
-    const int r = tid + i * kCta;
+    const int r = tid + i * nthr;
     if (r < N) V[r] = S(w[i] / nrm);
   }
   __syncthreads();
@@ -467,7 +468,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
       // w = H v_j (matvec in the storage precision)
 #pragma unroll
       for (int i = 0; i < R; ++i) {
-        const int r = tid + i * kCta;
+        const int r = tid + i * nthr;
         if (r < N) {
           S acc = (cE * S(P.e2[r]) + cm * S(P.stag[r])) * vj[r];
           const int q1 = P.rowptr[r + 1];
@@ -501,7 +502,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
           double p[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
           for (int i = 0; i < R; ++i) {
-            const int r = tid + i * kCta;
+            const int r = tid + i * nthr;
             if (r < N) {
 #pragma unroll
               for (int q = 0; q < 4; ++q)
@@ -526,10 +527,12 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
         __syncthreads();
         if (tid <= j) {
           double s0 = 0.0, s1 = 0.0;
-          for (int ww = 0; ww < kWarpsCta; ww += 2) {
+          int ww = 0;
+          for (; ww + 1 < nwarps; ww += 2) {
             s0 += s_part[tid][ww];
             s1 += s_part[tid][ww + 1];
           }
+          if (ww < nwarps) s0 += s_part[tid][ww];
           const double sum = s0 + s1;
           s_h[tid] = sum;
           if (tid == j) s_alpha[j] = (pass == 0) ? sum : s_alpha[j] + sum;
@@ -541,7 +544,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
           for (int q = 0; q < 4; ++q) h4[q] = (b0 + q <= j) ? s_h[b0 + q] : 0.0;
 #pragma unroll
           for (int i = 0; i < R; ++i) {
-            const int r = tid + i * kCta;
+            const int r = tid + i * nthr;
             if (r < N) {
 #pragma unroll
               for (int q = 0; q < 4; ++q)
@@ -569,7 +572,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
         const double rbeta = 1.0 / beta;
 #pragma unroll
         for (int i = 0; i < R; ++i) {
-          const int r = tid + i * kCta;
+          const int r = tid + i * nthr;
           if (r < N) vn[r] = S(w[i] * rbeta);
         }
       }
@@ -610,7 +613,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
     // Ritz vector x = sum z_i V_i (z of the last check, at size n)
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      const int r = tid + i * kCta;
+      const int r = tid + i * nthr;
       double xv = 0.0;
       if (r < N)
         for (int b = 0; b < n; ++b) xv = fma(s_z[b], widen(V[size_t(b) * N + r]), xv);
@@ -625,7 +628,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      const int r = tid + i * kCta;
+      const int r = tid + i * nthr;
       if (r < N) V[r] = S(w[i] / xn);
     }
     __syncthreads();
@@ -640,7 +643,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
   double* X = U.x;
 #pragma unroll
   for (int i = 0; i < R; ++i) {
-    const int r = tid + i * kCta;
+    const int r = tid + i * nthr;
     w[i] /= xn;
     if (r < N) X[r] = w[i];
   }
@@ -649,7 +652,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
   double ey = 0.0;
 #pragma unroll
   for (int i = 0; i < R; ++i) {
-    const int r = tid + i * kCta;
+    const int r = tid + i * nthr;
     y[i] = 0.0;
     if (r < N) {
       double acc = (U.cE * double(P.e2[r]) + U.cm * double(P.stag[r])) * X[r];
@@ -674,7 +677,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
   const double rnorm = sqrt(block_sum(rs, s_red));
 #pragma unroll
   for (int i = 0; i < R; ++i) {
-    const int r = tid + i * kCta;
+    const int r = tid + i * nthr;
     if (r < N) U.psi[size_t(r) * U.psi_stride] = w[i];
   }
   if (tid == 0) {
@@ -687,14 +690,24 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
   }
 }
 
+// Rows per thread R (a template case: the rows live in registers) and just
+// enough whole warps for the largest sector: idle lanes still occupy the
+// FP64 pipe in every warp instruction.  rows_per_thread = 0 takes the
+// smallest R with maxN <= 512 R; a larger R means fewer threads.
 template <typename S>
 cudaError_t launch_cta(const SmallProblem* probs, const SmallUnit* units, int nunits, int maxN,
-                       const SmallParams& prm, cudaStream_t s) {
-  const int R = (maxN + kCta - 1) / kCta;
-#define LGT_CTA_CASE(RR)                                                                  \
-  if (R <= RR) {                                                                          \
-    k_lanczos_cta<S, RR><<<nunits, kCta, 0, s>>>(probs, units, prm), lgt::note_launch(); \
-    return cudaGetLastError();                                                            \
+                       const SmallParams& prm, cudaStream_t s, int rows_per_thread) {
+  int R = (maxN + kCta - 1) / kCta;
+  if (rows_per_thread > R) R = rows_per_thread;
+  auto threads_for = [&](int rr) {
+    int t = ((maxN + rr - 1) / rr + 31) / 32 * 32;
+    return t < 64 ? 64 : t;  // the reduction of step j uses threads 0..j
+  };
+#define LGT_CTA_CASE(RR)                                                                    \
+  if (R <= RR) {                                                                            \
+    k_lanczos_cta<S, RR><<<nunits, threads_for(RR), 0, s>>>(probs, units, prm),            \
+        lgt::note_launch();                                                                 \
+    return cudaGetLastError();                                                              \
   }
   LGT_CTA_CASE(1)
   LGT_CTA_CASE(2)
@@ -835,8 +848,9 @@ std::string small_ground_states(const std::vector<SmallJob>& jobs, const SmallPa
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, s);
-  cudaError_t e = mixed ? launch_cta<float>(d_probs, d_units, int(nunits), maxN, prm, s)
-                        : launch_cta<double>(d_probs, d_units, int(nunits), maxN, prm, s);
+  cudaError_t e =
+      mixed ? launch_cta<float>(d_probs, d_units, int(nunits), maxN, prm, s, prm.rows_per_thread)
+            : launch_cta<double>(d_probs, d_units, int(nunits), maxN, prm, s, prm.rows_per_thread);
   cudaEventRecord(e1, s);
   if (e != cudaSuccess) return std::string("k_lanczos_cta: ") + cudaGetErrorString(e);
   std::vector<double> out(nunits * 8);
