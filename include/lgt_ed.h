@@ -164,6 +164,9 @@ LGT_API lgt_status lgt_basis_lookup(const lgt_basis* b, const int64_t* ref_keys,
 LGT_API lgt_status lgt_basis_rank(const lgt_basis* b, const uint64_t* order_keys, int64_t n,
                           int64_t* index0);
 
+/* Releases the caller's handle.  Hamiltonians made from the basis keep it
+   alive: handles may be destroyed in any order (the basis is freed with the
+   last of them). */
 LGT_API void lgt_basis_destroy(lgt_basis* b);
 
 /* Run this basis' work (and that of its Hamiltonians) on a caller-owned

@@ -258,14 +258,22 @@ lgt_status lgt_basis_rank(const lgt_basis* b, const uint64_t* order_keys, int64_
   return rank_common(b, order_keys, n, index0, false);
 }
 
-void lgt_basis_destroy(lgt_basis* b) {
-  if (!b) return;
+}  // extern "C"
+
+namespace {
+void release_basis(lgt_basis* b) {
+  if (!b || b->refs.fetch_sub(1) != 1) return;
   cudaSetDevice(b->device);
   cudaStreamSynchronize(b->B.stream);
   free_basis_device(&b->B);
   cudaStreamDestroy(b->own_stream);
   delete b;
 }
+}  // namespace
+
+extern "C" {
+
+void lgt_basis_destroy(lgt_basis* b) { release_basis(b); }
 
 lgt_status lgt_basis_set_stream(lgt_basis* b, void* stream) {
   if (!b) return fail(LGT_ERR_ARG, "null basis");
@@ -295,6 +303,7 @@ lgt_status lgt_ham_create(const lgt_basis* b, int32_t K, const double* g, const 
   lgt_ham* h = new (std::nothrow) lgt_ham();
   if (!h) return fail(LGT_ERR_MEMORY, "host allocation failed");
   h->b = b;
+  const_cast<lgt_basis*>(b)->refs.fetch_add(1);
   h->K = K;
   h->model = model;
   h->g.assign(g, g + K);
@@ -898,7 +907,9 @@ void lgt_ham_destroy(lgt_ham* h) {
   cudaFree(h->small.base);
   cudaFree(h->coef_d);
   cudaFree(h->coef_f);
+  lgt_basis* b = const_cast<lgt_basis*>(h->b);
   delete h;
+  release_basis(b);
 }
 
 }  // extern "C"

@@ -2,6 +2,8 @@
 // translation units that implement entry points).
 #pragma once
 
+#include <atomic>
+
 #include <string>
 #include <vector>
 
@@ -47,6 +49,10 @@ struct lgt_basis {
   BasisDev B;
   int device = 0;
   cudaStream_t own_stream = nullptr;
+  // owners: the caller's handle plus one per Hamiltonian made from it; the
+  // basis is freed when the last owner lets go (handles may be destroyed in
+  // any order, e.g. by a garbage collector)
+  std::atomic<int> refs{1};
 };
 
 struct lgt_ham {

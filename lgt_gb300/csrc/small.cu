@@ -17,7 +17,11 @@
 // nothing of the matrix values is stored.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "lgt_moves.cuh"
@@ -847,10 +851,47 @@ std::string small_ground_states(const std::vector<SmallJob>& jobs, const SmallPa
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
+  auto launch = [&](int rows) {
+    return mixed ? launch_cta<float>(d_probs, d_units, int(nunits), maxN, prm, s, rows)
+                 : launch_cta<double>(d_probs, d_units, int(nunits), maxN, prm, s, rows);
+  };
+  int rows = prm.rows_per_thread;
+  if (rows == 0 && !prm.start_given) {
+    // Autotuner: rows per thread R0 (the fewest that fit 512 threads) or
+    // 2 R0 (half the warps), timed on this batch once per (largest sector,
+    // CTAs, precision); the solve then runs with the faster one.
+    static std::mutex mu;
+    static std::map<std::tuple<int, int, int>, int> cache;
+    const auto key = std::make_tuple(maxN, int(nunits), mixed ? 1 : 0);
+    std::unique_lock<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+      rows = it->second;
+    } else {
+      const char* en = getenv("LGT_AUTOTUNE");
+      const int r0 = (maxN + 511) / 512;
+      rows = r0;
+      if (!(en && en[0] == '0') && 2 * r0 <= 16 && (maxN + 2 * r0 - 1) / (2 * r0) >= 64) {
+        float best = 3e38f;
+        for (int rr : {r0, 2 * r0}) {
+          cudaEventRecord(e0, s);
+          cudaError_t ce = launch(rr);
+          cudaEventRecord(e1, s);
+          if (ce != cudaSuccess) return std::string("k_lanczos_cta: ") + cudaGetErrorString(ce);
+          SCK(cudaEventSynchronize(e1));
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, e0, e1);
+          if (ms < best) {
+            best = ms;
+            rows = rr;
+          }
+        }
+      }
+      cache[key] = rows;
+    }
+  }
   cudaEventRecord(e0, s);
-  cudaError_t e =
-      mixed ? launch_cta<float>(d_probs, d_units, int(nunits), maxN, prm, s, prm.rows_per_thread)
-            : launch_cta<double>(d_probs, d_units, int(nunits), maxN, prm, s, prm.rows_per_thread);
+  cudaError_t e = launch(rows);
   cudaEventRecord(e1, s);
   if (e != cudaSuccess) return std::string("k_lanczos_cta: ") + cudaGetErrorString(e);
   std::vector<double> out(nunits * 8);

@@ -95,3 +95,13 @@ def test_sector_helpers_match_oracle(oracle):
     for nx, ny in [(3, 2), (4, 4), (3, 4)]:
         assert np.array_equal(L.staggered_charges(nx, ny), oracle.staggered_charges(nx, ny))
         assert np.array_equal(L.string_charges(nx, ny), oracle.string_charges(nx, ny))
+
+
+def test_basis_outlives_its_hamiltonians_any_destroy_order():
+    """Destroying the basis before a Hamiltonian made from it is allowed (the
+    basis is reference-counted in the library); needs no GPU to check the
+    symbol, the order itself is exercised by the GPU tests' garbage
+    collection."""
+    from lgt_gb300 import _capi as C
+    lib = C.load(build_if_missing=False)
+    assert hasattr(lib, "lgt_basis_destroy") and hasattr(lib, "lgt_ham_destroy")

@@ -38,3 +38,16 @@ def test_autotune_disabled_keeps_rules(lgt, monkeypatch):
     c = H.autotune(1, "fp64")
     assert not c["measured"] and c["hpsi_kernel"] == "rule" and c["reduce_blocks"] == 608
     H.close()
+
+
+def test_destroy_basis_before_hamiltonian(oracle, lgt):
+    """Handles may be released in any order: the basis stays alive while a
+    Hamiltonian made from it exists."""
+    gb = lgt.build_basis(3, 2, 1, lgt.staggered_charges(3, 2))[0]
+    H = lgt.build_hamiltonian(gb, g=1.0, t=1.0, m=0.5)
+    gb.close()  # the caller's basis handle goes first
+    E0, _ = lgt.find_ground_state(H, tol=1e-12)
+    ob = oracle.build_basis(3, 2, 1, oracle.staggered_charges(3, 2))
+    E0o = oracle.ground_state(oracle.build_hamiltonian(ob, g=1.0, t=1.0, m=0.5))[0]
+    assert abs(E0 - E0o) <= 1e-10 * abs(E0o)
+    H.close()
