@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "lgt_krylov.h"
+#include "lgt_tridiag.cuh"
 
 namespace lgt {
 
@@ -163,18 +164,28 @@ __global__ void __launch_bounds__(kT, LGT_MD_MINB) k_multidot(const S* __restric
   }
 }
 
-// h[i][k] = <V_i, W>_k (complex for NC = 2), summed over blocks in order.
-// alpha_j of active points accumulates Re h_j (first pass sets it).  With
-// self = 1 the extra dot (W against itself) goes to nb[k].
+// Sum over the per-block partials in a fixed order, one warp per output:
+// lane l adds blocks l, l + 32, ..., then a fixed shuffle tree.  (A single
+// thread walking all blocks waits on one dependent load and add per block.)
+__device__ __forceinline__ double warp_total(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// h[i][k] = <V_i, W>_k (complex for NC = 2).  alpha_j of active points
+// accumulates Re h_j (first pass sets it).  With self = 1 the extra dot (W
+// against itself) goes to nb[k].  One warp per (i, k); launch
+// finish_blocks(outputs) blocks of 128 threads.
 __global__ void k_finish_dots(const double* part, int nblk, int Jmax, const int* jstate,
                               int jfixed, int K, int C, int ncomp, double* h, double* alpha,
                               int ldT, int first_pass, const int* status, int self, double* nb) {
   const int J = jstate ? (*jstate + 1) : jfixed;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (t >= (J + self) * K) return;
   const int i = t / K, k = t - i * K;
   double re = 0.0, im = 0.0;
-  for (int b = 0; b < nblk; ++b) {
+  for (int b = lane; b < nblk; b += 32) {
     const double* p = part + (size_t(b) * Jmax + i) * 2 * C;
     if (ncomp == 1) {
       re += p[k];
@@ -183,6 +194,9 @@ __global__ void k_finish_dots(const double* part, int nblk, int Jmax, const int*
       im += p[C + 2 * k] - p[C + 2 * k + 1];
     }
   }
+  re = warp_total(re);
+  im = warp_total(im);
+  if (lane != 0) return;
   if (i == J) {  // self dot
     nb[k] = re;
     return;
@@ -194,6 +208,9 @@ __global__ void k_finish_dots(const double* part, int nblk, int Jmax, const int*
     *a = first_pass ? re : (*a + re);
   }
 }
+
+// Blocks of 128 threads (4 warps) for `outputs` warp-per-output finishers.
+inline unsigned finish_blocks(int outputs) { return unsigned((outputs + 3) / 4); }
 
 // W -= sum_{i<J} h_i V_i (complex product for NC = 2) for active points
 // (only those with need[k] != 0 when need is given), and per-block partial
@@ -276,30 +293,38 @@ __global__ void __launch_bounds__(kT) k_update(const S* __restrict__ V, size_t v
   }
 }
 
+// Sum over blocks of point k's partial norms (warp per point, fixed order).
+__device__ __forceinline__ double point_norm2(const double* npart, int nblk, int C, int ncomp,
+                                              int k, int lane) {
+  double s = 0.0;
+  for (int b = lane; b < nblk; b += 32)
+    for (int q = 0; q < ncomp; ++q) s += npart[size_t(b) * C + k * ncomp + q];
+  return warp_total(s);
+}
+
 // After a Gram-Schmidt pass: a further pass is needed for point k only when
 // the pass cancelled more than two digits, ||W_after||^2 < 1e-4 ||W_before||^2.
+// One warp per point.
 __global__ void k_need_pass(const double* npart, int nblk, int K, int C, int ncomp,
                             const int* status, double* nb, int* need) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (k >= K) return;
-  double s = 0.0;
-  for (int b = 0; b < nblk; ++b)
-    for (int q = 0; q < ncomp; ++q) s += npart[size_t(b) * C + k * ncomp + q];
+  const double s = point_norm2(npart, nblk, C, ncomp, k, lane);
+  if (lane != 0) return;
   need[k] = (status[k] == kActive && s < 1e-4 * nb[k]) ? 1 : 0;
   nb[k] = s;
 }
 
 // beta_j = ||W|| per point.  A Krylov space that has become invariant
 // (beta below the relative threshold) marks the point exhausted: its Ritz
-// pair on the current basis is exact.
+// pair on the current basis is exact.  One warp per point.
 __global__ void k_finish_norm(const double* npart, int nblk, int K, int C, int ncomp,
                               const int* jstate, double* beta, const double* alpha, int ldT,
                               int* status, int* len, double* bnorm, double tiny_rel, int write_beta) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (k >= K) return;
-  double s = 0.0;
-  for (int b = 0; b < nblk; ++b)
-    for (int q = 0; q < ncomp; ++q) s += npart[size_t(b) * C + k * ncomp + q];
+  const double s = point_norm2(npart, nblk, C, ncomp, k, lane);
+  if (lane != 0) return;
   const double nb = sqrt(s);
   bnorm[k] = nb;
   if (!write_beta || status[k] != kActive) return;
@@ -347,89 +372,38 @@ __global__ void k_set_int(int* p, int n, int v, const int* status, int only_stat
 
 // ---- tridiagonal solvers -----------------------------------------------------
 
-// Number of eigenvalues of T (diag a, off-diag b) below x (Sturm sequence).
-__device__ int sturm_count(const double* a, const double* b, int n, double x) {
-  int cnt = 0;
-  double q = 1.0;
-  for (int i = 0; i < n; ++i) {
-    const double bb = (i > 0) ? b[i - 1] * b[i - 1] : 0.0;
-    q = (a[i] - x) - ((i > 0) ? bb / q : 0.0);
-    if (q == 0.0) q = -1e-300;
-    if (q < 0.0) ++cnt;
-  }
-  return cnt;
-}
-
-// Lowest eigenpair of the n x n tridiagonal T: bisection on the Sturm count,
-// then inverse iteration on the positive-definite T - (theta - delta) I
-// (LDL^T without pivoting is stable there).  z normalised, z[0] >= 0.
-__device__ double lowest_eigpair(const double* a, const double* b, int n, double* z,
-                                 double* work) {
-  double lo = a[0], hi = a[0];
-  for (int i = 0; i < n; ++i) {
-    const double r = ((i > 0) ? fabs(b[i - 1]) : 0.0) + ((i < n - 1) ? fabs(b[i]) : 0.0);
-    lo = fmin(lo, a[i] - r);
-    hi = fmax(hi, a[i] + r);
-  }
-  const double scale = fmax(fmax(fabs(lo), fabs(hi)), 1e-300);
-  for (int it = 0; it < 200; ++it) {
-    const double mid = 0.5 * (lo + hi);
-    if (mid <= lo || mid >= hi) break;
-    if (sturm_count(a, b, n, mid) >= 1) hi = mid; else lo = mid;
-    if (hi - lo <= 2.2e-16 * scale) break;
-  }
-  const double theta = 0.5 * (lo + hi);
-  const double shift = theta - 4.0 * 2.2e-16 * scale;
-  for (int i = 0; i < n; ++i) z[i] = 1.0;
-  for (int rep = 0; rep < 3; ++rep) {
-    // LDL^T of T - shift I: d (work), l (work + n)
-    double* d = work;
-    double* l = work + kMaxDim;
-    d[0] = a[0] - shift;
-    if (d[0] <= 0.0) d[0] = 1e-300;
-    for (int i = 1; i < n; ++i) {
-      l[i - 1] = b[i - 1] / d[i - 1];
-      d[i] = (a[i] - shift) - l[i - 1] * b[i - 1];
-      if (d[i] <= 0.0) d[i] = 1e-300;
-    }
-    // solve L y = z, D w = y, L^T x = w
-    for (int i = 1; i < n; ++i) z[i] -= l[i - 1] * z[i - 1];
-    for (int i = 0; i < n; ++i) z[i] /= d[i];
-    for (int i = n - 2; i >= 0; --i) z[i] -= l[i] * z[i + 1];
-    double nn = 0.0, mx = 0.0;
-    for (int i = 0; i < n; ++i) mx = fmax(mx, fabs(z[i]));
-    for (int i = 0; i < n; ++i) {
-      z[i] /= mx;
-      nn += z[i] * z[i];
-    }
-    nn = sqrt(nn);
-    for (int i = 0; i < n; ++i) z[i] /= nn;
-  }
-  if (z[0] < 0.0)
-    for (int i = 0; i < n; ++i) z[i] = -z[i];
-  return theta;
-}
-
-// Ground-state convergence check, one block (thread 0) per point:
+// Ground-state convergence check, one warp per point:
 // Ritz value theta, residual beta_{n-1} |z_{n-1}|, coefficients z.
 __global__ void k_check_lowest(const double* alpha, const double* beta, int ldT, int* status,
                                const int* len, double* theta, double* resid, double* coef,
-                               double tol) {
-  const int k = blockIdx.x;
-  if (threadIdx.x != 0) return;
+                               double tol, int fp32) {
+  // one warp per point: warp multisection of the Sturm count (FP32 for the
+  // mixed path, whose basis resolves no more), bracket warm-started from
+  // this point's previous theta and residual (verified by Sturm counts, so
+  // stale values only cost the fallback to the Gershgorin interval)
+  __shared__ double s_a[kMaxDim], s_b[kMaxDim], s_z[kMaxDim], s_work[3 * kMaxDim];
+  const int k = blockIdx.x, lane = threadIdx.x;
   const int st = status[k];
   if (st >= kConverged) return;
   const int n = len[k];
-  double z[kMaxDim], work[2 * kMaxDim];
   if (n <= 0) return;
-  const double th = lowest_eigpair(alpha + size_t(k) * ldT, beta + size_t(k) * ldT, n, z, work);
-  const double r = fabs(beta[size_t(k) * ldT + n - 1] * z[n - 1]);
-  theta[k] = th;
-  resid[k] = (st == kExhausted) ? 0.0 : r;
-  for (int i = 0; i < ldT; ++i) {
-    coef[(size_t(k) * ldT + i) * 2 + 0] = (i < n) ? z[i] : 0.0;
+  for (int i = lane; i < n; i += 32) {
+    s_a[i] = alpha[size_t(k) * ldT + i];
+    s_b[i] = (i < n - 1) ? beta[size_t(k) * ldT + i] : 0.0;
+  }
+  __syncwarp();
+  const double tp = theta[k], rp = resid[k];
+  const bool warm = isfinite(tp) && isfinite(rp);
+  const double th = fp32 ? warp_lowest_eig_f32(s_a, s_b, n, s_z, s_work, warm, false, tp, rp)
+                         : warp_lowest_eig(s_a, s_b, n, s_z, s_work, warm, false, tp, rp);
+  const double r = fabs(beta[size_t(k) * ldT + n - 1] * s_z[n - 1]);
+  for (int i = lane; i < ldT; i += 32) {
+    coef[(size_t(k) * ldT + i) * 2 + 0] = (i < n) ? s_z[i] : 0.0;
     coef[(size_t(k) * ldT + i) * 2 + 1] = 0.0;
   }
+  if (lane != 0) return;
+  theta[k] = th;
+  resid[k] = (st == kExhausted) ? 0.0 : r;
   if (st == kExhausted || r <= tol) status[k] = kConverged;
 }
 
@@ -909,7 +883,7 @@ cudaError_t lanczos_step(const OpDev& op, Work<S>& w, int reorth, double tiny_re
                          cudaStream_t s) {
   cudaError_t e = apply_h<S>(op, w.V, w.jstate, w.vstride, w.W, w.hcomp, s);
   if (e != cudaSuccess) return e;
-  const int fdb = (w.ldT * w.K + 127) / 128;
+  const unsigned fdb = finish_blocks(w.ldT * w.K);
   // Classical Gram-Schmidt against the whole basis (this also performs the
   // three-term recurrence).  Further passes, up to `reorth`, act only on the
   // points whose previous pass cancelled more than two digits
@@ -918,7 +892,7 @@ cudaError_t lanczos_step(const OpDev& op, Work<S>& w, int reorth, double tiny_re
   for (int pass = 0; pass < reorth; ++pass) {
     const int* need = (pass == 0) ? nullptr : w.need;
     if (pass > 0)
-      k_need_pass<<<(w.K + 63) / 64, 64, 0, s>>>(w.npart, w.red.nblk, w.K, w.C, w.ncomp,
+      k_need_pass<<<finish_blocks(w.K), 128, 0, s>>>(w.npart, w.red.nblk, w.K, w.C, w.ncomp,
                                                  w.status, w.nb, w.need), lgt::note_launch();
     e = launch_multidot<S, S>(w, w.V, w.vstride, w.jstate, 0, w.W, s, pass == 0 ? 1 : 0, need);
     if (e != cudaSuccess) return e;
@@ -928,7 +902,7 @@ cudaError_t lanczos_step(const OpDev& op, Work<S>& w, int reorth, double tiny_re
     e = launch_update<S>(w, w.W, s, need);
     if (e != cudaSuccess) return e;
   }
-  k_finish_norm<<<(w.K + 63) / 64, 64, 0, s>>>(w.npart, w.red.nblk, w.K, w.C, w.ncomp, w.jstate,
+  k_finish_norm<<<finish_blocks(w.K), 128, 0, s>>>(w.npart, w.red.nblk, w.K, w.C, w.ncomp, w.jstate,
                                                w.beta, w.alpha, w.ldT, w.status, w.len, w.bnorm,
                                                tiny_rel, 1), lgt::note_launch();
   k_scale<S, S><<<grid_for(int64_t(w.vstride)), kT, 0, s>>>(w.W, w.V, w.vstride, w.jstate, 1, w.N,
@@ -944,7 +918,7 @@ std::string colnorms_double(Work<S>& w, const double* X, double* out_norm, cudaS
   k_residual_parts<<<w.red.nblk, kT, 0, s>>>(X, X, w.zeros, w.N, w.C, w.ncomp, w.red.rpb,
                                              w.npart), lgt::note_launch();
   KCK(cudaGetLastError());
-  k_finish_norm<<<(w.K + 63) / 64, 64, 0, s>>>(w.npart, w.red.nblk, w.K, w.C, w.ncomp, w.jstate,
+  k_finish_norm<<<finish_blocks(w.K), 128, 0, s>>>(w.npart, w.red.nblk, w.K, w.C, w.ncomp, w.jstate,
                                                w.beta, w.alpha, w.ldT, w.status, w.len, out_norm,
                                                0.0, 0), lgt::note_launch();
   KCK(cudaGetLastError());
@@ -956,7 +930,7 @@ template <typename S>
 std::string dots_ws(Work<S>& w, const double* x, const double* y, double* out_host,
                     cudaStream_t s) {
   KCK((launch_multidot<S, double>(w, x, 0, nullptr, 1, y, s)));
-  k_finish_dots<<<(w.K + 127) / 128, 128, 0, s>>>(w.part, w.red.nblk, w.ldT, nullptr, 1, w.K, w.C,
+  k_finish_dots<<<finish_blocks(w.K), 128, 0, s>>>(w.part, w.red.nblk, w.ldT, nullptr, 1, w.K, w.C,
                                                   w.ncomp, w.h, nullptr, 0, 0, nullptr, 0,
                                                   nullptr), lgt::note_launch();
   KCK(cudaGetLastError());
@@ -1281,6 +1255,7 @@ std::string ground_state_impl(const OpDev& op_in, const KrylovParams& p, Work<S>
   KCK(cudaMemsetAsync(w.status, 0, sizeof(int) * K, s));
   KCK(cudaMemsetAsync(w.len, 0, sizeof(int) * K, s));
   KCK(cudaMemsetAsync(w.fail, 0, sizeof(int), s));
+  KCK(cudaMemsetAsync(w.theta, 0xff, sizeof(double) * K, s));  // NaN: no warm bracket yet
   if (!p.start_given) {
     k_randn<double><<<grid_for(N * C), kT, 0, s>>>(X, N, C, ncomp, p.seed), lgt::note_launch();
     KCK(cudaGetLastError());
@@ -1300,7 +1275,7 @@ std::string ground_state_impl(const OpDev& op_in, const KrylovParams& p, Work<S>
     if (!err.empty()) return err;
     j += steps;
     k_check_lowest<<<K, 32, 0, s>>>(w.alpha, w.beta, w.ldT, w.status, w.len, w.theta, w.resid,
-                                    w.coef, tol_inner), lgt::note_launch();
+                                    w.coef, tol_inner, fp32 ? 1 : 0), lgt::note_launch();
     KCK(cudaGetLastError());
     KCK(cudaMemcpyAsync(st.data(), w.status, sizeof(int) * K, cudaMemcpyDeviceToHost, s));
     KCK(cudaStreamSynchronize(s));
@@ -1351,7 +1326,7 @@ std::string ground_state_impl(const OpDev& op_in, const KrylovParams& p, Work<S>
   if (!err.empty()) return err;
   KCK(cudaMemcpyAsync(w.theta, erq.data(), sizeof(double) * K, cudaMemcpyHostToDevice, s));
   k_residual_parts<<<w.red.nblk, kT, 0, s>>>(X, w.R, w.theta, N, C, ncomp, w.red.rpb, w.npart), lgt::note_launch();
-  k_finish_norm<<<(K + 63) / 64, 64, 0, s>>>(w.npart, w.red.nblk, K, C, ncomp, w.jstate, w.beta,
+  k_finish_norm<<<finish_blocks(K), 128, 0, s>>>(w.npart, w.red.nblk, K, C, ncomp, w.jstate, w.beta,
                                              w.alpha, w.ldT, w.status, w.len, w.bnorm, 0.0, 0), lgt::note_launch();
   KCK(cudaGetLastError());
   KCK(cudaMemcpyAsync(r2.data(), w.bnorm, sizeof(double) * K, cudaMemcpyDeviceToHost, s));
@@ -1496,7 +1471,7 @@ std::string expm_impl(const OpDev& op_in, const KrylovParams& p, Work<S>& w, dou
     // panel, K complex columns
     k_residual_parts<<<w.red.nblk, kT, 0, s>>>(X, X, w.zeros, N, C, 2, w.red.rpb,
                                                w.npart), lgt::note_launch();
-    k_finish_norm<<<(K + 63) / 64, 64, 0, s>>>(w.npart, w.red.nblk, K, C, 2, w.jstate, w.beta,
+    k_finish_norm<<<finish_blocks(K), 128, 0, s>>>(w.npart, w.red.nblk, K, C, 2, w.jstate, w.beta,
                                                w.alpha, w.ldT, w.status, w.len, w.rho, 0.0,
                                                0), lgt::note_launch();
     k_scale<double, double><<<grid_for(N * C), kT, 0, s>>>(X, X, 0, nullptr, 0, N, C, 2, w.rho,
