@@ -148,6 +148,22 @@ function nnz(H::Hamiltonian)
     return Int(n[])
 end
 
+"Autotuner report for H's Krylov panels (ncomp 1: ground states, 2: exp steps); tunes on first use."
+struct Tuning
+    hpsi_kernel::Int32
+    reduce_blocks::Int32
+    hpsi_ms::Float64
+    reduce_ms::Float64
+    measured::Int32
+end
+
+function autotune(H::Hamiltonian; ncomp::Integer=1, precision::Int32=LGT_FP64)
+    t = Ref{Tuning}()
+    check(ccall((:lgt_autotune, libpath), Int32, (Ptr{Cvoid}, Int32, Int32, Ref{Tuning}),
+                H.ptr, Int32(ncomp), precision, t))
+    return t[]
+end
+
 # ── find_ground_state (finite_ed.jl:333-341) ────────────────────────────────
 function find_ground_state(H::Hamiltonian; tol=1e-10, krylovdim=50, maxiter=300,
                            precision::Int32=LGT_FP64, seed::Integer=0)
