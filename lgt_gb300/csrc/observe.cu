@@ -128,13 +128,20 @@ __global__ void __launch_bounds__(kT) k_observe(Geom G, RankView R, const T* __r
   }
 }
 
+// Sum of the per-block partials, one warp per output (lane l adds blocks
+// l, l + 32, ..., then a fixed shuffle tree): a fixed order, and no single
+// thread waiting on one dependent load per block.
 __global__ void k_observe_finish(const double* part, int nblk, int K, int nfeat, double* out) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (t >= K * nfeat) return;
   double s = 0.0;
-  for (int b = 0; b < nblk; ++b) s += part[size_t(b) * K * nfeat + t];
-  out[t] = s;
+  for (int b = lane; b < nblk; b += 32) s += part[size_t(b) * K * nfeat + t];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) out[t] = s;
 }
+
+inline unsigned finish_blocks(int outputs) { return unsigned((outputs + 3) / 4); }  // 4 warps
 
 template <typename T, int NC, int MAXF>
 cudaError_t launch_obs3(const Geom& G, const RankView& R, const T* x, int K, int nfeat, int nblk,
@@ -166,9 +173,10 @@ cudaError_t launch_obs2(const Geom& G, const RankView& R, const T* x, int K, int
 int observe_nfeat(const Geom& G) { return 2 * G.ns + G.nP + 1; }
 
 void observe_plan(int64_t N, int* nblk, int64_t* rpb) {
-  // about 64 rows per block for small sectors (so a K = 64 batch of N = 645
-  // spreads over ten blocks), at most four blocks per SM
-  int64_t want = (N + 63) / 64;
+  // at least 4 rows per block (a K = 64 batch of N = 645 spreads over 162
+  // blocks: the per-row FP64 feature sums are the work), at most four
+  // blocks per SM
+  int64_t want = (N + 3) / 4;
   if (want > 152 * 4) want = 152 * 4;
   if (want < 1) want = 1;
   int64_t r = (N + want - 1) / want;
@@ -190,7 +198,7 @@ cudaError_t launch_observe(const Geom& G, const RankView& R, const T* x, int K, 
                       ? launch_obs2<T, 1>(G, R, x, K, nfeat, nblk, rpb, part, err, s)
                       : launch_obs2<T, 2>(G, R, x, K, nfeat, nblk, rpb, part, err, s);
   if (e != cudaSuccess) return e;
-  k_observe_finish<<<(K * nfeat + 127) / 128, 128, 0, s>>>(part, nblk, K, nfeat, out), lgt::note_launch();
+  k_observe_finish<<<finish_blocks(K * nfeat), 128, 0, s>>>(part, nblk, K, nfeat, out), lgt::note_launch();
   return cudaGetLastError();
 }
 
@@ -205,7 +213,7 @@ cudaError_t launch_observe_planned(const Geom& G, const RankView& R, const T* x,
                       ? launch_obs2<T, 1>(G, R, x, K, nfeat, nblk, rpb, part, err, s)
                       : launch_obs2<T, 2>(G, R, x, K, nfeat, nblk, rpb, part, err, s);
   if (e != cudaSuccess) return e;
-  k_observe_finish<<<(K * nfeat + 127) / 128, 128, 0, s>>>(part, nblk, K, nfeat, out), lgt::note_launch();
+  k_observe_finish<<<finish_blocks(K * nfeat), 128, 0, s>>>(part, nblk, K, nfeat, out), lgt::note_launch();
   return cudaGetLastError();
 }
 
