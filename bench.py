@@ -663,6 +663,9 @@ def main():
                      "traffic_note": "ncu DRAM bytes per launch; 3.0x the algorithmic bytes: "
                                      "neighbour gathers re-read x from HBM (LRU model of a "
                                      "100 MB L2: 4.4 misses per row)",
+                     "dram_gbs_of_traffic": RF_TRAFFIC_BYTES / (dom["ms"] * 1e-3) / 1e9,
+                     "dram_frac_of_traffic": RF_TRAFFIC_BYTES / (dom["ms"] * 1e-3) / 1e9
+                     / rf["peak"],
                      "peak_source": rf["peak_src"] + " (MEASURED_PEAKS.json hbm_gbs)",
                      "algo_bytes_per_launch": dom["algo_bytes"], "ms_per_launch": dom["ms"],
                      "variants": {k: v for k, v in rf.items() if isinstance(v, dict)}},
