@@ -10,12 +10,15 @@
 //        h = V_{0..j}^H W                 whole basis, FP64 accumulation)
 //        W -= V_{0..j} h,  alpha_j += Re h_j
 //     beta_j = ||W||,  V_{j+1} = W / beta_j
-// Every reduction is two-stage (per-block partials, then a fixed-order sum),
-// so results are bitwise reproducible.  All kernels read the step index j
-// from device memory, so the step sequence is captured once as a CUDA graph
-// and replayed.  The tridiagonal problems are solved on the device: lowest
-// eigenpair by Sturm bisection + inverse iteration (ground state), full
-// eigendecomposition by implicit QL (exponential).
+// (a further pass runs only for points whose pass cancelled more than two
+// digits).  Every reduction is two-stage (per-block partials, then a
+// fixed-order warp-parallel sum), so results are bitwise reproducible.  All
+// kernels read the step index j from device memory, so the step sequence is
+// captured once as a CUDA graph and replayed.  The tridiagonal problems are
+// solved on the device: lowest eigenpair by warp multisection of the Sturm
+// count + inverse iteration (ground state, lgt_tridiag.cuh), full
+// eigendecomposition by implicit QL (exponential, which runs the real and
+// imaginary parts of each point as two real Krylov columns).
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>

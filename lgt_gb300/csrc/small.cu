@@ -3,13 +3,15 @@
 //
 // For sectors up to kSmallMaxN states the step latency of the panel path
 // (about ten dependent kernels per Lanczos step) dominates, so here every
-// (problem, point) unit is one 512-thread CTA that keeps the current Lanczos
-// residual in registers (row r of thread t: r = t + i*512) and the Krylov
-// basis in global memory (L2-resident), and runs matvec, classical
-// Gram-Schmidt twice against the whole basis (FP64 accumulation), the
-// tridiagonal check, restarts and the FP64 finish without leaving the
-// kernel.  Units of different sectors and sizes share one launch (uneven
-// batch); the largest are scheduled first.
+// (problem, point) unit is one CTA of just enough warps for R rows per
+// thread (at most 512 threads) that keeps the current Lanczos residual in
+// registers (row r of thread t: r = t + i * blockDim) and the Krylov basis
+// in global memory (L2-resident), and runs matvec, classical Gram-Schmidt
+// against the whole basis (FP64 accumulation, warp reduce-scatter; a second
+// pass only on cancellation), the tridiagonal check (lgt_tridiag.cuh),
+// restarts and the FP64 finish without leaving the kernel.  Units of
+// different sectors and sizes share one launch (uneven batch); the largest
+// are scheduled first.
 //
 // The neighbour ranks of a lattice are computed once by a device "lookup
 // pass" (k_pattern_*: the move enumeration and rank of the H*psi kernel)
