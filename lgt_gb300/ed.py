@@ -492,12 +492,21 @@ def ite_ground_state_ED(states, key_dict, nx, ny, dg, *, g, t, m, model="ref", *
         H.close()
 
 
-def _obs_dict(basis, grid_nf, grid_e2, grid_pl, s):
+_OBS_FIELDS = ("t", "nf_mean", "nf_even", "nf_odd", "E2_mean", "plaq_mean", "n_stag", "norm2")
+
+
+def _obs_dicts(basis, K, nf, e2, pl, summ):
+    """All K measurement dicts at once: grids as [nx, ny] views of one
+    transposed array per observable, summaries through a numpy view of the
+    lgt_obs array (no per-field ctypes access)."""
     nx, ny = basis.nx, basis.ny
-    return dict(t=s.t, nf_mean=s.nf_mean, nf_even=s.nf_even, nf_odd=s.nf_odd, E2_mean=s.E2_mean,
-                nf_grid=grid_nf.reshape(ny, nx).T.copy(), E2_grid=grid_e2.reshape(ny, nx).T.copy(),
-                plaq_grid=grid_pl.reshape(max(ny - 1, 0), max(nx - 1, 0)).T.copy(),
-                plaq_mean=s.plaq_mean, n_stag=s.n_stag, norm2=s.norm2)
+    nf_g = nf.reshape(K, ny, nx).transpose(0, 2, 1).copy()
+    e2_g = e2.reshape(K, ny, nx).transpose(0, 2, 1).copy()
+    pnx, pny = max(nx - 1, 0), max(ny - 1, 0)
+    pl_g = pl[:K * pnx * pny].reshape(K, pny, pnx).transpose(0, 2, 1).copy()
+    sm = np.frombuffer(summ, dtype=np.float64).reshape(K, len(_OBS_FIELDS)).tolist()
+    return [dict(zip(_OBS_FIELDS, sm[k]), nf_grid=nf_g[k], E2_grid=e2_g[k], plaq_grid=pl_g[k])
+            for k in range(K)]
 
 
 def measure_ED(psi, states: Basis, nx=None, ny=None, dg=None, t_now: float = 0.0):
@@ -517,8 +526,7 @@ def measure_ED(psi, states: Basis, nx=None, ny=None, dg=None, t_now: float = 0.0
     summ = (C.Obs * K)()
     C.check(C.load().lgt_observe(obs.handle, _p(px), nc, C.LGT_FP64, 0, float(t_now), _p(nf),
                                  _p(e2), _p(pl), summ))
-    out = [_obs_dict(b, nf[k * ns:(k + 1) * ns], e2[k * ns:(k + 1) * ns],
-                     pl[k * npl:(k + 1) * npl], summ[k]) for k in range(K)]
+    out = _obs_dicts(b, K, nf, e2, pl, summ)
     return out[0] if psi.ndim == 1 else out
 
 
