@@ -9,6 +9,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/lgt_ed.h"
@@ -657,32 +658,63 @@ lgt_status lgt_ground_state_batch(int32_t nham, lgt_ham* const* hams, const lgt_
   lgt_info tot;
   std::memset(&tot, 0, sizeof(tot));
   lgt_status worst = LGT_OK;
-  if (!small.empty()) {
-    std::vector<std::vector<double>> rbuf(small.size());
-    std::vector<double*> rp(small.size());
-    for (size_t i = 0; i < small.size(); ++i) {
-      rbuf[i].resize(small[i]->K);
-      rp[i] = rs[i] ? rs[i] : rbuf[i].data();
-    }
-    lgt_info one;
-    std::memset(&one, 0, sizeof(one));
-    lgt_status rc = cta_solve(small, p, xs, e0s.data(), rp.data(), &one);
-    if (rc != LGT_OK && rc != LGT_ERR_NOCONV) return rc;
-    if (rc) worst = rc;
-    tot = one;
+  // The one-CTA-per-point launch of the small sectors runs on its own host
+  // thread (and its basis' stream) while the large sectors' panel solves
+  // run here, so the two overlap on the GPU.
+  std::vector<std::vector<double>> rbuf(small.size());
+  std::vector<double*> rp(small.size());
+  for (size_t i = 0; i < small.size(); ++i) {
+    rbuf[i].resize(small[i]->K);
+    rp[i] = rs[i] ? rs[i] : rbuf[i].data();
   }
+  lgt_info small_info;
+  std::memset(&small_info, 0, sizeof(small_info));
+  lgt_status small_rc = LGT_OK;
+  std::string small_err;
+  auto run_small = [&]() {
+    if (set_device(small[0]->b) != LGT_OK) {
+      small_rc = LGT_ERR_CUDA;
+      small_err = lgt_last_error();
+      return;
+    }
+    small_rc = cta_solve(small, p, xs, e0s.data(), rp.data(), &small_info);
+    if (small_rc != LGT_OK) small_err = lgt_last_error();
+  };
+  std::thread small_thread;
+  if (!small.empty()) {
+    if (large.empty())
+      run_small();
+    else
+      small_thread = std::thread(run_small);
+  }
+  lgt_status large_rc = LGT_OK;
   for (int i : large) {
     lgt_info one;
     std::memset(&one, 0, sizeof(one));
     lgt_status rc = lgt_ground_state(hams[i], opts, E0[i], psi ? psi[i] : nullptr,
                                      residual ? residual[i] : nullptr, flags, &one);
-    if (rc != LGT_OK && rc != LGT_ERR_NOCONV) return rc;
+    if (rc != LGT_OK && rc != LGT_ERR_NOCONV) {
+      large_rc = rc;
+      break;
+    }
     if (rc) worst = rc;
     tot.matvecs = std::max(tot.matvecs, one.matvecs);
     tot.restarts = std::max(tot.restarts, one.restarts);
     tot.converged += one.converged;
     tot.max_residual = std::max(tot.max_residual, one.max_residual);
     tot.seconds += one.seconds;
+  }
+  const std::string large_err = large_rc ? std::string(lgt_last_error()) : std::string();
+  if (small_thread.joinable()) small_thread.join();
+  if (small_rc != LGT_OK && small_rc != LGT_ERR_NOCONV) return fail(small_rc, small_err);
+  if (large_rc) return fail(large_rc, large_err);
+  if (small_rc) worst = small_rc;
+  if (!small.empty()) {
+    tot.matvecs = std::max(tot.matvecs, small_info.matvecs);
+    tot.restarts = std::max(tot.restarts, small_info.restarts);
+    tot.converged += small_info.converged;
+    tot.max_residual = std::max(tot.max_residual, small_info.max_residual);
+    tot.seconds = std::max(tot.seconds, small_info.seconds);
   }
   if (info) *info = tot;
   if (worst) return fail(worst, "NOCONV: some points did not converge within maxiter restarts");
