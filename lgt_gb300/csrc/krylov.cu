@@ -90,10 +90,13 @@ __global__ void k_randn(S* out, int64_t N, int C, int ncomp, uint64_t seed) {
 #define LGT_UPD_HOIST 0
 #endif
 #ifndef LGT_MD_MINB
-#define LGT_MD_MINB 4  // resident blocks per SM the dot kernel's registers must allow
+#define LGT_MD_MINB 4  // resident blocks per SM the dot kernel's registers must allow (FP64)
+#endif
+#ifndef LGT_MD_MINB_F32
+#define LGT_MD_MINB_F32 5  // the same for FP32 panels (measured: 5 beats 4 and 6)
 #endif
 template <typename S, int NC>
-__global__ void __launch_bounds__(kT, LGT_MD_MINB) k_multidot(const S* __restrict__ V, size_t vstride,
+__global__ void __launch_bounds__(kT, sizeof(S) == 4 ? LGT_MD_MINB_F32 : LGT_MD_MINB) k_multidot(const S* __restrict__ V, size_t vstride,
                                                  const int* jstate, int jfixed,
                                                  const S* __restrict__ W, int64_t N, int C,
                                                  int64_t rpb, double* part, int Jmax,

@@ -406,14 +406,29 @@ __global__ void __launch_bounds__(kThreads, PLAQ ? LGT_FIXED_MINB_PLAQ : LGT_FIX
           for (int e = 0; e < W; ++e) ap[e] += xs[u][e];
       }
     }
-#pragma unroll
-    for (int e = 0; e < W; ++e) {
-      const int col = col0 + e;
-      const int k = (ncomp == 2) ? (col >> 1) : col;
-      const T cd = s_coef[k] * e2 + s_coef[K + k] * stag;  // (g^2/2) e2 + m stag
+    // y = (cE e2 + cm stag) x + ch * hops (+ cp * plaquettes); the diagonal
+    // coefficient once per point (the re and im columns of a complex point
+    // share it; W and col0 are even)
+    auto finish = [&](int e, int k, T cd) {
       T v = fma(s_coef[2 * K + k], ah[e], cd * xd[e]);
       if (PLAQ) v = fma(s_coef[3 * K + k], ap[e], v);
       xd[e] = v;
+    };
+    if (ncomp == 2 && (W % 2) == 0) {
+#pragma unroll
+      for (int e = 0; e < W; e += 2) {
+        const int k = (col0 + e) >> 1;
+        const T cd = s_coef[k] * e2 + s_coef[K + k] * stag;  // (g^2/2) e2 + m stag
+        finish(e, k, cd);
+        finish(e + 1, k, cd);
+      }
+    } else {
+#pragma unroll
+      for (int e = 0; e < W; ++e) {
+        const int col = col0 + e;
+        const int k = (ncomp == 2) ? (col >> 1) : col;
+        finish(e, k, s_coef[k] * e2 + s_coef[K + k] * stag);
+      }
     }
     st_slice<T, V, LD>(y + size_t(row) * C + col0, xd);
   }
