@@ -42,7 +42,7 @@ G_LO, G_HI, T_HOP, MASS = 0.5, 2.0, 1.0, 0.5
 RF_NX, RF_NY, RF_K = 4, 4, 8          # roofline panel (4x4 quench, K = 8 complex)
 # DRAM bytes of one such launch (FP32, reference model), measured by ncu
 # (dram__bytes_read.sum + dram__bytes_write.sum, --set full, one launch)
-RF_TRAFFIC_BYTES = int((2.904194 + 0.533047) * 1e9)
+RF_TRAFFIC_BYTES = int((2.903165 + 0.533069) * 1e9)
 L2_FLUSH_BYTES = 512 << 20            # > 129 MB L2
 METRIC = "ground states/s, batched FP32-mixed Lanczos at |dE|/|E|<=1e-10"
 
