@@ -351,8 +351,7 @@ def quench(L, C, lib, torch, stream, dev, n_steps=5):
                      "max_rel_energy_drift": float(np.max(np.abs(e_after - e_before) /
                                                          np.abs(e_before))),
                      "E2_mean_t_end_point0": obs[n_steps * RF_K].E2_mean,
-                     "autotune": {"hpsi_kernel": ["rule", "generic", "fixed_vpl1",
-                                                  "fixed_vpl2", "fixed_wide"][tune.hpsi_kernel],
+                     "autotune": {"hpsi_kernel": L.HPSI_KERNELS[tune.hpsi_kernel],
                                   "reduce_blocks": tune.reduce_blocks,
                                   "measured": bool(tune.measured)}}
         del psi
@@ -520,8 +519,7 @@ def roofline(L, C, lib, torch, stream, dev, reps=10):
             if not generic:  # the autotuner's kernel for this shape (chosen at the first call)
                 tune = C.Tuning()
                 C.check(lib.lgt_autotune(H.handle, 2, code, ctypes_byref(tune)))
-                row["kernel"] = ["rule", "generic", "fixed_vpl1", "fixed_vpl2",
-                                 "fixed_wide"][tune.hpsi_kernel]
+                row["kernel"] = L.HPSI_KERNELS[tune.hpsi_kernel]
             out["%s_%s%s" % (model, prec, "_generic" if generic else "")] = row
             del x, y
         H.close()

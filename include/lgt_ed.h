@@ -271,16 +271,22 @@ LGT_API lgt_status lgt_energy(const lgt_ham* h, const void* psi, int32_t ncomp, 
 /* Autotuner report (no counterpart in the reference).  The Krylov drivers
    time their kernel candidates at the first solve of each operator shape
    (lattice, model, storage precision, panel width) and keep the fastest for
-   the process: the H*psi kernel (run-time geometry, or the fixed-shape
-   kernel with one of its load modes; lgt_matvec uses and, on its first call
-   for a shape, makes the same choice) and the block count of the
-   Gram-Schmidt reductions.  LGT_AUTOTUNE=0 in the environment keeps the
-   built-in rules; LGT_HPSI_VARIANT=1..4 forces one H*psi kernel (the
-   hpsi_kernel codes below) for cross-checks. */
+   the process: the H*psi kernel (run-time geometry, the fixed-shape kernel
+   or the stored-neighbour-table kernel, each with its load modes;
+   lgt_matvec uses and, on its first call for a shape, makes the same
+   choice) and the block count of the Gram-Schmidt reductions.  The table
+   kernel reads the neighbour ranks of every row from a table built once per
+   Hamiltonian (4 bytes per off-diagonal entry and per row; no matrix values)
+   when its size bound fits min(free device memory / 4, LGT_NBR_TABLE_MB,
+   default 16384 MB); LGT_NBR_TABLE=0 disables it.  LGT_AUTOTUNE=0 in the
+   environment keeps the built-in rules; LGT_HPSI_VARIANT=1..7 forces one
+   H*psi kernel (the hpsi_kernel codes below) for cross-checks. */
 typedef struct lgt_tuning {
   int32_t hpsi_kernel;    /* 0 built-in rule, 1 run-time geometry, fixed
                              shape with 2 one / 3 two 16-byte vectors per
-                             lane, 4 two vectors as one 32-byte access      */
+                             lane, 4 two vectors as one 32-byte access;
+                             5, 6, 7 the same load modes from the stored
+                             neighbour table                                */
   int32_t reduce_blocks;  /* block-count cap of the panel reductions         */
   double hpsi_ms;         /* one H*psi with the chosen kernel                */
   double reduce_ms;       /* one 8-vector Gram-Schmidt pass, chosen blocks   */

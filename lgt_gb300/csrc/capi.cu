@@ -936,6 +936,7 @@ void lgt_ham_destroy(lgt_ham* h) {
   h->part.release();
   h->out.release();
   free_pattern(&h->pattern);
+  free_nbr_table(&h->table);
   cudaFree(h->small.base);
   cudaFree(h->coef_d);
   cudaFree(h->coef_f);

@@ -109,10 +109,13 @@ __global__ void __launch_bounds__(kT, sizeof(S) == 4 ? LGT_MD_MINB_F32 : LGT_MD_
   const bool act = rg < RG && (!need || need[c / ncomp] != 0);
   const int64_t r0 = int64_t(blockIdx.x) * rpb;
   const int64_t r1 = (r0 + rpb < N) ? r0 + rpb : N;
+  constexpr int kB = (NC == 2) ? kIC : 1;  // imaginary parts (complex panels only)
   for (int i0 = 0; i0 < J; i0 += kIC) {
-    double a[kIC], b[kIC];
+    double a[kIC], b[kB];
 #pragma unroll
-    for (int q = 0; q < kIC; ++q) a[q] = b[q] = 0.0;
+    for (int q = 0; q < kIC; ++q) a[q] = 0.0;
+#pragma unroll
+    for (int q = 0; q < kB; ++q) b[q] = 0.0;
     if (act) {
       for (int64_t row = r0 + rg; row < r1; row += RG) {
         const size_t off = size_t(row) * C;
@@ -120,20 +123,22 @@ __global__ void __launch_bounds__(kT, sizeof(S) == 4 ? LGT_MD_MINB_F32 : LGT_MD_
         const double wx = (NC == 2) ? widen(W[off + (c ^ 1)]) : 0.0;
 #if LGT_MD_HOIST
         // every load of the chunk is issued before the first use; slots past
-        // the basis read its last vector again (an L1 hit) and are skipped
-        double v[kIC];
+        // the basis read its last vector again (an L1 hit) and are skipped.
+        // The loads stay in the storage type until their FMA (widened FP32
+        // values would hold twice the registers and spill).
+        S v[kIC];
         const int ilast = (Jv > 0) ? Jv - 1 : 0;
 #pragma unroll
         for (int q = 0; q < kIC; ++q) {
           const int i = (i0 + q < Jv) ? i0 + q : ilast;
-          v[q] = widen(V[size_t(i) * vstride + off + c]);
+          v[q] = V[size_t(i) * vstride + off + c];
         }
 #pragma unroll
         for (int q = 0; q < kIC; ++q) {
           if (i0 + q < J) {
-            const double vq = (i0 + q < Jv) ? v[q] : w;
+            const double vq = (i0 + q < Jv) ? widen(v[q]) : w;
             a[q] = fma(vq, w, a[q]);
-            if (NC == 2) b[q] = fma(vq, wx, b[q]);
+            if (NC == 2) b[q % kB] = fma(vq, wx, b[q % kB]);
           }
         }
 #else
@@ -142,7 +147,7 @@ __global__ void __launch_bounds__(kT, sizeof(S) == 4 ? LGT_MD_MINB_F32 : LGT_MD_
           if (i0 + q < J) {
             const double vq = (i0 + q < Jv) ? widen(V[size_t(i0 + q) * vstride + off + c]) : w;
             a[q] = fma(vq, w, a[q]);
-            if (NC == 2) b[q] = fma(vq, wx, b[q]);
+            if (NC == 2) b[q % kB] = fma(vq, wx, b[q % kB]);
           }
         }
 #endif
@@ -150,7 +155,7 @@ __global__ void __launch_bounds__(kT, sizeof(S) == 4 ? LGT_MD_MINB_F32 : LGT_MD_
 #pragma unroll
       for (int q = 0; q < kIC; ++q) {
         red[((rg * kIC + q) * 2 + 0) * C + c] = a[q];
-        red[((rg * kIC + q) * 2 + 1) * C + c] = b[q];
+        red[((rg * kIC + q) * 2 + 1) * C + c] = (NC == 2) ? b[q % kB] : 0.0;
       }
     } else if (rg < RG) {
 #pragma unroll
@@ -806,6 +811,17 @@ template <typename S>
 cudaError_t apply_h(const OpDev& op, const S* x, const int* xsel, size_t xstride, S* y, int ncomp,
                     cudaStream_t s);
 
+template <typename S>
+void set_table(const OpDev& op, HpsiArgs<S>* a) {
+  const NbrTable* T = op.table;
+  if (!op.use_table || !T || T->state != 1) return;
+  a->t_meta = T->meta;
+  a->t_off = T->tile_off;
+  a->t_nbr = T->nbr;
+  a->t_mm = T->mm;
+  a->use_table = 1;
+}
+
 template <>
 cudaError_t apply_h<double>(const OpDev& op, const double* x, const int* xsel, size_t xstride,
                             double* y, int ncomp, cudaStream_t s) {
@@ -828,6 +844,7 @@ cudaError_t apply_h<double>(const OpDev& op, const double* x, const int* xsel, s
   a.xstride = xstride;
   a.force_generic = op.force_generic;
   a.vpl = op.vpl;
+  set_table(op, &a);
   return launch_hpsi<double>(a, op.model, s);
 }
 
@@ -853,6 +870,7 @@ cudaError_t apply_h<float>(const OpDev& op, const float* x, const int* xsel, siz
   a.xstride = xstride;
   a.force_generic = op.force_generic;
   a.vpl = op.vpl;
+  set_table(op, &a);
   return launch_hpsi<float>(a, op.model, s);
 }
 
@@ -979,7 +997,65 @@ bool autotune_enabled() {
 
 void apply_variant(OpDev* op, int v) {
   op->force_generic = (v == kHpsiGeneric) ? 1 : 0;
-  op->vpl = (v == kHpsiFixed1) ? 1 : (v == kHpsiFixed2) ? 2 : (v == kHpsiFixed2w) ? 3 : 0;
+  op->use_table = (v >= kHpsiTable1 && v <= kHpsiTable2w) ? 1 : 0;
+  op->vpl = (v == kHpsiFixed1 || v == kHpsiTable1)    ? 1
+            : (v == kHpsiFixed2 || v == kHpsiTable2)  ? 2
+            : (v == kHpsiFixed2w || v == kHpsiTable2w) ? 3
+                                                       : 0;
+}
+
+bool is_table_variant(int v) { return v >= kHpsiTable1 && v <= kHpsiTable2w; }
+
+bool stream_capturing(cudaStream_t s) {
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) return true;
+  return cap != cudaStreamCaptureStatusNone;
+}
+
+// Builds op's neighbour table on first use when the format and the memory
+// budget allow; never while `s` is capturing.  Returns whether it is built.
+bool ensure_table(OpDev* op, cudaStream_t s) {
+  NbrTable* T = op->table;
+  if (!T) return false;
+  if (T->state != 0) return T->state == 1;
+  if (stream_capturing(s)) return false;
+  const char* en = getenv("LGT_NBR_TABLE");
+  size_t bound = 0;
+  if ((en && en[0] == '0') || !nbr_table_eligible(op->G, op->R.dim, op->model, &bound)) {
+    T->state = -1;
+    return false;
+  }
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = 0;
+  size_t cap = size_t(16384) << 20;
+  if (const char* mb = getenv("LGT_NBR_TABLE_MB")) cap = size_t(atoll(mb)) << 20;
+  if (free_b / 4 < cap) cap = free_b / 4;
+  if (bound > cap) {
+    T->state = -1;
+    return false;
+  }
+  const std::string e = build_nbr_table(op->G, op->R, op->model, op->err, T, s);
+  if (!e.empty()) {
+    free_nbr_table(T);
+    T->state = -1;
+    return false;
+  }
+  return true;
+}
+
+// The H*psi variant forced by LGT_HPSI_VARIANT (1..7), or 0.
+int hpsi_forced() {
+  const char* fv = getenv("LGT_HPSI_VARIANT");
+  const int v = fv ? atoi(fv) : 0;
+  return (v >= kHpsiGeneric && v <= kHpsiTable2w) ? v : 0;
+}
+
+// Applies variant v, or the built-in rule when v needs a table that cannot
+// be had; returns the variant applied.
+int apply_variant_checked(OpDev* op, int v, cudaStream_t s) {
+  if (is_table_variant(v) && !ensure_table(op, s)) v = kHpsiDefault;
+  apply_variant(op, v);
+  return v;
 }
 
 struct HpsiKey {
@@ -996,30 +1072,25 @@ std::map<HpsiKey, std::pair<int, double>> g_hpsi_tune;  // variant, ms per launc
 template <typename S>
 std::string tune_hpsi(OpDev* op, const S* x, S* y, int C, int hcomp, cudaStream_t s,
                       int* variant_out, double* ms_out) {
-  // LGT_HPSI_VARIANT=1..4 forces one variant (cross-checks of every kernel)
-  if (const char* fv = getenv("LGT_HPSI_VARIANT")) {
-    const int v = atoi(fv);
-    if (v >= kHpsiGeneric && v <= kHpsiFixed2w) {
-      apply_variant(op, v);
-      if (variant_out) *variant_out = v;
-      if (ms_out) *ms_out = 0.0;
-      return std::string();
-    }
+  // LGT_HPSI_VARIANT=1..7 forces one variant (cross-checks of every kernel)
+  if (const int v = hpsi_forced()) {
+    const int u = apply_variant_checked(op, v, s);
+    if (variant_out) *variant_out = u;
+    if (ms_out) *ms_out = 0.0;
+    return std::string();
   }
   const HpsiKey key{op->G.nx, op->G.ny, op->G.dg, int(op->model), int(sizeof(S)), C, op->R.dim};
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_hpsi_tune.find(key);
     if (it != g_hpsi_tune.end()) {
-      apply_variant(op, it->second.first);
-      if (variant_out) *variant_out = it->second.first;
+      const int u = apply_variant_checked(op, it->second.first, s);
+      if (variant_out) *variant_out = u;
       if (ms_out) *ms_out = it->second.second;
       return std::string();
     }
   }
-  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) cap = cudaStreamCaptureStatusActive;
-  if (!autotune_enabled() || cap != cudaStreamCaptureStatusNone) {
+  if (!autotune_enabled() || stream_capturing(s)) {
     apply_variant(op, kHpsiDefault);
     if (variant_out) *variant_out = kHpsiDefault;
     if (ms_out) *ms_out = 0.0;
@@ -1040,6 +1111,14 @@ std::string tune_hpsi(OpDev* op, const S* x, S* y, int C, int hcomp, cudaStream_
     cand.push_back(kHpsiFixed1);
     if (mode >= 2) cand.push_back(kHpsiFixed2);
     if (mode >= 3) cand.push_back(kHpsiFixed2w);
+  }
+  if (ensure_table(op, s)) {
+    probe.t_meta = op->table->meta;
+    if (table_load_mode(probe, &mode)) {
+      cand.push_back(kHpsiTable1);
+      if (mode >= 2) cand.push_back(kHpsiTable2);
+      if (mode >= 3) cand.push_back(kHpsiTable2w);
+    }
   }
   cudaEvent_t e0, e1;
   KCK(cudaEventCreate(&e0));
@@ -1066,6 +1145,8 @@ std::string tune_hpsi(OpDev* op, const S* x, S* y, int C, int hcomp, cudaStream_
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (e != cudaSuccess) return std::string("autotune: ") + cudaGetErrorString(e);
+  // A built table stays with the Hamiltonian even when another kernel wins
+  // here: graphs captured for its other panel widths may launch from it.
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_hpsi_tune[key] = {best_v, best};
@@ -1080,13 +1161,16 @@ template <typename S>
 std::string autotune(OpDev* op, Work<S>& w, cudaStream_t s, TuneChoice* out) {
   const TuneKey key{op->G.nx, op->G.ny, op->G.dg, int(op->model), int(sizeof(S)),
                     w.C, w.hcomp, w.N};
-  {
+  // a forced H*psi kernel (cross-checks) neither reads nor fills the cache
+  const bool forced = hpsi_forced();
+  if (!forced) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);
     if (it != g_tune.end()) {
-      apply_variant(op, it->second.hpsi_variant);
-      if (w.red.nblk != it->second.red_nblk) w.replan(it->second.red_blocks);
-      if (out) *out = it->second;
+      TuneChoice c = it->second;
+      c.hpsi_variant = apply_variant_checked(op, c.hpsi_variant, s);
+      if (w.red.nblk != c.red_nblk) w.replan(c.red_blocks);
+      if (out) *out = c;
       return std::string();
     }
   }
@@ -1151,8 +1235,8 @@ std::string autotune(OpDev* op, Work<S>& w, cudaStream_t s, TuneChoice* out) {
   }
   w.replan(c.red_blocks);
   c.red_nblk = w.red.nblk;
-  apply_variant(op, c.hpsi_variant);
-  {
+  c.hpsi_variant = apply_variant_checked(op, c.hpsi_variant, s);
+  if (!forced) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune[key] = c;
   }

@@ -72,6 +72,9 @@ struct lgt_ham {
   DevBuf x, y, part, out;
   Pattern pattern;          // lookup pass of the per-CTA solver (built on demand)
   SmallWork small;
+  // neighbour table of the panel H*psi (built on demand by the autotuner;
+  // mutable: op() hands out a pointer through which it is built)
+  mutable lgt::NbrTable table;
   OpDev op() const {
     OpDev o;
     o.G = b->B.G;
@@ -88,6 +91,7 @@ struct lgt_ham {
     o.cm_f = coef_f + K;
     o.ch_f = coef_f + 2 * K;
     o.cp_f = coef_f + 3 * K;
+    o.table = &table;
     return o;
   }
 };

@@ -1,6 +1,8 @@
 // lgt_hpsi.h -- launch interface of the H*psi and CSR-export kernels.
 #pragma once
 
+#include <string>
+
 #include "lgt_internal.h"
 
 namespace lgt {
@@ -28,7 +30,42 @@ struct HpsiArgs {
   int force_generic = 0;  // 1: run-time-geometry kernel even for a fixed shape
   int vpl = 0;            // fixed-shape load mode: 1 one vector per lane, 2 two,
                           // 3 two as one 32-byte access; 0 the built-in rule
+  // Stored neighbour table (nbr_table.cu); with use_table the table kernel
+  // runs (same load modes as the fixed-shape kernel).
+  const uint32_t* t_meta = nullptr;
+  const uint32_t* t_off = nullptr;
+  const uint32_t* t_nbr = nullptr;
+  int t_mm = 0;           // most entries a row can have
+  int use_table = 0;
 };
+
+// The neighbour ranks of every row of a basis for one model, kept in HBM
+// (nbr_table.cu): meta[N], tile_off[ceil(N/32) + 1], nbr[nnz].
+struct NbrTable {
+  int64_t N = 0, nnz = 0;
+  uint32_t model = 0;
+  int mm = 0;
+  uint32_t* meta = nullptr;
+  uint32_t* tile_off = nullptr;
+  uint32_t* nbr = nullptr;
+  size_t bytes = 0;
+  int state = 0;  // 0 not built, 1 built, -1 declined (size or representability)
+};
+
+// Whether the basis fits the table format (N < 2^31, fewer than 2^32
+// entries, counts and sum of e^2 below 256); *bytes: an upper bound of the
+// table's size.
+bool nbr_table_eligible(const Geom& G, int64_t N, uint32_t model, size_t* bytes);
+std::string build_nbr_table(const Geom& G, const RankView& R, uint32_t model, int* err,
+                            NbrTable* T, cudaStream_t s);
+void free_nbr_table(NbrTable* T);
+
+// Whether the table kernel serves these arguments (table present, vector-
+// aligned panels) and its widest load mode (as hpsi_fixed_applies).
+template <typename T>
+bool table_load_mode(const HpsiArgs<T>& a, int* max_vpl);
+template <typename T>
+cudaError_t launch_hpsi_table(const HpsiArgs<T>& a, uint32_t model, cudaStream_t s);
 
 // Whether a fixed-shape kernel serves these arguments, and the widest load
 // mode it may use (1, 2 when C is a multiple of two vectors, 3 when the
@@ -39,9 +76,10 @@ bool hpsi_fixed_applies(const HpsiArgs<T>& a, int* max_vpl);
 // Default staging decision for the top-level rank table.
 int hpsi_seg_smem_default(int nmasks);
 
-// y = H x.  Lattices with a compile-time kernel (4x4, 4x3, 3x4 at dg = 1,
-// rank tables present, vector-aligned panels) use it; all others the
-// run-time-geometry kernel.  Both give the same product.
+// y = H x.  With use_table and a table present, the stored-table kernel;
+// else lattices with a compile-time kernel (4x4, 4x3, 3x4 at dg = 1, rank
+// tables present, vector-aligned panels) use it; all others the
+// run-time-geometry kernel.  All give the same product.
 template <typename T>
 cudaError_t launch_hpsi(HpsiArgs<T> a, uint32_t model, cudaStream_t s);
 

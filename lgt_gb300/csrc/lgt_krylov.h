@@ -21,6 +21,8 @@ struct OpDev {
   const float *cE_f, *cm_f, *ch_f, *cp_f;
   int force_generic = 0;  // H*psi through the run-time-geometry kernel only
   int vpl = 0;            // fixed-shape H*psi: vector loads per lane (0: by width)
+  NbrTable* table = nullptr;  // the Hamiltonian's neighbour table (built on demand)
+  int use_table = 0;          // H*psi from the stored table
 };
 
 struct KrylovParams {
@@ -45,6 +47,9 @@ enum HpsiVariant : int {
   kHpsiFixed1 = 2,    // fixed shape, one 16-byte vector per lane
   kHpsiFixed2 = 3,    // fixed shape, two 16-byte vectors per lane
   kHpsiFixed2w = 4,   // fixed shape, two vectors as one 32-byte access
+  kHpsiTable1 = 5,    // stored neighbour table, one 16-byte vector per lane
+  kHpsiTable2 = 6,    // stored neighbour table, two 16-byte vectors per lane
+  kHpsiTable2w = 7,   // stored neighbour table, one 32-byte access per lane
 };
 struct TuneChoice {
   int hpsi_variant = kHpsiDefault;
@@ -64,6 +69,10 @@ std::string krylov_autotune(const OpDev& op, KrylovCache* cache, int ncomp, int 
 // H*psi variant for this operator and panel width, timed on (x, y) at the
 // first call of each shape (x is only read; y is overwritten); sets op's
 // kernel selection.  No timing while `s` is capturing or LGT_AUTOTUNE=0.
+// The table variants are candidates when op's neighbour table is built or
+// can be: the basis fits the format and the table's size bound is within
+// min(free device memory / 4, LGT_NBR_TABLE_MB, default 16384 MB);
+// LGT_NBR_TABLE=0 disables it.
 std::string hpsi_choose_d(OpDev* op, const double* x, double* y, int ncomp, cudaStream_t s);
 std::string hpsi_choose_f(OpDev* op, const float* x, float* y, int ncomp, cudaStream_t s);
 

@@ -35,6 +35,9 @@ _MODELS = {"ref": C.LGT_MODEL_REF, "jw": C.LGT_MODEL_JW, "plaq": C.LGT_MODEL_PLA
            "pjw": C.LGT_MODEL_PJW}
 _PREC = {"fp64": C.LGT_FP64, "fp32": C.LGT_FP32, "fp32_mixed": C.LGT_FP32_MIXED,
          "mixed": C.LGT_FP32_MIXED}
+# lgt_tuning.hpsi_kernel codes (include/lgt_ed.h)
+HPSI_KERNELS = {0: "rule", 1: "generic", 2: "fixed_vpl1", 3: "fixed_vpl2", 4: "fixed_wide",
+                5: "table_vpl1", 6: "table_vpl2", 7: "table_wide"}
 
 
 def _p(a):
@@ -352,8 +355,7 @@ class Hamiltonian:
         ground states, 2: exponential steps); tunes on first use."""
         t = C.Tuning()
         C.check(C.load().lgt_autotune(self._h, int(ncomp), _PREC[precision], ctypes.byref(t)))
-        names = {0: "rule", 1: "generic", 2: "fixed_vpl1", 3: "fixed_vpl2", 4: "fixed_wide"}
-        return {"hpsi_kernel": names.get(t.hpsi_kernel, str(t.hpsi_kernel)),
+        return {"hpsi_kernel": HPSI_KERNELS.get(t.hpsi_kernel, str(t.hpsi_kernel)),
                 "reduce_blocks": t.reduce_blocks, "hpsi_ms": t.hpsi_ms,
                 "reduce_ms": t.reduce_ms, "measured": bool(t.measured)}
 

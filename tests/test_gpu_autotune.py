@@ -19,7 +19,8 @@ def test_autotune_choice_is_reported_and_cached(oracle, lgt):
         for prec in ("fp64", "fp32_mixed"):
             c = H.autotune(ncomp, prec)
             assert c["measured"]
-            assert c["hpsi_kernel"] in ("generic", "fixed_vpl1", "fixed_vpl2", "fixed_wide")
+            assert c["hpsi_kernel"] in ("generic", "fixed_vpl1", "fixed_vpl2", "fixed_wide",
+                                        "table_vpl1", "table_vpl2", "table_wide")
             assert c["reduce_blocks"] in (304, 608, 912, 1216)
             assert 0.0 < c["hpsi_ms"] < 1e3 and 0.0 < c["reduce_ms"] < 1e3
             assert H.autotune(ncomp, prec) == c  # cached for the process

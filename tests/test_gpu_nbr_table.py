@@ -1,0 +1,131 @@
+"""GPU parity of the stored-neighbour-table H*psi (nbr_table.cu).
+
+The table is built once per Hamiltonian by the run-time-geometry move
+enumeration (any shape, any dg); its kernel gathers with the fixed-shape
+kernel's load modes (LGT_HPSI_VARIANT=5, 6, 7: one or two 16-byte vectors
+per lane, two as one 32-byte access).  Bars: 1e-12 relative to max |y|
+(FP64) and 2e-6 (FP32) against the FP64 oracle's CSR matrix (reference and
+plaquette+JW models), against the run-time-geometry kernel for the JW-only
+and plaquette-only models and on the 4x4 lattice; ground states within
+1e-10 of the oracle.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+COUPLINGS = [(1.0, 1.0, 0.5), (0.8, 1.3, 0.3), (2.0, 0.7, -1.1), (0.55, 1.0, 0.9),
+             (1.4, 0.9, 0.0), (0.3, 1.1, 2.0), (1.0, 0.5, -0.4), (2.5, 1.0, 0.7)]
+
+# (nx, ny, dg, sector)
+CASES = [(3, 2, 1, "stag"), (2, 3, 1, "zero"), (4, 2, 1, "string"), (3, 3, 1, "stag"),
+         (4, 3, 1, "stag"), (3, 4, 1, "string"), (2, 2, 2, "stag"), (3, 2, 2, "stag"),
+         (1, 4, 1, "stag"), (4, 1, 1, "stag")]
+WIDTHS = {"fp64": [(1, True), (2, True), (4, False)], "fp32": [(2, True), (4, True), (8, False)]}
+
+_cache = {}
+
+
+def _charges(O, nx, ny, kind):
+    if kind == "stag":
+        return O.staggered_charges(nx, ny)
+    if kind == "string":
+        return O.string_charges(nx, ny)
+    return np.zeros((nx, ny), np.int32)
+
+
+def _pair(O, L, nx, ny, dg, kind):
+    key = (nx, ny, dg, kind)
+    if key not in _cache:
+        g = _charges(O, nx, ny, kind)
+        _cache[key] = (O.build_basis(nx, ny, dg, g), L.build_basis(nx, ny, dg, g)[0])
+    return _cache[key]
+
+
+def _panel(rng, N, K, cplx, prec):
+    x = rng.standard_normal((N, K))
+    if cplx:
+        x = x + 1j * rng.standard_normal((N, K))
+    return x.astype(np.complex64 if cplx else np.float32) if prec == "fp32" else x
+
+
+def _tol(prec):
+    return 1e-12 if prec == "fp64" else 2e-6
+
+
+@pytest.mark.parametrize("variant", ["5", "6", "7"])
+@pytest.mark.parametrize("model", ["ref", "jw", "plaq", "pjw"])
+@pytest.mark.parametrize("nx,ny,dg,kind", CASES)
+def test_table_vs_oracle(oracle, lgt, nx, ny, dg, kind, model, variant, monkeypatch):
+    monkeypatch.setenv("LGT_HPSI_VARIANT", variant)
+    ob, gb = _pair(oracle, lgt, nx, ny, dg, kind)
+    rng = np.random.default_rng(nx * 100 + ny * 10 + dg)
+    Hos = {}
+    for prec in ("fp64", "fp32"):
+        for K, cplx in WIDTHS[prec]:
+            gs, ts, ms = (np.array(v) for v in zip(*COUPLINGS[:K]))
+            H = lgt.build_hamiltonian(gb, g=gs, t=ts, m=ms, model=model)
+            x = _panel(rng, ob.dim, K, cplx, prec)
+            y = H.matvec(x, precision=prec)
+            if model in ("jw", "plaq"):  # no oracle matrix: the run-time-geometry kernel
+                yg = H.matvec(x, precision=prec, generic=True)
+                scale = max(1.0, float(np.max(np.abs(yg))))
+                assert np.max(np.abs(y - yg)) <= _tol(prec) * scale, (prec, K, cplx)
+                H.close()
+                continue
+            for k in range(K):
+                if k not in Hos:
+                    g, t, m = COUPLINGS[k]
+                    Hos[k] = oracle.build_hamiltonian(ob, g=g, t=t, m=m, model=model)
+                yo = Hos[k] @ x[:, k].astype(np.complex128 if cplx else np.float64)
+                err = np.max(np.abs(y[:, k] - yo))
+                assert err <= _tol(prec) * max(1.0, np.max(np.abs(yo))), (prec, K, cplx, k, err)
+            H.close()
+
+
+@pytest.mark.parametrize("variant", ["6", "7"])
+@pytest.mark.parametrize("model", ["ref", "pjw"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_table_4x4_vs_generic(lgt, model, prec, variant, monkeypatch):
+    """4x4 staggered sector (N = 8,563,545), K = 4 complex."""
+    monkeypatch.setenv("LGT_HPSI_VARIANT", variant)
+    st, _ = lgt.build_basis(4, 4, 1, lgt.staggered_charges(4, 4))
+    rng = np.random.default_rng(45)
+    gs, ts, ms = (np.array(v) for v in zip(*COUPLINGS[:4]))
+    H = lgt.build_hamiltonian(st, g=gs, t=ts, m=ms, model=model)
+    x = _panel(rng, len(st), 4, True, prec)
+    y = H.matvec(x, precision=prec)
+    yg = H.matvec(x, precision=prec, generic=True)
+    assert np.max(np.abs(y - yg)) <= _tol(prec) * max(1.0, float(np.max(np.abs(yg))))
+    H.close()
+
+
+def test_table_disabled_falls_back(oracle, lgt, monkeypatch):
+    """With LGT_NBR_TABLE=0 a forced table variant runs the built-in rule."""
+    monkeypatch.setenv("LGT_HPSI_VARIANT", "6")
+    monkeypatch.setenv("LGT_NBR_TABLE", "0")
+    ob, gb = _pair(oracle, lgt, 4, 3, 1, "stag")
+    H = lgt.build_hamiltonian(gb, g=[0.9, 1.2], t=1.0, m=0.4)
+    x = _panel(np.random.default_rng(7), ob.dim, 2, True, "fp64")
+    y = H.matvec(x)
+    for k, g in enumerate((0.9, 1.2)):
+        yo = oracle.build_hamiltonian(ob, g=g, t=1.0, m=0.4) @ x[:, k]
+        assert np.max(np.abs(y[:, k] - yo)) <= 1e-12 * max(1.0, np.max(np.abs(yo)))
+    H.close()
+
+
+@pytest.mark.parametrize("model", ["ref", "pjw"])
+def test_table_ground_states(oracle, lgt, model, monkeypatch):
+    """Panel Lanczos (FP64 and FP32-mixed) with the table kernel forced."""
+    monkeypatch.setenv("LGT_HPSI_VARIANT", "6")
+    ob, gb = _pair(oracle, lgt, 4, 3, 1, "stag")
+    gs = np.array([0.6, 1.1, 1.7, 2.4])
+    H = lgt.build_hamiltonian(gb, g=gs, t=1.0, m=0.3, model=model)
+    E0o = [oracle.ground_state(oracle.build_hamiltonian(ob, g=g, t=1.0, m=0.3, model=model))[0]
+           for g in gs]
+    for prec in ("fp64", "fp32_mixed"):
+        E0, _ = lgt.find_ground_state(H, tol=1e-12, solver="panel", precision=prec,
+                                      as_complex=False)
+        for k in range(len(gs)):
+            assert abs(E0[k] - E0o[k]) <= 1e-10 * abs(E0o[k]), (prec, k)
+    H.close()
