@@ -52,6 +52,7 @@ struct SmallParams {
   uint64_t seed;
   int start_given;
   int rows_per_thread = 0;  // launch shape: 0 the smallest R with N <= 512 R
+  int v_smem = 0;           // set by the launcher: Krylov basis in shared memory
 };
 
 // One Hamiltonian's share of a batched launch.

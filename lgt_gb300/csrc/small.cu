@@ -11,7 +11,10 @@
 // pass only on cancellation), the tridiagonal check (lgt_tridiag.cuh),
 // restarts and the FP64 finish without leaving the kernel.  Units of
 // different sectors and sizes share one launch (uneven batch); the largest
-// are scheduled first.
+// are scheduled first.  When the basis of the largest sector fits (the
+// FP32-mixed path up to about 1000 states at krylovdim 50), it sits in
+// shared memory instead: one CTA per SM either way, and the Gram-Schmidt
+// and matvec loads then wait on shared memory, not on L2.
 //
 // The neighbour ranks of a lattice are computed once by a device "lookup
 // pass" (k_pattern_*: the move enumeration and rank of the H*psi kernel)
@@ -159,6 +162,7 @@ __device__ double block_sum(double v, double* red) {
 template <typename S, int R>
 __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* probs,
                                                       const SmallUnit* units, SmallParams prm) {
+  extern __shared__ __align__(16) unsigned char s_basis[];  // (m + 1) x N when prm.v_smem
   __shared__ double s_alpha[kMaxM + 1], s_beta[kMaxM + 1], s_h[kMaxM + 1], s_z[kMaxM + 1];
   __shared__ double s_part[kMaxM + 1][kWarpsCta];
   __shared__ double s_red[kWarpsCta];
@@ -171,7 +175,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int nthr = blockDim.x, nwarps = nthr >> 5;  // rows r = tid + i * nthr, i < R
   const int m = (prm.m < N) ? prm.m : N;
-  S* V = reinterpret_cast<S*>(U.V);
+  S* V = reinterpret_cast<S*>(prm.v_smem ? static_cast<void*>(s_basis) : U.V);
   const S cE = S(U.cE), cm = S(U.cm), ch = S(U.ch), cp = S(U.cp);
   const bool fp32 = sizeof(S) == 4;
   const double tiny_rel = fp32 ? 1e-6 : 1e-12;
@@ -435,18 +439,45 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
 // enough whole warps for the largest sector: idle lanes still occupy the
 // FP64 pipe in every warp instruction.  rows_per_thread = 0 takes the
 // smallest R with maxN <= 512 R; a larger R means fewer threads.
+// Environment switch (default `def`): "0" turns it off.
+bool getenv_flag(const char* name, int def) {
+  const char* e = getenv(name);
+  if (!e || !e[0]) return def != 0;
+  return e[0] != '0';
+}
+
+// Dynamic shared memory a CTA may take beside the kernel's static arrays.
+constexpr int kCtaSmemMax = 200 * 1024;
+
 template <typename S>
 cudaError_t launch_cta(const SmallProblem* probs, const SmallUnit* units, int nunits, int maxN,
-                       const SmallParams& prm, cudaStream_t s, int rows_per_thread) {
+                       const SmallParams& prm_in, cudaStream_t s, int rows_per_thread) {
   int R = (maxN + kCta - 1) / kCta;
   if (rows_per_thread > R) R = rows_per_thread;
   auto threads_for = [&](int rr) {
     int t = ((maxN + rr - 1) / rr + 31) / 32 * 32;
     return t < 64 ? 64 : t;  // the reduction of step j uses threads 0..j
   };
+  // Krylov basis of every unit in shared memory when the largest fits
+  SmallParams prm = prm_in;
+  const int mmax = (prm.m < maxN) ? prm.m : maxN;
+  const size_t vbytes = size_t(mmax + 1) * size_t(maxN) * sizeof(S);
+  const bool smem = getenv_flag("LGT_CTA_BASIS_SMEM", 1) && vbytes <= size_t(kCtaSmemMax);
+  prm.v_smem = smem ? 1 : 0;
+  const int dyn = smem ? int((vbytes + 15) / 16 * 16) : 0;
 #define LGT_CTA_CASE(RR)                                                                    \
   if (R <= RR) {                                                                            \
-    k_lanczos_cta<S, RR><<<nunits, threads_for(RR), 0, s>>>(probs, units, prm),            \
+    if (dyn > 48 * 1024) {                                                                  \
+      static int attr = 48 * 1024;                                                          \
+      if (dyn > attr) {                                                                     \
+        cudaError_t ea = cudaFuncSetAttribute(k_lanczos_cta<S, RR>,                         \
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                                              kCtaSmemMax);                                 \
+        if (ea != cudaSuccess) return ea;                                                   \
+        attr = kCtaSmemMax;                                                                 \
+      }                                                                                     \
+    }                                                                                       \
+    k_lanczos_cta<S, RR><<<nunits, threads_for(RR), dyn, s>>>(probs, units, prm),          \
         lgt::note_launch();                                                                 \
     return cudaGetLastError();                                                              \
   }

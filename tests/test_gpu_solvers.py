@@ -110,3 +110,23 @@ def test_quench_4x3_batched(oracle, lgt, precision, tol_state, model):
         assert abs(e1 - e0) <= 100 * tol_state * abs(e0)
     assert np.all(drift < (1e-12 if precision == "fp64" else 1e-5))
     H.close()
+
+
+@pytest.mark.parametrize("smem", ["0", "1"])
+@pytest.mark.parametrize("precision,krylovdim", [("fp32_mixed", 50), ("fp64", 30), ("fp64", 50)])
+def test_cta_basis_placement(oracle, lgt, monkeypatch, smem, precision, krylovdim):
+    """The per-CTA solver keeps the Krylov basis in shared memory when it
+    fits (FP32 at krylovdim 50, FP64 at 30 on the 4x2 sector) and in global
+    memory otherwise or with LGT_CTA_BASIS_SMEM=0: same results."""
+    monkeypatch.setenv("LGT_CTA_BASIS_SMEM", smem)
+    ob, gb = _basis(oracle, lgt, 4, 2)
+    gs = np.array([0.5, 0.9, 1.4, 2.0])
+    H = lgt.build_hamiltonian(gb, g=gs, t=1.0, m=0.5)
+    E0, psi = lgt.find_ground_state(H, tol=1e-12, precision=precision, solver="cta",
+                                    krylovdim=krylovdim, as_complex=False)
+    for k in range(len(gs)):
+        Ho = oracle.build_hamiltonian(ob, g=gs[k], t=1.0, m=0.5)
+        E0o, psio = oracle.ground_state(Ho)
+        assert abs(E0[k] - E0o) <= 1e-10 * abs(E0o), (k, E0[k], E0o)
+        assert abs(abs(np.dot(psi[:, k], psio)) - 1.0) <= 1e-8
+    H.close()
