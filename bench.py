@@ -40,9 +40,11 @@ import numpy as np  # noqa: E402
 NX, NY, DG, KPTS = 4, 2, 1, 64
 G_LO, G_HI, T_HOP, MASS = 0.5, 2.0, 1.0, 0.5
 RF_NX, RF_NY, RF_K = 4, 4, 8          # roofline panel (4x4 quench, K = 8 complex)
-# DRAM bytes of one such launch (FP32, reference model), measured by ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum, --set full, one launch)
-RF_TRAFFIC_BYTES = int((2.903165 + 0.533069) * 1e9)
+# DRAM bytes of one such launch (FP32, reference model) per kernel family,
+# measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum, --set full,
+# one launch; profiles/k_hpsi_*_4x4_K8_complex.md)
+RF_TRAFFIC_BYTES = {"fixed": int((2.903165 + 0.533069) * 1e9),
+                    "table": int((3.239323 + 0.532817) * 1e9)}
 L2_FLUSH_BYTES = 512 << 20            # > 129 MB L2
 METRIC = "ground states/s, batched FP32-mixed Lanczos at |dE|/|E|<=1e-10"
 
@@ -474,7 +476,11 @@ def ctypes_byref(v):
     return ctypes.byref(v)
 
 
-def roofline(L, C, lib, torch, stream, dev, reps=10):
+def roofline(L, C, lib, torch, stream, dev, reps=10, only=None):
+    """H*psi on the 4x4 quench panel: every kernel family for both models and
+    precisions, or with `only` ("auto", "generic", "fixed", "table") that one
+    on the reference model's FP32 panel (a fixed launch list for ncu)."""
+    import ctypes
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -491,38 +497,69 @@ def roofline(L, C, lib, torch, stream, dev, reps=10):
     C.check(lib.lgt_basis_set_stream(b.handle, ctypes_ptr(stream.cuda_stream)))
     gs = np.random.default_rng(0).uniform(0.5, 1.5, RF_K)
     out = {"N": N, "basis_build_s": basis_s}
-    for model in ("ref", "pjw"):
+    # variants: the autotuner's choice, and each kernel family forced
+    # (LGT_HPSI_VARIANT: 3 fixed shape, 6 stored table; two vectors per lane)
+    forced = {"": None, "_generic": None, "_fixed": "3", "_table": "6"}
+    models, precs = ("ref", "pjw"), (("fp64", torch.float64, 16), ("fp32", torch.float32, 8))
+    if only is not None:
+        sfx = "" if only == "auto" else "_" + only
+        forced = {sfx: forced[sfx]}
+        models, precs = ("ref",), (("fp32", torch.float32, 8),)
+    saved = os.environ.get("LGT_HPSI_VARIANT")
+    for model in models:
         H = L.build_hamiltonian(b, g=gs, t=1.0, m=0.5, model=model)
-        for prec, dtype, s, generic in (("fp64", torch.float64, 16, False),
-                                        ("fp32", torch.float32, 8, False),
-                                        ("fp64", torch.float64, 16, True),
-                                        ("fp32", torch.float32, 8, True)):
-            x = torch.randn((N, RF_K, 2), dtype=dtype, device="cuda")
-            y = torch.empty_like(x)
-            flags = C.LGT_DEVICE_PTRS | C.LGT_ASYNC | (C.LGT_GENERIC_KERNELS if generic else 0)
-            code = C.LGT_FP64 if prec == "fp64" else C.LGT_FP32
-            ts = []
-            for it in range(reps + 2):
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                with torch.cuda.stream(stream):
-                    e0.record(stream)
-                    C.check(lib.lgt_matvec(H.handle, x.data_ptr(), y.data_ptr(), 2, code, flags))
-                    e1.record(stream)
-                e1.synchronize()
-                if it >= 2:
-                    ts.append(e0.elapsed_time(e1) * 1e-3)
-            t = statistics.mean(ts)
-            algo = N * 8 + 2 * RF_K * N * s   # key table + x + y, neighbour gathers 0
-            row = {"ms": t * 1e3, "algo_bytes": algo, "gbs": algo / t / 1e9,
-                   "frac": algo / t / 1e9 / peak}
-            if not generic:  # the autotuner's kernel for this shape (chosen at the first call)
-                tune = C.Tuning()
-                C.check(lib.lgt_autotune(H.handle, 2, code, ctypes_byref(tune)))
-                row["kernel"] = L.HPSI_KERNELS[tune.hpsi_kernel]
-            out["%s_%s%s" % (model, prec, "_generic" if generic else "")] = row
-            del x, y
+        nnz = ctypes.c_int64()
+        C.check(lib.lgt_ham_nnz(H.handle, ctypes.byref(nnz)))
+        # stored table: meta word per row, offset per 32 rows, 4 bytes per
+        # off-diagonal entry (the CSR count less the diagonal)
+        table_bytes = 4 * (N + (N + 31) // 32 + 1 + (nnz.value - N))
+        for prec, dtype, s in precs:
+            for suffix, var in forced.items():
+                generic = suffix == "_generic"
+                if var is None:
+                    os.environ.pop("LGT_HPSI_VARIANT", None)
+                else:
+                    os.environ["LGT_HPSI_VARIANT"] = var
+                x = torch.randn((N, RF_K, 2), dtype=dtype, device="cuda")
+                y = torch.empty_like(x)
+                flags = C.LGT_DEVICE_PTRS | C.LGT_ASYNC | (C.LGT_GENERIC_KERNELS if generic else 0)
+                code = C.LGT_FP64 if prec == "fp64" else C.LGT_FP32
+                ts = []
+                for it in range(reps + 2):
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    with torch.cuda.stream(stream):
+                        e0.record(stream)
+                        C.check(lib.lgt_matvec(H.handle, x.data_ptr(), y.data_ptr(), 2, code,
+                                               flags))
+                        e1.record(stream)
+                    e1.synchronize()
+                    if it >= 2:
+                        ts.append(e0.elapsed_time(e1) * 1e-3)
+                t = statistics.mean(ts)
+                if generic:
+                    kernel = "generic"
+                elif var is not None:
+                    kernel = "fixed_vpl2" if var == "3" else "table_vpl2"
+                else:  # the autotuner's kernel for this shape (chosen at the first call)
+                    tune = C.Tuning()
+                    C.check(lib.lgt_autotune(H.handle, 2, code, ctypes_byref(tune)))
+                    kernel = L.HPSI_KERNELS[tune.hpsi_kernel]
+                # algorithmic bytes: x read once, y written once, plus the
+                # per-row stream the kernel must read (order keys for the
+                # matrix-free kernels, the stored table for the table kernel)
+                xy = 2 * RF_K * N * s
+                algo = xy + (table_bytes if kernel.startswith("table") else N * 8)
+                out["%s_%s%s" % (model, prec, suffix)] = {
+                    "ms": t * 1e3, "algo_bytes": algo, "gbs": algo / t / 1e9,
+                    "frac": algo / t / 1e9 / peak, "kernel": kernel,
+                    "matrix_free_algo_bytes": xy + N * 8}
+                del x, y
         H.close()
+    if saved is None:
+        os.environ.pop("LGT_HPSI_VARIANT", None)
+    else:
+        os.environ["LGT_HPSI_VARIANT"] = saved
     b.close()
     out["peak"] = peak
     out["peak_src"] = peak_src
@@ -537,6 +574,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quench-steps", type=int, default=4,
                     help="timed 4x4 quench steps (dt = 0.05; t = 5 needs 100)")
+    ap.add_argument("--hpsi-only", default=None, choices=["auto", "generic", "fixed", "table"],
+                    help="--part hpsi: time one kernel family on the reference FP32 panel")
     ap.add_argument("--part", default="all", choices=["all", "hpsi", "gs", "quench"],
                     help="hpsi: only the 4x4 H*psi roofline loop; gs: only the headline "
                          "ground-state loop (both for profiling: no child processes)")
@@ -595,7 +634,8 @@ def main():
         import lgt_gb300 as L
         from lgt_gb300 import _capi as C
         torch.cuda.set_device(0)
-        rf = roofline(L, C, C.load(), torch, torch.cuda.Stream(), 0, reps=args.steps)
+        rf = roofline(L, C, C.load(), torch, torch.cuda.Stream(), 0, reps=args.steps,
+                      only=args.hpsi_only)
         print(json.dumps({"part": "hpsi", "roofline": rf}))
         return
 
@@ -632,6 +672,8 @@ def main():
     pool.close()
     rf = r["rf"]
     dom = rf["ref_fp32"]
+    fam = "table" if dom["kernel"].startswith("table") else "fixed"
+    traffic = RF_TRAFFIC_BYTES.get(fam) if dom["kernel"] != "generic" else None
     e2e_val = KPTS / statistics.mean(r["e2e_times"])
     line = {
         "metric": METRIC,
@@ -654,16 +696,20 @@ def main():
             "pjw_fp32_mixed_batched_gs_per_s": KPTS / statistics.mean(r["t_pjw"]),
             "matvecs_per_solve_mixed": r["matvecs_mix"], "restarts_mixed": r["restarts_mix"],
         },
-        "roofline": {"kernel": "k_hpsi_fixed (H*psi), 4x4 N=8563545, K=8 complex FP32 (the "
-                               "FP32-mixed quench panel), reference model",
+        "roofline": {"kernel": "%s (H*psi, autotuned: %s), 4x4 N=8563545, K=8 complex FP32 "
+                               "(the FP32-mixed quench panel), reference model"
+                               % ("k_hpsi_table" if fam == "table" else "k_hpsi_fixed",
+                                  dom["kernel"]),
                      "bound": "hbm", "achieved": dom["gbs"], "peak": rf["peak"], "unit": "GB/s",
-                     "frac": dom["frac"], "traffic": RF_TRAFFIC_BYTES,
-                     "traffic_note": "ncu DRAM bytes per launch; 3.0x the algorithmic bytes: "
-                                     "neighbour gathers re-read x from HBM (LRU model of a "
-                                     "100 MB L2: 4.4 misses per row)",
-                     "dram_gbs_of_traffic": RF_TRAFFIC_BYTES / (dom["ms"] * 1e-3) / 1e9,
-                     "dram_frac_of_traffic": RF_TRAFFIC_BYTES / (dom["ms"] * 1e-3) / 1e9
-                     / rf["peak"],
+                     "frac": dom["frac"], "traffic": traffic,
+                     "traffic_note": "ncu DRAM bytes per launch; neighbour gathers re-read x "
+                                     "from HBM (LRU model of a 100 MB L2: 4.4 misses per row); "
+                                     "algorithmic bytes: x + y + %s"
+                                     % ("the stored neighbour table" if fam == "table"
+                                        else "the order keys"),
+                     "dram_gbs_of_traffic": traffic / (dom["ms"] * 1e-3) / 1e9 if traffic else None,
+                     "dram_frac_of_traffic": traffic / (dom["ms"] * 1e-3) / 1e9 / rf["peak"]
+                     if traffic else None,
                      "peak_source": rf["peak_src"] + " (MEASURED_PEAKS.json hbm_gbs)",
                      "algo_bytes_per_launch": dom["algo_bytes"], "ms_per_launch": dom["ms"],
                      "variants": {k: v for k, v in rf.items() if isinstance(v, dict)}},

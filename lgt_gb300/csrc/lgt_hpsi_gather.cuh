@@ -18,10 +18,11 @@ namespace lgt {
 namespace gather {
 
 // Neighbour rows gathered per loop trip: measured on the 4x4 lattice, K = 8
-// complex, 4 rows in flight for FP32, 2 for FP64 (bound by the FP64 pipe,
-// not by latency).
+// complex, 8 rows in flight for FP32 (the table kernel: 0.757 -> 0.714 ms
+// against 4; the fixed-shape kernel is indifferent), 2 for FP64 (bound by
+// the FP64 pipe, not by latency; 8 costs 15%).
 #ifndef LGT_GATHER_UNROLL
-#define LGT_GATHER_UNROLL (sizeof(T) == 4 ? 4 : 2)
+#define LGT_GATHER_UNROLL (sizeof(T) == 4 ? 8 : 2)
 #endif
 
 // Per-row meta word of a neighbour list: entry count, hop count (hops come

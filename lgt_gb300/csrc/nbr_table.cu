@@ -34,9 +34,11 @@ namespace {
 constexpr int kBuildThreads = 256;
 constexpr int kTabWarps = 8;
 constexpr int kTabThreads = kTabWarps * 32;
-// resident blocks per SM (same register budget as the fixed-shape kernel)
+// Resident blocks per SM the register budget must allow.  Measured on the
+// 4x4 lattice, K = 8 complex FP32: 5 blocks with 8 rows in flight beat 6
+// with 4 (0.714 vs 0.757 ms); 8 blocks (32 registers) spill.
 #ifndef LGT_TABLE_MINB
-#define LGT_TABLE_MINB 6
+#define LGT_TABLE_MINB 5
 #endif
 #ifndef LGT_TABLE_MINB_PLAQ
 #define LGT_TABLE_MINB_PLAQ 4
