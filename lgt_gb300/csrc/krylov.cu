@@ -83,9 +83,6 @@ __global__ void k_randn(S* out, int64_t N, int C, int ncomp, uint64_t seed) {
 // Measured on the 4x4 quench panel (K = 8 complex, FP64 and FP32 storage):
 // the dot kernel issues a chunk's loads before its FMAs and keeps 4 blocks
 // per SM; the update's plain two-chain loop beats hoisted loads.
-#ifndef LGT_MD_HOIST
-#define LGT_MD_HOIST 1
-#endif
 #ifndef LGT_UPD_HOIST
 #define LGT_UPD_HOIST 0
 #endif
@@ -99,8 +96,61 @@ __global__ void k_randn(S* out, int64_t N, int C, int ncomp, uint64_t seed) {
 #define LGT_MD_MINB 4  // resident blocks per SM the dot kernel's registers must allow (FP64)
 #endif
 #ifndef LGT_MD_MINB_F32
-#define LGT_MD_MINB_F32 5  // the same for FP32 panels (measured: 5 beats 4 and 6)
+#define LGT_MD_MINB_F32 4  // the same for FP32 panels (measured with chunks sized to the
+                           // vectors left: 4 without spills beats 5 with them)
 #endif
+// One chunk of a dot pass: the NQ basis vectors i0 .. i0 + NQ - 1 (those
+// from J on are skipped) against W, per thread one column and every RG-th
+// row of the block's range, into red[rg][q][comp][c].  Every load of a row
+// is issued before the first FMA; slots past the basis read its last vector
+// again (an L1 hit).  The loads stay in the storage type until their FMA
+// (widened FP32 values would hold twice the registers and spill).
+template <typename S, int NC, int NQ>
+__device__ __forceinline__ void dots_chunk(const S* __restrict__ V, size_t vstride,
+                                           const S* __restrict__ W, int64_t r0, int64_t r1,
+                                           int rg, int RG, int c, int C, int i0, int J, int Jv,
+                                           bool act, double* red) {
+  constexpr int kB = (NC == 2) ? NQ : 1;  // imaginary parts (complex panels only)
+  double a[NQ], b[kB];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) a[q] = 0.0;
+#pragma unroll
+  for (int q = 0; q < kB; ++q) b[q] = 0.0;
+  if (act) {
+    const int ilast = (Jv > 0) ? Jv - 1 : 0;
+    for (int64_t row = r0 + rg; row < r1; row += RG) {
+      const size_t off = size_t(row) * C;
+      const double w = widen(W[off + c]);
+      const double wx = (NC == 2) ? widen(W[off + (c ^ 1)]) : 0.0;
+      S v[NQ];
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        const int i = (i0 + q < Jv) ? i0 + q : ilast;
+        v[q] = V[size_t(i) * vstride + off + c];
+      }
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        if (i0 + q < J) {
+          const double vq = (i0 + q < Jv) ? widen(v[q]) : w;
+          a[q] = fma(vq, w, a[q]);
+          if (NC == 2) b[q % kB] = fma(vq, wx, b[q % kB]);
+        }
+      }
+    }
+  }
+  if (rg < RG) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      red[((rg * kIC + q) * 2 + 0) * C + c] = act ? a[q] : 0.0;
+      red[((rg * kIC + q) * 2 + 1) * C + c] = (act && NC == 2) ? b[q % kB] : 0.0;
+    }
+  }
+}
+
+// Partial dots of W against the basis vectors 0 .. J-1 (and W itself when
+// self = 1) per block, in chunks of up to kIC vectors; a chunk of nq
+// vectors runs the code for the next power of two >= nq, so that a short
+// pass does not pay for kIC loads a row.
 template <typename S, int NC>
 __global__ void __launch_bounds__(kT, sizeof(S) == 4 ? LGT_MD_MINB_F32 : LGT_MD_MINB) k_multidot(const S* __restrict__ V, size_t vstride,
                                                  const int* jstate, int jfixed,
@@ -115,63 +165,19 @@ __global__ void __launch_bounds__(kT, sizeof(S) == 4 ? LGT_MD_MINB_F32 : LGT_MD_
   const bool act = rg < RG && (!need || need[c / ncomp] != 0);
   const int64_t r0 = int64_t(blockIdx.x) * rpb;
   const int64_t r1 = (r0 + rpb < N) ? r0 + rpb : N;
-  constexpr int kB = (NC == 2) ? kIC : 1;  // imaginary parts (complex panels only)
   for (int i0 = 0; i0 < J; i0 += kIC) {
-    double a[kIC], b[kB];
-#pragma unroll
-    for (int q = 0; q < kIC; ++q) a[q] = 0.0;
-#pragma unroll
-    for (int q = 0; q < kB; ++q) b[q] = 0.0;
-    if (act) {
-      for (int64_t row = r0 + rg; row < r1; row += RG) {
-        const size_t off = size_t(row) * C;
-        const double w = widen(W[off + c]);
-        const double wx = (NC == 2) ? widen(W[off + (c ^ 1)]) : 0.0;
-#if LGT_MD_HOIST
-        // every load of the chunk is issued before the first use; slots past
-        // the basis read its last vector again (an L1 hit) and are skipped.
-        // The loads stay in the storage type until their FMA (widened FP32
-        // values would hold twice the registers and spill).
-        S v[kIC];
-        const int ilast = (Jv > 0) ? Jv - 1 : 0;
-#pragma unroll
-        for (int q = 0; q < kIC; ++q) {
-          const int i = (i0 + q < Jv) ? i0 + q : ilast;
-          v[q] = V[size_t(i) * vstride + off + c];
-        }
-#pragma unroll
-        for (int q = 0; q < kIC; ++q) {
-          if (i0 + q < J) {
-            const double vq = (i0 + q < Jv) ? widen(v[q]) : w;
-            a[q] = fma(vq, w, a[q]);
-            if (NC == 2) b[q % kB] = fma(vq, wx, b[q % kB]);
-          }
-        }
-#else
-#pragma unroll
-        for (int q = 0; q < kIC; ++q) {
-          if (i0 + q < J) {
-            const double vq = (i0 + q < Jv) ? widen(V[size_t(i0 + q) * vstride + off + c]) : w;
-            a[q] = fma(vq, w, a[q]);
-            if (NC == 2) b[q % kB] = fma(vq, wx, b[q % kB]);
-          }
-        }
-#endif
-      }
-#pragma unroll
-      for (int q = 0; q < kIC; ++q) {
-        red[((rg * kIC + q) * 2 + 0) * C + c] = a[q];
-        red[((rg * kIC + q) * 2 + 1) * C + c] = (NC == 2) ? b[q % kB] : 0.0;
-      }
-    } else if (rg < RG) {
-#pragma unroll
-      for (int q = 0; q < kIC; ++q) {
-        red[((rg * kIC + q) * 2 + 0) * C + c] = 0.0;
-        red[((rg * kIC + q) * 2 + 1) * C + c] = 0.0;
-      }
-    }
+    const int nq = (J - i0 < kIC) ? J - i0 : kIC;
+    const int nq2 = nq <= 1 ? 1 : nq <= 2 ? 2 : nq <= 4 ? 4 : kIC;
+    if (nq2 == 1)
+      dots_chunk<S, NC, 1>(V, vstride, W, r0, r1, rg, RG, c, C, i0, J, Jv, act, red);
+    else if (nq2 == 2)
+      dots_chunk<S, NC, 2>(V, vstride, W, r0, r1, rg, RG, c, C, i0, J, Jv, act, red);
+    else if (nq2 == 4)
+      dots_chunk<S, NC, 4>(V, vstride, W, r0, r1, rg, RG, c, C, i0, J, Jv, act, red);
+    else
+      dots_chunk<S, NC, kIC>(V, vstride, W, r0, r1, rg, RG, c, C, i0, J, Jv, act, red);
     __syncthreads();
-    for (int q = threadIdx.x; q < kIC * 2 * C; q += kT) {
+    for (int q = threadIdx.x; q < nq2 * 2 * C; q += kT) {
       double s = 0.0;
       for (int g = 0; g < RG; ++g) s += red[g * kIC * 2 * C + q];
       const int ii = q / (2 * C);
