@@ -99,11 +99,13 @@ lgt_status upload_couplings(lgt_ham* h) {
     cd[3 * K + k] = -(1.0 / (2.0 * (g * g)));  // matter_gauge_entanglement_pjw.jl:131,142-143
   }
   for (size_t i = 0; i < cd.size(); ++i) cf[i] = float(cd[i]);
+  // Copies from pageable memory stage the host data before they return, and
+  // every kernel that reads the coefficients runs later on the same stream:
+  // no synchronisation needed here.
   CUDA_OR_FAIL(cudaMemcpyAsync(h->coef_d, cd.data(), sizeof(double) * cd.size(),
                                cudaMemcpyHostToDevice, h->b->B.stream));
   CUDA_OR_FAIL(cudaMemcpyAsync(h->coef_f, cf.data(), sizeof(float) * cf.size(),
                                cudaMemcpyHostToDevice, h->b->B.stream));
-  CUDA_OR_FAIL(cudaStreamSynchronize(h->b->B.stream));
   return LGT_OK;
 }
 
