@@ -144,16 +144,31 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// Block-wide sum of one double per thread (all threads get the result).
-__device__ double block_sum(double v, double* red) {
-  v = warp_sum(v);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+// Block-wide sum of one double per thread (all threads get the result):
+// the values go to shared memory and warp 0 alone adds them (lanes over
+// every 32nd value, then a shuffle tree), so one warp, not all of them,
+// spends FP64 instructions on the reduction (GB300's FP64 pipe is narrow).
+// With root, thread 0 also stores sqrt(sum) in out[1] and 1 / sqrt(sum) in
+// out[2] (the norm and its reciprocal, computed once for the block).
+// red: blockDim.x doubles; out: 3 doubles.
+__device__ double block_sum(double v, double* red, double* out, bool root = false) {
+  const int tid = threadIdx.x;
+  red[tid] = v;
   __syncthreads();
-  if (lane == 0) red[wid] = v;
+  if (tid < 32) {
+    double s = 0.0;
+    for (int i = tid; i < int(blockDim.x); i += 32) s += red[i];
+    s = warp_sum(s);
+    if (tid == 0) {
+      out[0] = s;
+      if (root) {
+        out[1] = sqrt(s);
+        out[2] = 1.0 / out[1];
+      }
+    }
+  }
   __syncthreads();
-  double s = 0.0;
-  for (int w = 0; w < nw; ++w) s += red[w];
-  return s;
+  return out[0];
 }
 
 // One ground-state solve per CTA.  S: storage/matvec precision of the
@@ -165,7 +180,8 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
   extern __shared__ __align__(16) unsigned char s_basis[];  // (m + 1) x N when prm.v_smem
   __shared__ double s_alpha[kMaxM + 1], s_beta[kMaxM + 1], s_h[kMaxM + 1], s_z[kMaxM + 1];
   __shared__ double s_part[kMaxM + 1][kWarpsCta];
-  __shared__ double s_red[kWarpsCta];
+  __shared__ double s_red[kCta];
+  __shared__ double s_sum[3];  // block_sum results: sum, sqrt, 1 / sqrt
   __shared__ double s_work[3 * kMaxM];
   __shared__ double s_theta, s_resid;
   __shared__ int s_flag, s_zwarm;
@@ -192,7 +208,8 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
                    : 0.0;
     nrm += w[i] * w[i];
   }
-  nrm = sqrt(block_sum(nrm, s_red));
+  block_sum(nrm, s_red, s_sum, true);
+  nrm = s_sum[1];
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const int r = tid + i * nthr;
@@ -239,7 +256,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
         double s0 = 0.0;
 #pragma unroll
         for (int i = 0; i < R; ++i) s0 = fma(w[i], w[i], s0);
-        nb = block_sum(s0, s_red);
+        nb = block_sum(s0, s_red, s_sum, true);  // sqrt kept for reorth = 0
       }
       double ss = nb;
       for (int pass = 0; pass < prm.reorth; ++pass) {
@@ -300,11 +317,12 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
         double s1 = 0.0;
 #pragma unroll
         for (int i = 0; i < R; ++i) s1 = fma(w[i], w[i], s1);
-        ss = block_sum(s1, s_red);
+        ss = block_sum(s1, s_red, s_sum, true);
         if (!(ss < 1e-4 * nb)) break;
         nb = ss;
       }
-      const double beta = sqrt(ss);
+      const double beta = s_sum[1];  // sqrt(ss), from the last pass's block_sum
+      const double rbeta = s_sum[2];
       if (tid == 0) s_beta[j] = beta;
       n = j + 1;
       ++steps;
@@ -314,7 +332,6 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
         exhausted = true;
       } else if (j + 1 < m + 1) {
         S* vn = V + size_t(j + 1) * N;
-        const double rbeta = 1.0 / beta;
 #pragma unroll
         for (int i = 0; i < R; ++i) {
           const int r = tid + i * nthr;
@@ -369,7 +386,8 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
     double s2 = 0.0;
 #pragma unroll
     for (int i = 0; i < R; ++i) s2 = fma(w[i], w[i], s2);
-    const double xn = sqrt(block_sum(s2, s_red));
+    block_sum(s2, s_red, s_sum, true);
+    const double xn = s_sum[1];
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < R; ++i) {
@@ -384,7 +402,8 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
   double s2 = 0.0;
 #pragma unroll
   for (int i = 0; i < R; ++i) s2 = fma(w[i], w[i], s2);
-  const double xn = sqrt(block_sum(s2, s_red));
+  block_sum(s2, s_red, s_sum, true);
+  const double xn = s_sum[1];
   double* X = U.x;
 #pragma unroll
   for (int i = 0; i < R; ++i) {
@@ -412,14 +431,15 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
     }
     ey = fma(w[i], y[i], ey);
   }
-  const double Erq = block_sum(ey, s_red);
+  const double Erq = block_sum(ey, s_red, s_sum);
   double rs = 0.0;
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const double d = y[i] - Erq * w[i];
     rs = fma(d, d, rs);
   }
-  const double rnorm = sqrt(block_sum(rs, s_red));
+  block_sum(rs, s_red, s_sum, true);
+  const double rnorm = s_sum[1];
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const int r = tid + i * nthr;
@@ -467,8 +487,8 @@ cudaError_t launch_cta(const SmallProblem* probs, const SmallUnit* units, int nu
   const int dyn = smem ? int((vbytes + 15) / 16 * 16) : 0;
 #define LGT_CTA_CASE(RR)                                                                    \
   if (R <= RR) {                                                                            \
-    if (dyn > 48 * 1024) {                                                                  \
-      static int attr = 48 * 1024;                                                          \
+    if (dyn > 0) { /* static + dynamic may pass 48 KB: opt in once per case */             \
+      static int attr = 0;                                                                  \
       if (dyn > attr) {                                                                     \
         cudaError_t ea = cudaFuncSetAttribute(k_lanczos_cta<S, RR>,                         \
                                               cudaFuncAttributeMaxDynamicSharedMemorySize,  \
@@ -483,6 +503,7 @@ cudaError_t launch_cta(const SmallProblem* probs, const SmallUnit* units, int nu
   }
   LGT_CTA_CASE(1)
   LGT_CTA_CASE(2)
+  LGT_CTA_CASE(3)
   LGT_CTA_CASE(4)
   LGT_CTA_CASE(8)
   LGT_CTA_CASE(16)
@@ -625,9 +646,10 @@ std::string small_ground_states(const std::vector<SmallJob>& jobs, const SmallPa
   };
   int rows = prm.rows_per_thread;
   if (rows == 0 && !prm.start_given) {
-    // Autotuner: rows per thread R0 (the fewest that fit 512 threads) or
-    // 2 R0 (half the warps), timed on this batch once per (largest sector,
-    // CTAs, precision); the solve then runs with the faster one.
+    // Autotuner: rows per thread R0 (the fewest that fit 512 threads), R0 + 1
+    // or 2 R0 (fewer warps: fewer FP64 instructions per basis vector, less
+    // latency hiding), timed on this batch once per (largest sector, CTAs,
+    // precision); the solve then runs with the fastest.
     static std::mutex mu;
     static std::map<std::tuple<int, int, int>, int> cache;
     const auto key = std::make_tuple(maxN, int(nunits), mixed ? 1 : 0);
@@ -639,9 +661,19 @@ std::string small_ground_states(const std::vector<SmallJob>& jobs, const SmallPa
       const char* en = getenv("LGT_AUTOTUNE");
       const int r0 = (maxN + 511) / 512;
       rows = r0;
-      if (!(en && en[0] == '0') && 2 * r0 <= 16 && (maxN + 2 * r0 - 1) / (2 * r0) >= 64) {
+      // candidates: the rows-per-thread cases R0, R0 + 1 and 2 R0 (rounded up
+      // to an instantiated case), each with at least 64 threads
+      auto round_case = [](int r) { return r <= 3 ? r : (r <= 4 ? 4 : (r <= 8 ? 8 : 16)); };
+      std::vector<int> cand;
+      for (int r : {r0, r0 + 1, 2 * r0}) {
+        const int rc = round_case(r);
+        if (rc <= 16 && (maxN + rc - 1) / rc >= 64 &&
+            std::find(cand.begin(), cand.end(), rc) == cand.end())
+          cand.push_back(rc);
+      }
+      if (!(en && en[0] == '0') && cand.size() > 1) {
         float best = 3e38f;
-        for (int rr : {r0, 2 * r0}) {
+        for (int rr : cand) {
           cudaEventRecord(e0, s);
           cudaError_t ce = launch(rr);
           cudaEventRecord(e1, s);
