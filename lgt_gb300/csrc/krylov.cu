@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(kT) k_update(const S* __restrict__ V, size_t v
         a0 = fma(-h0, widen(v0[oa]), a0);
         b0 = fma(-h0, widen(v0[ob]), b0);
       }
-      const S sa = S(a0 + a1), sb = S(b0 + b1);
+      const S sa = to_storage<S>(a0 + a1), sb = to_storage<S>(b0 + b1);
       W[oa] = sa;
       W[ob] = sb;
       const double wa = widen(sa), wb = widen(sb);
@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(kT) k_update(const S* __restrict__ V, size_t v
         }
       }
       const double w = w0 + w1;
-      const S wst = S(w);
+      const S wst = to_storage<S>(w);
       if (Ju > 0) W[off + c] = wst;
       const double ws = widen(wst);
       nrm = fma(ws, ws, nrm);

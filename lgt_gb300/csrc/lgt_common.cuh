@@ -175,6 +175,34 @@ __device__ __forceinline__ double widen(float f) {
   return __hiloint2double(int(hi), int(m << 29));
 }
 __device__ __forceinline__ double widen(double d) { return d; }
+
+// FP64 -> FP32 rounding to nearest (ties to even) by integer operations on
+// the bit pattern, the counterpart of widen: magnitudes below the FP32
+// normal range (2^-126) become signed zero, those above it infinity; NaN
+// stays NaN.  A mantissa that rounds up to 2^24 carries into the exponent
+// through the addition.
+__device__ __forceinline__ float narrow(double d) {
+  const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(d));
+  const uint32_t sign = uint32_t(u >> 32) & 0x80000000u;
+  const int e = int((u >> 52) & 0x7ffu);
+  const unsigned long long mant = u & 0xfffffffffffffull;
+  if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (mant ? 0x400000u : 0u));
+  const int e32 = e - 1023 + 127;
+  if (e32 <= 0) return __uint_as_float(sign);
+  uint32_t m = uint32_t(mant >> 29);
+  const uint32_t rem = uint32_t(mant & 0x1fffffffull);
+  if (rem > 0x10000000u || (rem == 0x10000000u && (m & 1u))) ++m;
+  uint32_t bits = (uint32_t(e32) << 23) + m;
+  if (e32 >= 255 || bits >= 0x7f800000u) bits = 0x7f800000u;
+  return __uint_as_float(sign | bits);
+}
+
+// A value in the storage type S of a Krylov basis (float: narrow).
+template <typename S>
+__device__ __forceinline__ S to_storage(double d) {
+  if constexpr (sizeof(S) == 4) return narrow(d);
+  else return S(d);
+}
 #endif
 
 }  // namespace lgt

@@ -148,10 +148,11 @@ __device__ __forceinline__ double warp_sum(double v) {
 // the values go to shared memory and warp 0 alone adds them (lanes over
 // every 32nd value, then a shuffle tree), so one warp, not all of them,
 // spends FP64 instructions on the reduction (GB300's FP64 pipe is narrow).
-// With root, thread 0 also stores sqrt(sum) in out[1] and 1 / sqrt(sum) in
-// out[2] (the norm and its reciprocal, computed once for the block).
-// red: blockDim.x doubles; out: 3 doubles.
-__device__ double block_sum(double v, double* red, double* out, bool root = false) {
+// Thread 0 also calls root(sum) before the block reads the result, for
+// scalars that only depend on it (a norm and its reciprocal, computed once
+// for the block instead of by every thread).  red: blockDim.x doubles.
+template <class Root>
+__device__ double block_sum(double v, double* red, double* out, Root root) {
   const int tid = threadIdx.x;
   red[tid] = v;
   __syncthreads();
@@ -161,14 +162,14 @@ __device__ double block_sum(double v, double* red, double* out, bool root = fals
     s = warp_sum(s);
     if (tid == 0) {
       out[0] = s;
-      if (root) {
-        out[1] = sqrt(s);
-        out[2] = 1.0 / out[1];
-      }
+      root(s);
     }
   }
   __syncthreads();
   return out[0];
+}
+__device__ double block_sum(double v, double* red, double* out) {
+  return block_sum(v, red, out, [](double) {});
 }
 
 // One ground-state solve per CTA.  S: storage/matvec precision of the
@@ -182,6 +183,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
   __shared__ double s_part[kMaxM + 1][kWarpsCta];
   __shared__ double s_red[kCta];
   __shared__ double s_sum[3];  // block_sum results: sum, sqrt, 1 / sqrt
+  __shared__ int s_exh;        // the step's Krylov space is exhausted
   __shared__ double s_work[3 * kMaxM];
   __shared__ double s_theta, s_resid;
   __shared__ int s_flag, s_zwarm;
@@ -208,7 +210,12 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
                    : 0.0;
     nrm += w[i] * w[i];
   }
-  block_sum(nrm, s_red, s_sum, true);
+  // thread 0's root: the norm and its reciprocal into s_sum[1], s_sum[2]
+  auto norm_root = [&](double sv) {
+    s_sum[1] = sqrt(sv);
+    s_sum[2] = 1.0 / s_sum[1];
+  };
+  block_sum(nrm, s_red, s_sum, norm_root);
   nrm = s_sum[1];
 #pragma unroll
   for (int i = 0; i < R; ++i) {
@@ -240,7 +247,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
             const S c = (kind == kPlaq) ? cp : ((kind == kHopNeg) ? -ch : ch);
             acc = fma(c, vj[e >> 2], acc);
           }
-          w[i] = double(acc);
+          w[i] = widen(acc);
         } else {
           w[i] = 0.0;
         }
@@ -256,7 +263,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
         double s0 = 0.0;
 #pragma unroll
         for (int i = 0; i < R; ++i) s0 = fma(w[i], w[i], s0);
-        nb = block_sum(s0, s_red, s_sum, true);  // sqrt kept for reorth = 0
+        nb = block_sum(s0, s_red, s_sum);
       }
       double ss = nb;
       for (int pass = 0; pass < prm.reorth; ++pass) {
@@ -317,25 +324,34 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
         double s1 = 0.0;
 #pragma unroll
         for (int i = 0; i < R; ++i) s1 = fma(w[i], w[i], s1);
-        ss = block_sum(s1, s_red, s_sum, true);
+        // beta = ||w||, 1 / beta and the exhaustion test of this step, by
+        // thread 0 (alpha_j is final: the pass's reduction synchronised)
+        ss = block_sum(s1, s_red, s_sum, [&](double sv) {
+          const double b = sqrt(sv);
+          s_sum[1] = b;
+          s_sum[2] = 1.0 / b;
+          double scl = fabs(s_alpha[j]);
+          if (j > 0) scl = fmax(scl, s_beta[j - 1]);
+          s_exh = (b > tiny_rel * fmax(scl, 1.0)) ? 0 : 1;
+        });
         if (!(ss < 1e-4 * nb)) break;
         nb = ss;
       }
-      const double beta = s_sum[1];  // sqrt(ss), from the last pass's block_sum
+      // beta = sqrt(ss) and the exhaustion flag from the last pass's block_sum
+      // (reorth_passes >= 1: at least one pass ran)
+      const double beta = s_sum[1];
       const double rbeta = s_sum[2];
       if (tid == 0) s_beta[j] = beta;
       n = j + 1;
       ++steps;
-      double scl = fabs(s_alpha[j]);
-      if (j > 0) scl = fmax(scl, s_beta[j - 1]);
-      if (!(beta > tiny_rel * fmax(scl, 1.0))) {
+      if (s_exh) {
         exhausted = true;
       } else if (j + 1 < m + 1) {
         S* vn = V + size_t(j + 1) * N;
 #pragma unroll
         for (int i = 0; i < R; ++i) {
           const int r = tid + i * nthr;
-          if (r < N) vn[r] = S(w[i] * rbeta);
+          if (r < N) vn[r] = to_storage<S>(w[i] * rbeta);
         }
       }
       // first check after 2 * check_every steps, then every check_every
@@ -386,7 +402,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
     double s2 = 0.0;
 #pragma unroll
     for (int i = 0; i < R; ++i) s2 = fma(w[i], w[i], s2);
-    block_sum(s2, s_red, s_sum, true);
+    block_sum(s2, s_red, s_sum, norm_root);
     const double xn = s_sum[1];
     __syncthreads();
 #pragma unroll
@@ -402,7 +418,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
   double s2 = 0.0;
 #pragma unroll
   for (int i = 0; i < R; ++i) s2 = fma(w[i], w[i], s2);
-  block_sum(s2, s_red, s_sum, true);
+  block_sum(s2, s_red, s_sum, norm_root);
   const double xn = s_sum[1];
   double* X = U.x;
 #pragma unroll
@@ -438,7 +454,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
     const double d = y[i] - Erq * w[i];
     rs = fma(d, d, rs);
   }
-  block_sum(rs, s_red, s_sum, true);
+  block_sum(rs, s_red, s_sum, norm_root);
   const double rnorm = s_sum[1];
 #pragma unroll
   for (int i = 0; i < R; ++i) {
