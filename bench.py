@@ -44,7 +44,7 @@ RF_NX, RF_NY, RF_K = 4, 4, 8          # roofline panel (4x4 quench, K = 8 comple
 # measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum, --set full,
 # one launch; profiles/k_hpsi_*_4x4_K8_complex.md)
 RF_TRAFFIC_BYTES = {"fixed": int((2.903165 + 0.533069) * 1e9),
-                    "table": int((3.239323 + 0.532817) * 1e9)}
+                    "table": int((3.236144 + 0.532940) * 1e9)}
 L2_FLUSH_BYTES = 512 << 20            # > 129 MB L2
 METRIC = "ground states/s, batched FP32-mixed Lanczos at |dE|/|E|<=1e-10"
 
