@@ -211,9 +211,11 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
     nrm += w[i] * w[i];
   }
   // thread 0's root: the norm and its reciprocal into s_sum[1], s_sum[2]
+  // (one rsqrt: |x| = x^2 * rsqrt(x^2), both within an ulp or two)
   auto norm_root = [&](double sv) {
-    s_sum[1] = sqrt(sv);
-    s_sum[2] = 1.0 / s_sum[1];
+    const double rs = (sv > 0.0) ? rsqrt(sv) : 0.0;
+    s_sum[1] = sv * rs;
+    s_sum[2] = rs;
   };
   block_sum(nrm, s_red, s_sum, norm_root);
   nrm = s_sum[1];
@@ -258,16 +260,12 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
       // prm.reorth) runs only when a pass cancels more than two digits,
       // ||w_after|| < 1e-2 ||w_before||: the rounding error it leaves along the
       // basis is then above eps * 100 relative to w.
-      double nb;
-      {
-        double s0 = 0.0;
-#pragma unroll
-        for (int i = 0; i < R; ++i) s0 = fma(w[i], w[i], s0);
-        nb = block_sum(s0, s_red, s_sum);
-      }
-      double ss = nb;
+      // ||w||^2 before the first pass comes with that pass's dots: w against
+      // itself in slot j + 1 (no separate block reduction)
+      double nb = 0.0, ss = 0.0;
       for (int pass = 0; pass < prm.reorth; ++pass) {
-        for (int b0 = 0; b0 <= j; b0 += 4) {
+        const int jd = (pass == 0) ? j + 1 : j;
+        for (int b0 = 0; b0 <= jd; b0 += 4) {
           double p[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
           for (int i = 0; i < R; ++i) {
@@ -275,7 +273,10 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
             if (r < N) {
 #pragma unroll
               for (int q = 0; q < 4; ++q)
-                if (b0 + q <= j) p[q] = fma(widen(V[size_t(b0 + q) * N + r]), w[i], p[q]);
+                if (b0 + q <= jd) {
+                  const double vq = (b0 + q <= j) ? widen(V[size_t(b0 + q) * N + r]) : w[i];
+                  p[q] = fma(vq, w[i], p[q]);
+                }
             }
           }
           // reduce-scatter over the warp: after the xor-16 and xor-8 steps
@@ -291,10 +292,10 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
           kk += __shfl_xor_sync(0xffffffffu, kk, 2);
           kk += __shfl_xor_sync(0xffffffffu, kk, 1);
           const int qv = lane >> 3;  // lanes 0, 8, 16, 24 hold values 0..3
-          if ((lane & 7) == 0 && b0 + qv <= j) s_part[b0 + qv][wid] = kk;
+          if ((lane & 7) == 0 && b0 + qv <= jd) s_part[b0 + qv][wid] = kk;
         }
         __syncthreads();
-        if (tid <= j) {
+        if (tid <= jd) {
           double s0 = 0.0, s1 = 0.0;
           int ww = 0;
           for (; ww + 1 < nwarps; ww += 2) {
@@ -307,6 +308,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
           if (tid == j) s_alpha[j] = (pass == 0) ? sum : s_alpha[j] + sum;
         }
         __syncthreads();
+        if (pass == 0) nb = ss = s_h[j + 1];
         for (int b0 = 0; b0 <= j; b0 += 4) {
           double h4[4];
 #pragma unroll
@@ -327,9 +329,10 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
         // beta = ||w||, 1 / beta and the exhaustion test of this step, by
         // thread 0 (alpha_j is final: the pass's reduction synchronised)
         ss = block_sum(s1, s_red, s_sum, [&](double sv) {
-          const double b = sqrt(sv);
+          const double rs = (sv > 0.0) ? rsqrt(sv) : 0.0;
+          const double b = sv * rs;
           s_sum[1] = b;
-          s_sum[2] = 1.0 / b;
+          s_sum[2] = rs;
           double scl = fabs(s_alpha[j]);
           if (j > 0) scl = fmax(scl, s_beta[j - 1]);
           s_exh = (b > tiny_rel * fmax(scl, 1.0)) ? 0 : 1;
