@@ -19,6 +19,7 @@ namespace lgt {
 namespace {
 
 constexpr int kT = 256;
+constexpr int kFCh = 8;  // features reduced per round (two barriers a round)
 
 template <typename T, int NC, int MAXF>
 __global__ void __launch_bounds__(kT) k_observe(Geom G, RankView R, const T* __restrict__ x,
@@ -110,18 +111,24 @@ __global__ void __launch_bounds__(kT) k_observe(Geom G, RankView R, const T* __r
       }
     }
   }
-  // reduce the row subgroups, one feature at a time
+  // reduce the row subgroups, kFCh features a round: red[q][thread], then
+  // thread (q, k) adds subgroups g = 0 .. RS-1 in order for feature f0 + q
   __syncthreads();
   double* red = reinterpret_cast<double*>(smem);
 #pragma unroll
-  for (int f = 0; f < MAXF; ++f) {
-    if (f < nfeat) {
-      red[threadIdx.x] = worker ? acc[f] : 0.0;
+  for (int f0 = 0; f0 < MAXF; f0 += kFCh) {
+    if (f0 < nfeat) {
+#pragma unroll
+      for (int q = 0; q < kFCh; ++q)
+        red[q * kT + threadIdx.x] = (worker && f0 + q < nfeat) ? acc[f0 + q] : 0.0;
       __syncthreads();
-      if (threadIdx.x < K) {
-        double s = 0.0;
-        for (int g = 0; g < RS; ++g) s += red[g * K + threadIdx.x];
-        part[(size_t(blockIdx.x) * K + threadIdx.x) * nfeat + f] = s;
+      for (int t = threadIdx.x; t < kFCh * K; t += kT) {
+        const int q = t / K, kk = t - q * K;
+        if (f0 + q < nfeat) {
+          double s = 0.0;
+          for (int g = 0; g < RS; ++g) s += red[q * kT + g * K + kk];
+          part[(size_t(blockIdx.x) * K + kk) * nfeat + f0 + q] = s;
+        }
       }
       __syncthreads();
     }
@@ -148,7 +155,8 @@ cudaError_t launch_obs3(const Geom& G, const RankView& R, const T* x, int K, int
                         int64_t rpb, double* part, int* err, cudaStream_t s) {
   const size_t sh0 = 32 * 33 * 4 + kT * 4 + size_t((kT * G.ns + 15) / 16) * 16 +
                      size_t(kT) * (G.nP > 0 ? G.nP : 1) * 4;
-  const size_t sh = sh0 > kT * sizeof(double) ? sh0 : kT * sizeof(double);
+  const size_t shr = size_t(kFCh) * kT * sizeof(double);  // the reduction's rounds
+  const size_t sh = sh0 > shr ? sh0 : shr;
   auto kern = k_observe<T, NC, MAXF>;
   static size_t attr_bytes = 48 * 1024;
   if (sh > attr_bytes) {
