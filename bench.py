@@ -42,7 +42,7 @@ G_LO, G_HI, T_HOP, MASS = 0.5, 2.0, 1.0, 0.5
 RF_NX, RF_NY, RF_K = 4, 4, 8          # roofline panel (4x4 quench, K = 8 complex)
 # DRAM bytes of one such launch (FP32, reference model) per kernel family,
 # measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum, --set full,
-# one launch; profiles/k_hpsi_*_4x4_K8_complex.md)
+# one launch of each kernel on this panel)
 RF_TRAFFIC_BYTES = {"fixed": int((2.903165 + 0.533069) * 1e9),
                     "table": int((3.236144 + 0.532940) * 1e9)}
 L2_FLUSH_BYTES = 512 << 20            # > 129 MB L2

@@ -1,6 +1,6 @@
 """GPU parity: the CUDA library against the CPU oracle, through the C ABI.
 
-Bars (see DESIGN.md): basis, keys, ranks, nonzero pattern and signs
+Bars: basis, keys, ranks, nonzero pattern and signs
 bit-exact; CSR values bit-exact (same summation order as the reference);
 H*psi within 1e-12 relative (FP64) / 2e-6 relative (FP32); energies within
 1e-10 relative and observables within 1e-9 absolute of the FP64 oracle.
