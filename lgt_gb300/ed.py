@@ -499,16 +499,19 @@ _OBS_FIELDS = ("t", "nf_mean", "nf_even", "nf_odd", "E2_mean", "plaq_mean", "n_s
 
 def _obs_dicts(basis, K, nf, e2, pl, summ):
     """All K measurement dicts at once: grids as [nx, ny] views of one
-    transposed array per observable, summaries through a numpy view of the
-    lgt_obs array (no per-field ctypes access)."""
+    transposed array per observable (taken by iterating it), summaries
+    through a numpy view of the lgt_obs array (no per-field ctypes access),
+    each dict built as one display with the fields of lgt_obs in order."""
     nx, ny = basis.nx, basis.ny
-    nf_g = nf.reshape(K, ny, nx).transpose(0, 2, 1).copy()
-    e2_g = e2.reshape(K, ny, nx).transpose(0, 2, 1).copy()
+    nf_g = list(nf.reshape(K, ny, nx).transpose(0, 2, 1).copy())
+    e2_g = list(e2.reshape(K, ny, nx).transpose(0, 2, 1).copy())
     pnx, pny = max(nx - 1, 0), max(ny - 1, 0)
-    pl_g = pl[:K * pnx * pny].reshape(K, pny, pnx).transpose(0, 2, 1).copy()
+    pl_g = list(pl[:K * pnx * pny].reshape(K, pny, pnx).transpose(0, 2, 1).copy())
     sm = np.frombuffer(summ, dtype=np.float64).reshape(K, len(_OBS_FIELDS)).tolist()
-    return [dict(zip(_OBS_FIELDS, sm[k]), nf_grid=nf_g[k], E2_grid=e2_g[k], plaq_grid=pl_g[k])
-            for k in range(K)]
+    return [{"t": r[0], "nf_mean": r[1], "nf_even": r[2], "nf_odd": r[3], "E2_mean": r[4],
+             "plaq_mean": r[5], "n_stag": r[6], "norm2": r[7],
+             "nf_grid": a, "E2_grid": b, "plaq_grid": c}
+            for r, a, b, c in zip(sm, nf_g, e2_g, pl_g)]
 
 
 def measure_ED(psi, states: Basis, nx=None, ny=None, dg=None, t_now: float = 0.0):
