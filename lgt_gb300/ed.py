@@ -236,12 +236,19 @@ def build_basis(nx: int, ny: int, dg: int, g_charges, device: int = -1):
 # ---------------------------------------------------------------------------
 
 def _as_points(g, t, m):
-    g = np.atleast_1d(np.asarray(g, dtype=np.float64))
-    t = np.atleast_1d(np.asarray(t, dtype=np.float64))
-    m = np.atleast_1d(np.asarray(m, dtype=np.float64))
-    K = max(g.size, t.size, m.size)
-    g, t, m = (np.ascontiguousarray(np.broadcast_to(a, (K,))) for a in (g, t, m))
-    return K, g, t, m
+    """(K, g[K], t[K], m[K]) as contiguous float64 arrays: each coupling is a
+    scalar (or one value), repeated, or an array of the K points."""
+    arrs = [np.atleast_1d(np.asarray(a, dtype=np.float64)) for a in (g, t, m)]
+    K = max(a.size for a in arrs)
+    out = []
+    for a in arrs:
+        if a.ndim == 1 and a.size == K:
+            out.append(np.ascontiguousarray(a))
+        elif a.size == 1:
+            out.append(np.full(K, a.flat[0]))
+        else:
+            raise ValueError("couplings of %d and %d points cannot be combined" % (a.size, K))
+    return (K, *out)
 
 
 class Hamiltonian:

@@ -41,3 +41,17 @@ def test_obs_dicts_layout():
             for ix in range(nx - 1):
                 for iy in range(ny - 1):
                     assert d["plaq_grid"][ix, iy] == pl[k * npl + iy * (nx - 1) + ix]
+
+
+def test_coupling_points_broadcast():
+    K, g, t, m = ed._as_points([0.5, 1.0, 2.0], 1.0, np.array([0.1]))
+    assert K == 3 and g.tolist() == [0.5, 1.0, 2.0]
+    assert t.tolist() == [1.0] * 3 and m.tolist() == [0.1] * 3
+    assert all(a.dtype == np.float64 and a.flags.c_contiguous for a in (g, t, m))
+    K, g, t, m = ed._as_points(0.8, 1.0, 0.3)
+    assert K == 1 and (g[0], t[0], m[0]) == (0.8, 1.0, 0.3)
+    K, g, t, m = ed._as_points(np.arange(4)[::2] + 1.0, [1, 1], 0.0)  # strided input
+    assert g.tolist() == [1.0, 3.0] and g.flags.c_contiguous and t.dtype == np.float64
+    import pytest
+    with pytest.raises(ValueError):
+        ed._as_points([1.0, 2.0], [1.0, 2.0, 3.0], 0.0)
