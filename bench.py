@@ -61,14 +61,18 @@ def points(rank: int = 0):
 def _cpu_point(args):
     """basis + H + Lanczos ground state + measure for one coupling point,
     the span gs_benchmark.jl:116-125 times (eigsolve settings of
-    finite_ed.jl:336-338: krylovdim 50, tol 1e-10, lowest)."""
-    g, seed = args
+    finite_ed.jl:336-338: krylovdim 50, tol 1e-10, lowest).  args: (g, seed)
+    on the headline lattice, or (nx, ny, g, m, seed)."""
+    if len(args) == 2:
+        (g, seed), (nx, ny, m) = args, (NX, NY, MASS)
+    else:
+        nx, ny, g, m, seed = args
     from scipy.sparse.linalg import eigsh
 
     from oracle import oracle as O
     t0 = time.perf_counter()
-    b = O.build_basis(NX, NY, DG, O.staggered_charges(NX, NY))
-    H = O.build_hamiltonian(b, g=g, t=T_HOP, m=MASS, model="ref")
+    b = O.build_basis(nx, ny, DG, O.staggered_charges(nx, ny))
+    H = O.build_hamiltonian(b, g=g, t=T_HOP, m=m, model="ref")
     v0 = np.random.default_rng(seed).standard_normal(b.dim)
     w, v = eigsh(H, k=1, which="SA", tol=1e-10, ncv=min(50, b.dim), v0=v0)
     O.measure(v[:, 0], b)
@@ -243,22 +247,39 @@ def gpu_workloads(args, rank, world):
     Hp.close()
 
     # ---- end to end through the public API, host buffers ----------------------
-    e2e_times = []
-    h2d = d2h = 0
+    # (a) span-matched: every step builds the basis and the Hamiltonian, then
+    # solves and measures, the span gs_benchmark.jl:116-125 times per point
+    # and the CPU arm times here; (b) the same with the basis and Hamiltonian
+    # handles kept across steps (a sweep that only changes couplings).
+    e2e_times, e2e_reuse = [], []
     C.check(lib.lgt_basis_set_stream(states.handle, None))
     for it in range(args.warmup + args.steps):
         flush.fill_(float(it))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        H.set_couplings(g=gs, t=T_HOP, m=MASS)                       # H2D: couplings
-        E0, P = L.find_ground_state(H, precision="fp32_mixed", as_complex=False)  # D2H: E0, psi
-        obs = L.measure_ED(P, states, NX, NY, DG, 0.0)               # H2D psi, D2H grids
+        st, kd = L.build_basis(NX, NY, DG, g_ch, device=dev)               # H2D: charges
+        Hs = L.build_hamiltonian(st, kd, NX, NY, DG, g=gs, t=T_HOP, m=MASS)  # H2D: couplings
+        E0, P = L.find_ground_state(Hs, precision="fp32_mixed", as_complex=False)  # D2H: E0, psi
+        obs = L.measure_ED(P, st, NX, NY, DG, 0.0)                          # H2D psi, D2H grids
+        Hs.close()
+        st.close()
         dt_ = time.perf_counter() - t0
         if it >= args.warmup:
             e2e_times.append(dt_)
-    h2d = 3 * KPTS * 8 + N * KPTS * 8
-    d2h = KPTS * 8 * 2 + N * KPTS * 8 + KPTS * (2 * NX * NY + (NX - 1) * (NY - 1)) * 8 + KPTS * 64
     dE_e2e = float(np.max(np.abs(E0 - E_ref) / np.abs(E_ref)))
+    for it in range(args.warmup + args.steps):
+        flush.fill_(float(it))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        H.set_couplings(g=gs, t=T_HOP, m=MASS)
+        E0, P = L.find_ground_state(H, precision="fp32_mixed", as_complex=False)
+        obs = L.measure_ED(P, states, NX, NY, DG, 0.0)
+        dt_ = time.perf_counter() - t0
+        if it >= args.warmup:
+            e2e_reuse.append(dt_)
+    dE_e2e = max(dE_e2e, float(np.max(np.abs(E0 - E_ref) / np.abs(E_ref))))
+    h2d = NX * NY * 4 + 3 * KPTS * 8 + N * KPTS * 8
+    d2h = KPTS * 8 * 2 + N * KPTS * 8 + KPTS * (2 * NX * NY + (NX - 1) * (NY - 1)) * 8 + KPTS * 64
     _ = obs
     H.close()
 
@@ -268,7 +289,8 @@ def gpu_workloads(args, rank, world):
     states.close()
     return dict(t_mix=t_mix, dE_mix=dE_mix, launches=launches, clocks=clocks, info_mix=info_mix,
                 t_b64=t_b64, dE_b64=dE_b64, plain_times=plain_times, dE_plain=dE_plain,
-                t_pjw=t_pjw, dE_pjw=dE_pjw, e2e_times=e2e_times, h2d=h2d, d2h=d2h,
+                t_pjw=t_pjw, dE_pjw=dE_pjw, e2e_times=e2e_times, e2e_reuse=e2e_reuse,
+                h2d=h2d, d2h=d2h,
                 dE_e2e=dE_e2e, basis_ms=basis_ms, N=N, rf=rf, quench=qn,
                 matvecs_mix=info_mix.matvecs, restarts_mix=info_mix.restarts)
 
@@ -310,18 +332,24 @@ def gs_only(args):
     return {"gs_per_s": KPTS / statistics.mean(ts), "ms_per_step": 1e3 * statistics.mean(ts)}
 
 
-def quench(L, C, lib, torch, stream, dev, n_steps=5):
+def quench(L, C, lib, torch, stream, dev, n_steps=100):
     """4x4 real-time quench panel: K = 8 points g ~ U[0.5, 1.5] (seed 0), m = 0.5,
     t = 1, from the staggered product state, dt = 0.05; n_steps Krylov
-    exp(-iH dt) steps with observables every step, FP64 and FP32-mixed."""
+    exp(-iH dt) steps (100: t = 5) with observables every step, FP64 and
+    FP32-mixed.  Reports steps/s, the norm drift (max |1 - ||psi||| before
+    each renormalisation), the energy drift at the end, and the largest
+    difference between the FP32-mixed and FP64 trajectories of <E^2>,
+    <n_f> and the site grid of <n_f> over all steps and points."""
     b, _ = L.build_basis(RF_NX, RF_NY, DG, L.staggered_charges(RF_NX, RF_NY), device=dev)
     C.check(lib.lgt_basis_set_stream(b.handle, ctypes_ptr(stream.cuda_stream)))
     N = len(b)
+    ns = RF_NX * RF_NY
     gs = np.random.default_rng(0).uniform(0.5, 1.5, RF_K)
     H = L.build_hamiltonian(b, g=gs, t=1.0, m=0.5, model="ref")
     v0 = L.staggered_product_state(b)
     i0 = int(np.argmax(np.abs(v0)))
-    out = {"N": N, "K": RF_K, "dt": 0.05, "steps_timed": n_steps}
+    out = {"N": N, "K": RF_K, "dt": 0.05, "steps_timed": n_steps, "t_end": 0.05 * n_steps}
+    traj = {}
     for prec, code in (("fp64", C.LGT_FP64), ("fp32_mixed", C.LGT_FP32_MIXED)):
         psi = torch.zeros((N, RF_K, 2), dtype=torch.float64, device="cuda")
         psi[i0, :, 0] = 1.0
@@ -332,7 +360,9 @@ def quench(L, C, lib, torch, stream, dev, n_steps=5):
         C.check(lib.lgt_autotune(H.handle, 2, code, ctypes_byref(tune)))
         o = C.defaults(True)
         o.precision = code
-        obs = (C.Obs * ((n_steps + 1) * RF_K))()
+        R = (n_steps + 1) * RF_K
+        obs = (C.Obs * R)()
+        nfg = np.zeros(R * ns)
         drift = np.zeros(RF_K)
         info = C.Info()
         torch.cuda.synchronize()
@@ -340,23 +370,28 @@ def quench(L, C, lib, torch, stream, dev, n_steps=5):
         e1 = torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(stream):
             e0.record(stream)
-            C.check(lib.lgt_expm_steps(H.handle, o, 0.05, n_steps, psi.data_ptr(), obs,
-                                       drift.ctypes.data, C.LGT_DEVICE_PTRS, info))
+            C.check(lib.lgt_expm_steps_grids(H.handle, o, 0.05, n_steps, psi.data_ptr(), obs,
+                                             nfg.ctypes.data, None, None, drift.ctypes.data,
+                                             C.LGT_DEVICE_PTRS, info))
             e1.record(stream)
         e1.synchronize()
         t = e0.elapsed_time(e1) * 1e-3
         e_after = np.zeros(RF_K)
         C.check(lib.lgt_energy(H.handle, psi.data_ptr(), 2, C.LGT_DEVICE_PTRS, e_after.ctypes.data))
+        sm = np.frombuffer(obs, dtype=np.float64).reshape(n_steps + 1, RF_K, 8)
+        traj[prec] = (sm, nfg.reshape(n_steps + 1, RF_K, ns))
         out[prec] = {"quench_steps_per_s": n_steps / t, "s_per_step": t / n_steps,
                      "matvecs_per_step": info.matvecs / n_steps,
                      "max_norm_drift": float(drift.max()),
                      "max_rel_energy_drift": float(np.max(np.abs(e_after - e_before) /
                                                          np.abs(e_before))),
-                     "E2_mean_t_end_point0": obs[n_steps * RF_K].E2_mean,
-                     "autotune": {"hpsi_kernel": L.HPSI_KERNELS[tune.hpsi_kernel],
-                                  "reduce_blocks": tune.reduce_blocks,
-                                  "measured": bool(tune.measured)}}
+                     "E2_mean_t_end_point0": float(sm[-1, 0, 4]),
+                     "hpsi_kernel": L.HPSI_KERNELS[tune.hpsi_kernel]}
         del psi
+    (s64, g64), (s32, g32) = traj["fp64"], traj["fp32_mixed"]
+    out["mixed_vs_fp64_max_abs"] = {"E2_mean": float(np.max(np.abs(s32[..., 4] - s64[..., 4]))),
+                                    "nf_mean": float(np.max(np.abs(s32[..., 1] - s64[..., 1]))),
+                                    "nf_grid": float(np.max(np.abs(g32 - g64)))}
     H.close()
     b.close()
     return out
@@ -433,7 +468,7 @@ def extra_configs(L, pool, dev, reps=3):
         bases.append(bb)
         Hs.append(L.build_hamiltonian(bb, kk, nx, ny, 1, g=g, t=1.0, m=m))
     ts4 = []
-    for it in range(1 + reps):
+    for it in range(1 + 2 * reps):
         t0 = time.perf_counter()
         res4 = L.find_ground_states(Hs, precision="fp32_mixed")
         if it >= 1:
@@ -442,6 +477,13 @@ def extra_configs(L, pool, dev, reps=3):
         H.close()
     for bb in bases:
         bb.close()
+    # C4 on the host cores: the oracle port of the per-point span, one point
+    # per process (after the GPU timing, so the host cores are idle then)
+    c4_jobs = [(nx, ny, float(g[i]), float(m[i]), i)
+               for (nx, ny), (g, m) in zip(C4_LATTICES, pts) for i in range(16)]
+    t0 = time.perf_counter()
+    pool.map(_cpu_point, c4_jobs)
+    c4_cpu_s = time.perf_counter() - t0
     # the oracle's reference values, computed after the timed sections so that
     # the host cores are idle while those run
     ref = pool.map(_oracle_point, jobs)
@@ -462,9 +504,19 @@ def extra_configs(L, pool, dev, reps=3):
     out["c4_uneven_batch"] = {
         "lattices": ["%dx%d" % l for l in C4_LATTICES], "points_per_lattice": 16,
         "rows_total": int(sum(16 * bb for bb in (90, 645, 2443, 72211))),
-        "gs_per_s_incl_host_copies": 64 / statistics.mean(ts4),
+        "gs_per_s_incl_host_copies": 64 / statistics.median(ts4),
+        "gs_per_s_min_max": [64 / max(ts4), 64 / min(ts4)], "repeats": len(ts4),
+        "cpu_baseline_gs_per_s": 64 / c4_cpu_s,
         "max_rel_dE_fp32_mixed": float(np.max(np.abs(got - e4) / np.abs(e4)))}
     return out
+
+
+def _r(x, digits=4):
+    """x rounded to `digits` significant digits (None passes through)."""
+    if x is None:
+        return None
+    x = float(x)
+    return float("%.*g" % (digits, x)) if np.isfinite(x) else x
 
 
 def ctypes_ptr(v):
@@ -546,15 +598,19 @@ def roofline(L, C, lib, torch, stream, dev, reps=10, only=None):
                     tune = C.Tuning()
                     C.check(lib.lgt_autotune(H.handle, 2, code, ctypes_byref(tune)))
                     kernel = L.HPSI_KERNELS[tune.hpsi_kernel]
-                # algorithmic bytes: x read once, y written once, plus the
-                # per-row stream the kernel must read (order keys for the
-                # matrix-free kernels, the stored table for the table kernel)
+                # algorithmic bytes of a batched matvec, 8 N + 2 K N s: the
+                # order keys read once, x read once, y written once, neighbour
+                # gathers counted as cache hits.  The same figure for every
+                # kernel; the stored table's own stream (a design choice, not
+                # compulsory work) is reported beside it.
                 xy = 2 * RF_K * N * s
-                algo = xy + (table_bytes if kernel.startswith("table") else N * 8)
-                out["%s_%s%s" % (model, prec, suffix)] = {
-                    "ms": t * 1e3, "algo_bytes": algo, "gbs": algo / t / 1e9,
-                    "frac": algo / t / 1e9 / peak, "kernel": kernel,
-                    "matrix_free_algo_bytes": xy + N * 8}
+                algo = xy + N * 8
+                rec = {"ms": t * 1e3, "algo_bytes": algo, "gbs": algo / t / 1e9,
+                       "frac": algo / t / 1e9 / peak, "kernel": kernel}
+                if kernel.startswith("table"):
+                    rec["algo_bytes_incl_table"] = xy + table_bytes
+                    rec["frac_incl_table"] = (xy + table_bytes) / t / 1e9 / peak
+                out["%s_%s%s" % (model, prec, suffix)] = rec
                 del x, y
         H.close()
     if saved is None:
@@ -573,8 +629,11 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--quench-steps", type=int, default=4,
-                    help="timed 4x4 quench steps (dt = 0.05; t = 5 needs 100)")
+    ap.add_argument("--quench-steps", type=int, default=100,
+                    help="timed 4x4 quench steps (dt = 0.05; 100 reach t = 5)")
+    ap.add_argument("--detail", default=None,
+                    help="also write every measured figure (roofline variants, per-config "
+                         "detail, quench trajectories' summaries) to this JSON file")
     ap.add_argument("--hpsi-only", default=None, choices=["auto", "generic", "fixed", "table"],
                     help="--part hpsi: time one kernel family on the reference FP32 panel")
     ap.add_argument("--part", default="all", choices=["all", "hpsi", "gs", "quench"],
@@ -676,55 +735,71 @@ def main():
     fam = "table" if dom["kernel"].startswith("table") else "fixed"
     traffic = RF_TRAFFIC_BYTES.get(fam) if dom["kernel"] != "generic" else None
     e2e_val = KPTS / statistics.mean(r["e2e_times"])
+    qn = r["quench"]
+    c3 = extra["c3_4x3_mixed_vs_fp64"]["errors_vs_fp64_oracle"]
+    c4 = extra["c4_uneven_batch"]
     line = {
         "metric": METRIC,
         "value": value, "unit": "GS/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "fp32-mixed (f32 H*psi and Krylov storage, f64 dots/reorth/tridiagonal/RQ)",
+        "dtype": "fp32-mixed (f32 H*psi and Krylov storage; f64-class dots/reorth, f64 "
+                 "tridiagonal/RQ)",
         "data": "synthetic",
         "config": {"workload": workload, "l2": "flushed between steps (512 MB write, untimed)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
-                   "basis_build_ms": r["basis_ms"]},
-        "accuracy": {"max_rel_dE_fp32_mixed": r["dE_mix"], "max_rel_dE_fp64_batched": r["dE_b64"],
-                     "max_rel_dE_fp64_plain": r["dE_plain"], "max_rel_dE_pjw_mixed_8pts": r["dE_pjw"],
-                     "max_rel_dE_e2e": r["dE_e2e"], "reference": "FP64 oracle, dense eigh"},
-        "arms": {
-            "fp32_mixed_batched_gs_per_s": value,
-            "fp64_batched_gs_per_s": KPTS / statistics.mean(r["t_b64"]),
-            "fp64_plain_gs_per_s": 1.0 / statistics.mean(r["plain_times"]),
-            "speedup_vs_plain_fp64": value * statistics.mean(r["plain_times"]),
-            "pjw_fp32_mixed_batched_gs_per_s": KPTS / statistics.mean(r["t_pjw"]),
-            "matvecs_per_solve_mixed": r["matvecs_mix"], "restarts_mixed": r["restarts_mix"],
-        },
-        "roofline": {"kernel": "%s (H*psi, autotuned: %s), 4x4 N=8563545, K=8 complex FP32 "
-                               "(the FP32-mixed quench panel), reference model"
-                               % ("k_hpsi_table" if fam == "table" else "k_hpsi_fixed",
-                                  dom["kernel"]),
-                     "bound": "hbm", "achieved": dom["gbs"], "peak": rf["peak"], "unit": "GB/s",
-                     "frac": dom["frac"], "traffic": traffic,
-                     "traffic_note": "ncu DRAM bytes per launch; neighbour gathers re-read x "
-                                     "from HBM (LRU model of a 100 MB L2: 4.4 misses per row); "
-                                     "algorithmic bytes: x + y + %s"
-                                     % ("the stored neighbour table" if fam == "table"
-                                        else "the order keys"),
-                     "dram_gbs_of_traffic": traffic / (dom["ms"] * 1e-3) / 1e9 if traffic else None,
-                     "dram_frac_of_traffic": traffic / (dom["ms"] * 1e-3) / 1e9 / rf["peak"]
-                     if traffic else None,
-                     "peak_source": rf["peak_src"] + " (MEASURED_PEAKS.json hbm_gbs)",
-                     "algo_bytes_per_launch": dom["algo_bytes"], "ms_per_launch": dom["ms"],
-                     "variants": {k: v for k, v in rf.items() if isinstance(v, dict)}},
-        "quench_4x4": r["quench"],
-        "configs": extra,
-        "cpu_baseline": {"value": cpu_val, "unit": "GS/s", "cores": ncores, "kind": "port",
-                         "sample": "one step: all 64 points, one point per host process; oracle "
-                                   "port of finite_ed.jl (C basis + H, scipy eigsh tol 1e-10 ncv 50)"},
+                   "basis_build_ms": _r(r["basis_ms"])},
+        "roofline": {"kernel": "k_hpsi_%s (%s), 4x4 N=8563545 K=8 complex FP32, ref model"
+                               % (fam, dom["kernel"]),
+                     "bound": "hbm", "achieved": _r(dom["gbs"]), "peak": rf["peak"],
+                     "unit": "GB/s", "frac": _r(dom["frac"]), "traffic": traffic,
+                     "algo_bytes_per_launch": dom["algo_bytes"], "ms_per_launch": _r(dom["ms"]),
+                     "traffic_over_algo": _r(traffic / dom["algo_bytes"]) if traffic else None,
+                     "frac_incl_table": _r(dom.get("frac_incl_table")),
+                     "peak_source": rf["peak_src"]},
+        "cpu_baseline": {"value": _r(cpu_val), "unit": "GS/s", "cores": ncores, "kind": "port",
+                         "sample": "one step (64 points), one point per host process: oracle "
+                                   "basis+H, scipy eigsh tol 1e-10 ncv 50, measure"},
         "e2e": {"value": e2e_val, "unit": "GS/s", "h2d_bytes_per_step": r["h2d"],
                 "d2h_bytes_per_step": r["d2h"],
-                "path": "lgt_gb300.find_ground_state + measure_ED, host numpy buffers"},
+                "path": "build_basis+build_hamiltonian+find_ground_state+measure_ED each step, "
+                        "host numpy buffers",
+                "handles_kept_gs_per_s": _r(KPTS / statistics.mean(r["e2e_reuse"]))},
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],
+        "configs": {
+            "c1_rel_dE": _r(extra["c1_3x2_fp64_tol1e-12"]["rel_dE"]),
+            "c3_4x3": {k: [_r(v["rel_dE0"]), _r(v["abs_dE2"]), _r(v["abs_dn_stag"])]
+                       for k, v in c3.items()},
+            "c3_cols": "rel dE0, abs dE2, abs dn_stag vs FP64 oracle",
+            "c4_gs_per_s": _r(c4["gs_per_s_incl_host_copies"]),
+            "c4_min_max": [_r(v) for v in c4["gs_per_s_min_max"]],
+            "c4_cpu_gs_per_s": _r(c4["cpu_baseline_gs_per_s"]),
+            "c4_max_rel_dE": _r(c4["max_rel_dE_fp32_mixed"])},
+        "quench_4x4": {"K": RF_K, "t_end": qn["t_end"],
+                       "steps_per_s": {p: _r(qn[p]["quench_steps_per_s"])
+                                       for p in ("fp64", "fp32_mixed")},
+                       "norm_drift": {p: _r(qn[p]["max_norm_drift"]) for p in ("fp64", "fp32_mixed")},
+                       "energy_drift": {p: _r(qn[p]["max_rel_energy_drift"])
+                                        for p in ("fp64", "fp32_mixed")},
+                       "mixed_vs_fp64": {k: _r(v) for k, v in qn["mixed_vs_fp64_max_abs"].items()}},
+        "accuracy": {"max_rel_dE_fp32_mixed": _r(r["dE_mix"]),
+                     "max_rel_dE_fp64_batched": _r(r["dE_b64"]),
+                     "max_rel_dE_fp64_plain": _r(r["dE_plain"]),
+                     "max_rel_dE_pjw_mixed_8pts": _r(r["dE_pjw"]),
+                     "max_rel_dE_e2e": _r(r["dE_e2e"]), "vs": "FP64 oracle, dense eigh"},
+        "arms": {
+            "fp32_mixed_batched_gs_per_s": _r(value),
+            "fp64_batched_gs_per_s": _r(KPTS / statistics.mean(r["t_b64"])),
+            "fp64_plain_gs_per_s": _r(1.0 / statistics.mean(r["plain_times"])),
+            "speedup_vs_plain_fp64": _r(value * statistics.mean(r["plain_times"])),
+            "pjw_fp32_mixed_batched_gs_per_s": _r(KPTS / statistics.mean(r["t_pjw"])),
+            "matvecs_per_solve_mixed": r["matvecs_mix"]},
     }
+    if args.detail:
+        with open(args.detail, "w") as f:
+            json.dump({"line": line, "roofline_variants": rf, "quench_4x4": qn,
+                       "configs": extra}, f, indent=1, default=float)
     print(json.dumps(line))
 
 

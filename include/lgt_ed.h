@@ -239,6 +239,18 @@ LGT_API lgt_status lgt_expm_steps(lgt_ham* h, const lgt_krylov_opts* opts, doubl
                           void* psi, lgt_obs* obs, double* norm_drift, uint32_t flags,
                           lgt_info* info);
 
+/* lgt_expm_steps that also returns the site grids of every step's
+   measure_ED record (evolve_ED! keeps the whole record, nf_grid and
+   E2_grid included, for each step: finite_ed.jl:380-386,409,421-422).
+   nf_grid, E2_grid: (n_steps + 1) * K * nx*ny doubles; plaq_grid:
+   (n_steps + 1) * K * (nx-1)*(ny-1) doubles; record (step, k) starts at
+   (step * K + k) times the grid size, each grid column-major.  Any grid
+   pointer may be NULL; with all of them and obs NULL nothing is measured. */
+LGT_API lgt_status lgt_expm_steps_grids(lgt_ham* h, const lgt_krylov_opts* opts, double dt,
+                                        int32_t n_steps, void* psi, lgt_obs* obs,
+                                        double* nf_grid, double* E2_grid, double* plaq_grid,
+                                        double* norm_drift, uint32_t flags, lgt_info* info);
+
 /* measure_ED (finite_ed.jl:369-393) of K states: per point the nx*ny grids
    <n_f> and <E^2> (column-major, point after point) and the (nx-1)*(ny-1)
    plaquette grid <W + W^dag>; any grid pointer may be NULL.  summary: K

@@ -46,7 +46,8 @@ EXPORTS = (
     "lgt_basis_lookup", "lgt_basis_rank", "lgt_basis_destroy", "lgt_basis_set_stream",
     "lgt_launch_count",
     "lgt_ham_create", "lgt_ham_set_couplings", "lgt_ham_nnz", "lgt_ham_export_csr",
-    "lgt_matvec", "lgt_ground_state", "lgt_ground_state_batch", "lgt_expm_steps", "lgt_observe",
+    "lgt_matvec", "lgt_ground_state", "lgt_ground_state_batch", "lgt_expm_steps",
+    "lgt_expm_steps_grids", "lgt_observe",
     "lgt_observe_noalloc", "lgt_energy", "lgt_autotune", "lgt_ham_destroy",
 )
 
@@ -158,6 +159,8 @@ def load(build_if_missing: bool = True):
                                          ctypes.POINTER(Info)]),
         "lgt_expm_steps": (i32, [vp, ctypes.POINTER(KrylovOpts), dbl, i32, vp, vp, vp, u32,
                                  ctypes.POINTER(Info)]),
+        "lgt_expm_steps_grids": (i32, [vp, ctypes.POINTER(KrylovOpts), dbl, i32, vp, vp, vp, vp,
+                                       vp, vp, u32, ctypes.POINTER(Info)]),
         "lgt_observe": (i32, [vp, vp, i32, i32, u32, dbl, vp, vp, vp, vp]),
         "lgt_observe_noalloc": (i32, [vp, vp, i32, i32, dbl, vp, vp, vp, vp]),
         "lgt_energy": (i32, [vp, vp, i32, u32, vp]),

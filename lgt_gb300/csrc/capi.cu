@@ -91,12 +91,16 @@ lgt_status upload_couplings(lgt_ham* h) {
   std::vector<float> cf(4 * size_t(K));
   for (int k = 0; k < K; ++k) {
     const double g = h->g[k], t = h->t[k], m = h->m[k];
-    if (!std::isfinite(g) || !std::isfinite(t) || !std::isfinite(m) || g == 0.0)
-      return fail(LGT_ERR_ARG, "couplings must be finite and g != 0");
+    if (!std::isfinite(g) || !std::isfinite(t) || !std::isfinite(m))
+      return fail(LGT_ERR_ARG, "couplings must be finite");
+    // g = 0 is a valid reference-model point (no electric energy); only the
+    // plaquette's 1/(2 g^2) needs g != 0
+    const bool plaq = (h->model & LGT_MODEL_PLAQ) != 0;
+    if (plaq && g == 0.0) return fail(LGT_ERR_ARG, "the plaquette term needs g != 0");
     cd[k] = (g * g) / 2;             // finite_ed.jl:268,271
     cd[K + k] = m;                   // finite_ed.jl:274
     cd[2 * K + k] = -t;              // finite_ed.jl:293-294,312-313
-    cd[3 * K + k] = -(1.0 / (2.0 * (g * g)));  // matter_gauge_entanglement_pjw.jl:131,142-143
+    cd[3 * K + k] = plaq ? -(1.0 / (2.0 * (g * g))) : 0.0;  // matter_gauge_entanglement_pjw.jl:131,142-143
   }
   for (size_t i = 0; i < cd.size(); ++i) cf[i] = float(cd[i]);
   // Copies from pageable memory stage the host data before they return, and
@@ -727,36 +731,6 @@ lgt_status lgt_ground_state_batch(int32_t nham, lgt_ham* const* hams, const lgt_
 
 void lgt::set_last_error(const std::string& msg) { g_last_error = msg; }
 
-void lgt::summarize_obs(const Geom& G, const double* feat, double t_now, lgt_obs* o) {
-  // measure_ED's means (finite_ed.jl:387-390) plus plaquette / staggered density
-  const int ns = G.ns;
-  double nf = 0, e2 = 0, ne = 0, no = 0, st = 0, pl = 0;
-  int cnt_e = 0, cnt_o = 0;
-  for (int iy = 0; iy < G.ny; ++iy)
-    for (int ix = 0; ix < G.nx; ++ix) {
-      const int s = iy * G.nx + ix;
-      nf += feat[s];
-      e2 += feat[ns + s];
-      if ((ix + iy) % 2 == 0) {
-        ne += feat[s];
-        st += feat[s];
-        ++cnt_e;
-      } else {
-        no += feat[s];
-        st -= feat[s];
-        ++cnt_o;
-      }
-    }
-  for (int q = 0; q < G.nP; ++q) pl += feat[2 * ns + q];
-  o->t = t_now;
-  o->nf_mean = nf / ns;
-  o->nf_even = cnt_e ? ne / cnt_e : NAN;
-  o->nf_odd = cnt_o ? no / cnt_o : NAN;
-  o->E2_mean = e2 / ns;
-  o->plaq_mean = G.nP ? pl / G.nP : 0.0;
-  o->n_stag = st / ns;
-  o->norm2 = feat[2 * ns + G.nP];
-}
 
 namespace {
 
@@ -781,17 +755,31 @@ lgt_status observe_dev(lgt_ham* h, const T* x, int ncomp, std::vector<double>* f
   return LGT_OK;
 }
 
+// Observables after every step: the summaries and, where asked for, the
+// site grids of that step (finite_ed.jl:409,421-422 keep measure_ED's whole
+// record, grids included, for every step).
 struct ObsRecorder : StepObserver {
-  lgt_ham* h;
-  lgt_obs* obs;
-  double dt;
+  lgt_ham* h = nullptr;
+  lgt_obs* obs = nullptr;
+  double* nf_grid = nullptr;
+  double* E2_grid = nullptr;
+  double* plaq_grid = nullptr;
+  double dt = 0.0;
+  bool wanted() const { return obs || nf_grid || E2_grid || plaq_grid; }
   std::string on_step(int step, const double* X) override {
-    if (!obs) return std::string();
+    if (!wanted()) return std::string();
     std::vector<double> feat;
     if (observe_dev<double>(h, X, 2, &feat) != LGT_OK) return std::string(lgt_last_error());
-    const int nf = observe_nfeat(h->b->B.G);
-    for (int k = 0; k < h->K; ++k)
-      summarize_obs(h->b->B.G, feat.data() + size_t(k) * nf, step * dt, obs + size_t(step) * h->K + k);
+    const Geom& G = h->b->B.G;
+    const int nf = observe_nfeat(G);
+    for (int k = 0; k < h->K; ++k) {
+      const double* f = feat.data() + size_t(k) * nf;
+      const size_t rec = size_t(step) * h->K + k;
+      if (obs) summarize_obs(G, f, step * dt, obs + rec);
+      if (nf_grid) std::memcpy(nf_grid + rec * G.ns, f, sizeof(double) * G.ns);
+      if (E2_grid) std::memcpy(E2_grid + rec * G.ns, f + G.ns, sizeof(double) * G.ns);
+      if (plaq_grid && G.nP) std::memcpy(plaq_grid + rec * G.nP, f + 2 * G.ns, sizeof(double) * G.nP);
+    }
     return std::string();
   }
 };
@@ -803,6 +791,14 @@ extern "C" {
 lgt_status lgt_expm_steps(lgt_ham* h, const lgt_krylov_opts* opts, double dt, int32_t n_steps,
                           void* psi, lgt_obs* obs, double* norm_drift, uint32_t flags,
                           lgt_info* info) {
+  return lgt_expm_steps_grids(h, opts, dt, n_steps, psi, obs, nullptr, nullptr, nullptr,
+                              norm_drift, flags, info);
+}
+
+lgt_status lgt_expm_steps_grids(lgt_ham* h, const lgt_krylov_opts* opts, double dt,
+                                int32_t n_steps, void* psi, lgt_obs* obs, double* nf_grid,
+                                double* E2_grid, double* plaq_grid, double* norm_drift,
+                                uint32_t flags, lgt_info* info) {
   if (!h || !psi) return fail(LGT_ERR_ARG, "null argument");
   if (n_steps < 0 || !std::isfinite(dt)) return fail(LGT_ERR_ARG, "bad dt or n_steps");
   KrylovParams p = to_params(opts, 1);
@@ -823,10 +819,13 @@ lgt_status lgt_expm_steps(lgt_ham* h, const lgt_krylov_opts* opts, double dt, in
   ObsRecorder rec;
   rec.h = h;
   rec.obs = obs;
+  rec.nf_grid = nf_grid;
+  rec.E2_grid = E2_grid;
+  rec.plaq_grid = plaq_grid;
   rec.dt = dt;
   KrylovReport rep;
-  std::string m = krylov_expm(h->op(), p, h->cache, dt, n_steps, X, norm_drift, obs ? &rec : nullptr,
-                              s, &rep);
+  std::string m = krylov_expm(h->op(), p, h->cache, dt, n_steps, X, norm_drift,
+                              rec.wanted() ? &rec : nullptr, s, &rep);
   if (info) {
     info->matvecs = rep.matvecs;
     info->restarts = rep.restarts;

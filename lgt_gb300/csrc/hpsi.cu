@@ -218,13 +218,9 @@ template <typename T, int V, bool PLAQ, bool JW>
 cudaError_t launch_t(const HpsiArgs<T>& a, cudaStream_t s) {
   const SmemLayout L = smem_layout<T>(a.R.nmasks, a.seg_smem, a.K, row_stride(a.G, PLAQ));
   auto kern = k_hpsi<T, V, PLAQ, JW>;
-  // raise the dynamic shared-memory limit once per kernel (outside any graph
-  // capture: the first launch of a configuration is always eager)
-  static int attr_bytes = 48 * 1024;
-  if (L.total > attr_bytes) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total);
+  {
+    cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(kern), L.total);
     if (e != cudaSuccess) return e;
-    attr_bytes = L.total;
   }
   const int64_t blocks = (a.N + kThreads - 1) / kThreads;
   if (blocks <= 0) return cudaSuccess;

@@ -1167,9 +1167,9 @@ std::string tune_hpsi(OpDev* op, const S* x, S* y, int C, int hcomp, cudaStream_
       if (mode >= 3) cand.push_back(kHpsiTable2w);
     }
   }
-  cudaEvent_t e0, e1;
-  KCK(cudaEventCreate(&e0));
-  KCK(cudaEventCreate(&e1));
+  EventPair evp;
+  KCK(evp.create());
+  cudaEvent_t e0 = evp.a, e1 = evp.b;
   int best_v = kHpsiDefault;
   double best = 1e30;
   cudaError_t e = cudaSuccess;
@@ -1189,8 +1189,6 @@ std::string tune_hpsi(OpDev* op, const S* x, S* y, int C, int hcomp, cudaStream_
       best_v = v;
     }
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   if (e != cudaSuccess) return std::string("autotune: ") + cudaGetErrorString(e);
   // A built table stays with the Hamiltonian even when another kernel wins
   // here: graphs captured for its other panel widths may launch from it.
@@ -1231,9 +1229,9 @@ std::string autotune(OpDev* op, Work<S>& w, cudaStream_t s, TuneChoice* out) {
     // H*psi variant (shared with lgt_matvec's choice for this shape)
     std::string err = tune_hpsi<S>(op, w.V, w.W, w.C, w.hcomp, s, &c.hpsi_variant, &c.hpsi_ms);
     if (!err.empty()) return err;
-    cudaEvent_t e0, e1;
-    KCK(cudaEventCreate(&e0));
-    KCK(cudaEventCreate(&e1));
+    EventPair evp;
+    KCK(evp.create());
+    cudaEvent_t e0 = evp.a, e1 = evp.b;
     auto timed = [&](auto&& launch) -> double {  // one warm-up, mean of three
       cudaError_t e = launch();
       if (e == cudaSuccess) e = cudaEventRecord(e0, s);
@@ -1275,8 +1273,6 @@ std::string autotune(OpDev* op, Work<S>& w, cudaStream_t s, TuneChoice* out) {
       }
     }
     c.red_ms = best;
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     if (!err.empty()) return err;
     c.measured = 1;
   }
@@ -1388,10 +1384,9 @@ std::string ground_state_impl(const OpDev& op_in, const KrylovParams& p, Work<S>
   // solve stops there and the Ritz pair is finished in FP64 below.
   const double tol_inner = fp32 ? fmax(p.tol, 2e-5) : p.tol;
 
-  cudaEvent_t ev0, ev1;
-  cudaEventCreate(&ev0);
-  cudaEventCreate(&ev1);
-  cudaEventRecord(ev0, s);
+  EventPair ev;
+  KCK(ev.create());
+  cudaEventRecord(ev.a, s);
   KCK(cudaMemsetAsync(w.status, 0, sizeof(int) * K, s));
   KCK(cudaMemsetAsync(w.len, 0, sizeof(int) * K, s));
   KCK(cudaMemsetAsync(w.fail, 0, sizeof(int), s));
@@ -1470,12 +1465,10 @@ std::string ground_state_impl(const OpDev& op_in, const KrylovParams& p, Work<S>
                                              w.alpha, w.ldT, w.status, w.len, w.bnorm, 0.0, 0), lgt::note_launch();
   KCK(cudaGetLastError());
   KCK(cudaMemcpyAsync(r2.data(), w.bnorm, sizeof(double) * K, cudaMemcpyDeviceToHost, s));
-  cudaEventRecord(ev1, s);
+  cudaEventRecord(ev.b, s);
   KCK(cudaStreamSynchronize(s));
   float ms = 0.f;
-  cudaEventElapsedTime(&ms, ev0, ev1);
-  cudaEventDestroy(ev0);
-  cudaEventDestroy(ev1);
+  cudaEventElapsedTime(&ms, ev.a, ev.b);
   int conv = 0;
   double maxr = 0.0;
   for (int k = 0; k < K; ++k) {
@@ -1532,10 +1525,9 @@ std::string expm_impl(const OpDev& op_in, const KrylovParams& p, Work<S>& w, dou
   int64_t matvecs = 0;
   int substeps = 0;
   double maxerr = 0.0;
-  cudaEvent_t ev0, ev1;
-  cudaEventCreate(&ev0);
-  cudaEventCreate(&ev1);
-  cudaEventRecord(ev0, s);
+  EventPair ev;
+  KCK(ev.create());
+  cudaEventRecord(ev.a, s);
   KCK(cudaMemsetAsync(w.fail, 0, sizeof(int), s));
   if (obs) {
     err = obs->on_step(0, X);
@@ -1581,15 +1573,16 @@ std::string expm_impl(const OpDev& op_in, const KrylovParams& p, Work<S>& w, dou
         // largest tau = remaining / 2^q meeting the tolerance (scaled to the
         // sub-interval) for every column, then continue from there.
         double t = remaining;
-        for (int q = 0; q < 40; ++q) {
+        bool ok = false;
+        for (int q = 0; q < 40 && !ok; ++q) {
           t *= 0.5;
           k_check_expm<<<Kc, 64, 0, s>>>(w.alpha, w.beta, w.ldT, w.status, w.len, w.rho, t,
                                          w.resid, w.coef, tol * (t / dt), 0, w.fail), lgt::note_launch();
-          bool ok = false;
           err = all_converged(&ok);
           if (!err.empty()) return err;
-          if (ok) break;
         }
+        if (!ok)
+          return std::string("NOCONV: no sub-step down to dt / 2^40 meets the tolerance");
         tau = t;
         KCK(cudaMemsetAsync(w.status, 0, sizeof(int) * Kc, s));
         k_check_expm<<<Kc, 64, 0, s>>>(w.alpha, w.beta, w.ldT, w.status, w.len, w.rho, tau,
@@ -1629,12 +1622,10 @@ std::string expm_impl(const OpDev& op_in, const KrylovParams& p, Work<S>& w, dou
   }
   int fail = 0;
   KCK(cudaMemcpyAsync(&fail, w.fail, sizeof(int), cudaMemcpyDeviceToHost, s));
-  cudaEventRecord(ev1, s);
+  cudaEventRecord(ev.b, s);
   KCK(cudaStreamSynchronize(s));
   float ms = 0.f;
-  cudaEventElapsedTime(&ms, ev0, ev1);
-  cudaEventDestroy(ev0);
-  cudaEventDestroy(ev1);
+  cudaEventElapsedTime(&ms, ev.a, ev.b);
   if (rep) {
     rep->matvecs += matvecs;
     rep->restarts += substeps;

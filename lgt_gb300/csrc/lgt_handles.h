@@ -3,7 +3,7 @@
 #pragma once
 
 #include <atomic>
-
+#include <cmath>
 #include <string>
 #include <vector>
 
@@ -39,8 +39,40 @@ struct DevBuf {
 void set_last_error(const std::string& msg);
 
 // measure_ED's means (finite_ed.jl:387-390) plus plaquette and staggered
-// density, from the per-point feature vector of the observables kernel.
-void summarize_obs(const Geom& G, const double* feat, double t_now, lgt_obs* o);
+// density, from the per-point feature vector of the observables kernel
+// (n_f per site, E^2 per site, plaquettes, norm).  One definition for the
+// host summaries of lgt_observe / lgt_expm_steps and the device summaries
+// of lgt_observe_noalloc, so the two cannot drift apart.
+__host__ __device__ inline void summarize_obs(const Geom& G, const double* feat, double t_now,
+                                              lgt_obs* o) {
+  const int ns = G.ns;
+  double nf = 0, e2 = 0, ne = 0, no = 0, st = 0, pl = 0;
+  int cnt_e = 0, cnt_o = 0;
+  for (int iy = 0; iy < G.ny; ++iy)
+    for (int ix = 0; ix < G.nx; ++ix) {
+      const int s = iy * G.nx + ix;
+      nf += feat[s];
+      e2 += feat[ns + s];
+      if ((ix + iy) % 2 == 0) {
+        ne += feat[s];
+        st += feat[s];
+        ++cnt_e;
+      } else {
+        no += feat[s];
+        st -= feat[s];
+        ++cnt_o;
+      }
+    }
+  for (int q = 0; q < G.nP; ++q) pl += feat[2 * ns + q];
+  o->t = t_now;
+  o->nf_mean = nf / ns;
+  o->nf_even = cnt_e ? ne / cnt_e : NAN;
+  o->nf_odd = cnt_o ? no / cnt_o : NAN;
+  o->E2_mean = e2 / ns;
+  o->plaq_mean = G.nP ? pl / G.nP : 0.0;
+  o->n_stag = st / ns;
+  o->norm2 = feat[2 * ns + G.nP];
+}
 
 }  // namespace lgt
 

@@ -257,20 +257,9 @@ template <int NX, int NY, typename T, int LD, bool PLAQ, bool JW>
 cudaError_t launch_shape_v(const HpsiArgs<T>& a, cudaStream_t s) {
   auto kern = k_hpsi_fixed<NX, NY, T, LD, PLAQ, JW>;
   const int bytes = smem_bytes<NX, NY, PLAQ, T>(a.K);
-  static int attr_bytes = 48 * 1024;  // raised once, outside any capture (first launch is eager)
-#ifdef LGT_FIXED_CARVEOUT
-  static bool carve = false;
-  if (!carve) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                         LGT_FIXED_CARVEOUT);
+  {
+    cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(kern), bytes);
     if (e != cudaSuccess) return e;
-    carve = true;
-  }
-#endif
-  if (bytes > attr_bytes) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e != cudaSuccess) return e;
-    attr_bytes = bytes;
   }
   const int64_t blocks = (a.N + kThreads - 1) / kThreads;
   if (blocks <= 0) return cudaSuccess;

@@ -3,7 +3,10 @@
 #pragma once
 
 #include <cstdint>
+#include <map>
+#include <mutex>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -11,6 +14,44 @@
 #include "lgt_common.cuh"
 
 namespace lgt {
+
+// Raises `func`'s dynamic shared-memory limit to at least `bytes` on the
+// current device.  The attribute belongs to the (function, device) pair, so
+// the raised limit is remembered per device, under a lock (host threads of
+// different handles launch concurrently).  The first launch of a
+// configuration is eager, so the attribute call never falls inside a graph
+// capture.
+inline cudaError_t raise_smem_limit(const void* func, int bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, int> raised;
+  std::lock_guard<std::mutex> lock(mu);
+  int& have = raised[std::make_pair(func, dev)];
+  if (bytes <= have) return cudaSuccess;
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) have = bytes;
+  return e;
+}
+
+// Two timing events destroyed with the scope, whatever path leaves it.
+struct EventPair {
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaError_t create() {
+    cudaError_t e = cudaEventCreate(&a);
+    if (e == cudaSuccess) e = cudaEventCreate(&b);
+    return e;
+  }
+  ~EventPair() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+  EventPair() = default;
+  EventPair(const EventPair&) = delete;
+  EventPair& operator=(const EventPair&) = delete;
+};
 
 // Everything a kernel needs to turn an order key into a basis index.
 //

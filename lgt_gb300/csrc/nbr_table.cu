@@ -203,11 +203,9 @@ template <typename T, int LD, bool PLAQ, bool JW>
 cudaError_t launch_table_v(const HpsiArgs<T>& a, cudaStream_t s) {
   auto kern = k_hpsi_table<T, LD, PLAQ, JW>;
   const int bytes = table_smem<T>(a.K, a.t_mm);
-  static int attr_bytes = 48 * 1024;  // raised once, outside any capture (first launch is eager)
-  if (bytes > attr_bytes) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  {
+    cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(kern), bytes);
     if (e != cudaSuccess) return e;
-    attr_bytes = bytes;
   }
   const int64_t blocks = (a.N + kTabThreads - 1) / kTabThreads;
   if (blocks <= 0) return cudaSuccess;

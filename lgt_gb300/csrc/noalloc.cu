@@ -56,42 +56,13 @@ cudaError_t scratch_address(int device, double** out) {
   return cudaSuccess;
 }
 
-// measure_ED's means (finite_ed.jl:387-390) plus plaquette and staggered
-// density, one thread per point, straight into the scratch.
+// Per-point summaries (lgt::summarize_obs, shared with lgt_observe), one
+// thread per point, straight into the scratch.
 __global__ void k_summarize(lgt::Geom G, const double* feat, int K, int nfeat, double t_now,
                             lgt_obs* out) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= K) return;
-  const double* f = feat + size_t(k) * nfeat;
-  const int ns = G.ns;
-  double nf = 0, e2 = 0, ne = 0, no = 0, st = 0, pl = 0;
-  int ce = 0, co = 0;
-  for (int iy = 0; iy < G.ny; ++iy)
-    for (int ix = 0; ix < G.nx; ++ix) {
-      const int s = iy * G.nx + ix;
-      nf += f[s];
-      e2 += f[ns + s];
-      if ((ix + iy) % 2 == 0) {
-        ne += f[s];
-        st += f[s];
-        ++ce;
-      } else {
-        no += f[s];
-        st -= f[s];
-        ++co;
-      }
-    }
-  for (int q = 0; q < G.nP; ++q) pl += f[2 * ns + q];
-  lgt_obs o;
-  o.t = t_now;
-  o.nf_mean = nf / ns;
-  o.nf_even = ce ? ne / ce : NAN;
-  o.nf_odd = co ? no / co : NAN;
-  o.E2_mean = e2 / ns;
-  o.plaq_mean = G.nP ? pl / G.nP : 0.0;
-  o.n_stag = st / ns;
-  o.norm2 = f[2 * ns + G.nP];
-  out[k] = o;
+  lgt::summarize_obs(G, feat + size_t(k) * nfeat, t_now, out + k);
 }
 
 lgt_status fail_na(lgt_status code, const std::string& msg) {
@@ -147,6 +118,8 @@ lgt_status lgt_observe_noalloc(const lgt_ham* h, const void* psi, int32_t ncomp,
                                                ncomp, nblk, rpb, part, feat, b->B.err, s);
   if (e != cudaSuccess) return fail_na(LGT_ERR_CUDA, cudaGetErrorString(e));
   k_summarize<<<(K + 63) / 64, 64, 0, s>>>(G, feat, K, nfeat, t_now, obs), lgt::note_launch();
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return fail_na(LGT_ERR_CUDA, std::string("k_summarize: ") + cudaGetErrorString(e));
   const size_t pitch = size_t(nfeat) * sizeof(double);
   if (nf_grid)
     e = cudaMemcpy2DAsync(nf_grid, sizeof(double) * G.ns, feat, pitch, sizeof(double) * G.ns, K,

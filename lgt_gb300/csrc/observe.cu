@@ -158,11 +158,9 @@ cudaError_t launch_obs3(const Geom& G, const RankView& R, const T* x, int K, int
   const size_t shr = size_t(kFCh) * kT * sizeof(double);  // the reduction's rounds
   const size_t sh = sh0 > shr ? sh0 : shr;
   auto kern = k_observe<T, NC, MAXF>;
-  static size_t attr_bytes = 48 * 1024;
-  if (sh > attr_bytes) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sh));
+  {
+    cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(kern), int(sh));
     if (e != cudaSuccess) return e;
-    attr_bytes = sh;
   }
   kern<<<nblk, kT, sh, s>>>(G, R, x, R.dim, K, nfeat, rpb, part, err), lgt::note_launch();
   return cudaGetLastError();

@@ -506,15 +506,10 @@ cudaError_t launch_cta(const SmallProblem* probs, const SmallUnit* units, int nu
   const int dyn = smem ? int((vbytes + 15) / 16 * 16) : 0;
 #define LGT_CTA_CASE(RR)                                                                    \
   if (R <= RR) {                                                                            \
-    if (dyn > 0) { /* static + dynamic may pass 48 KB: opt in once per case */             \
-      static int attr = 0;                                                                  \
-      if (dyn > attr) {                                                                     \
-        cudaError_t ea = cudaFuncSetAttribute(k_lanczos_cta<S, RR>,                         \
-                                              cudaFuncAttributeMaxDynamicSharedMemorySize,  \
-                                              kCtaSmemMax);                                 \
-        if (ea != cudaSuccess) return ea;                                                   \
-        attr = kCtaSmemMax;                                                                 \
-      }                                                                                     \
+    if (dyn > 0) { /* static + dynamic may pass 48 KB: opt in per device */                \
+      cudaError_t ea = lgt::raise_smem_limit(                                               \
+          reinterpret_cast<const void*>(k_lanczos_cta<S, RR>), kCtaSmemMax);                \
+      if (ea != cudaSuccess) return ea;                                                     \
     }                                                                                       \
     k_lanczos_cta<S, RR><<<nunits, threads_for(RR), dyn, s>>>(probs, units, prm),          \
         lgt::note_launch();                                                                 \
@@ -656,9 +651,9 @@ std::string small_ground_states(const std::vector<SmallJob>& jobs, const SmallPa
                       cudaMemcpyHostToDevice, s));
   SCK(cudaMemcpyAsync(d_units, units.data(), sizeof(SmallUnit) * units.size(),
                       cudaMemcpyHostToDevice, s));
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
+  EventPair evp;
+  SCK(evp.create());
+  cudaEvent_t e0 = evp.a, e1 = evp.b;
   auto launch = [&](int rows) {
     return mixed ? launch_cta<float>(d_probs, d_units, int(nunits), maxN, prm, s, rows)
                  : launch_cta<double>(d_probs, d_units, int(nunits), maxN, prm, s, rows);
@@ -718,8 +713,6 @@ std::string small_ground_states(const std::vector<SmallJob>& jobs, const SmallPa
   SCK(cudaStreamSynchronize(s));
   float ms = 0.f;
   cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   if (seconds) *seconds = ms * 1e-3;
   for (size_t u = 0; u < nunits; ++u) {
     const SmallJob& J = jobs[unit_src[u].first];

@@ -549,7 +549,8 @@ def evolve_ED(psi, H: Hamiltonian, states=None, nx=None, ny=None, dg=None, *, dt
     psi <- exp(-i H dt) psi, renormalised after each, observables measured at
     every step (the reference measures every step and prints every
     ``measure_every``).  Returns the list of measurement dicts (t = step*dt,
-    starting with t = 0); with return_state=True also the final state and
+    starting with t = 0), each with the site grids nf_grid and E2_grid
+    (and plaq_grid) like measure_ED's; with return_state=True also the final state and
     the per-point norm drift.  As in the reference, the caller's psi is not
     modified.  For K > 1, psi is (N, K) and each entry of the list is a list
     of K dicts."""
@@ -561,20 +562,19 @@ def evolve_ED(psi, H: Hamiltonian, states=None, nx=None, ny=None, dg=None, *, dt
     p[..., 0] = np.real(v)
     p[..., 1] = np.imag(v)
     o = _opts(True, tol, krylovdim, maxiter, precision, 0, check_every, 0, use_graph)
-    obs = (C.Obs * ((n_steps + 1) * K))()
+    R = (n_steps + 1) * K
+    obs = (C.Obs * R)()
+    ns, npl = b.nx * b.ny, max((b.nx - 1) * (b.ny - 1), 0)
+    nf = np.zeros(R * ns)
+    e2 = np.zeros(R * ns)
+    pl = np.zeros(max(R * npl, 1))
     drift = np.zeros(K)
     info = C.Info()
-    C.check(C.load().lgt_expm_steps(H.handle, ctypes.byref(o), float(dt), int(n_steps), _p(p),
-                                    obs, _p(drift), 0, ctypes.byref(info)))
-    data = []
-    for s in range(n_steps + 1):
-        row = []
-        for k in range(K):
-            r = obs[s * K + k]
-            row.append(dict(t=r.t, nf_mean=r.nf_mean, nf_even=r.nf_even, nf_odd=r.nf_odd,
-                            E2_mean=r.E2_mean, plaq_mean=r.plaq_mean, n_stag=r.n_stag,
-                            norm2=r.norm2))
-        data.append(row[0] if K == 1 else row)
+    C.check(C.load().lgt_expm_steps_grids(H.handle, ctypes.byref(o), float(dt), int(n_steps),
+                                          _p(p), obs, _p(nf), _p(e2), _p(pl), _p(drift), 0,
+                                          ctypes.byref(info)))
+    recs = _obs_dicts(b, R, nf, e2, pl, obs)
+    data = [recs[s * K] if K == 1 else recs[s * K:(s + 1) * K] for s in range(n_steps + 1)]
     if return_state:
         out = p[..., 0] + 1j * p[..., 1]
         return data, (out[:, 0] if psi.ndim == 1 else out), drift

@@ -209,14 +209,20 @@ end
 function evolve_ED!(ψ::Vector{ComplexF64}, H::Hamiltonian, states::Basis, nx::Int, ny::Int,
                     dg::Int; dt::Float64, n_steps::Int, measure_every::Int=10)
     o = defaults(true)
-    obs = Vector{Obs}(undef, (n_steps + 1) * H.K)
+    R = (n_steps + 1) * H.K
+    obs = Vector{Obs}(undef, R)
+    nf = zeros(Float64, nx * ny, R)
+    e2 = zeros(Float64, nx * ny, R)
     info = Ref{Info}()
     ψw = copy(ψ)   # the reference rebinds ψ inside evolve_ED!, leaving the caller's vector as is
-    check(ccall((:lgt_expm_steps, libpath), Int32,
-                (Ptr{Cvoid}, Ref{KrylovOpts}, Float64, Int32, Ptr{ComplexF64}, Ptr{Obs}, Ptr{Float64}, UInt32, Ref{Info}),
-                H.ptr, Ref(o), dt, n_steps, ψw, obs, C_NULL, 0, info))
-    return [(t=r.t, nf_mean=r.nf_mean, nf_even=r.nf_even, nf_odd=r.nf_odd, E2_mean=r.E2_mean)
-            for r in obs]
+    check(ccall((:lgt_expm_steps_grids, libpath), Int32,
+                (Ptr{Cvoid}, Ref{KrylovOpts}, Float64, Int32, Ptr{ComplexF64}, Ptr{Obs},
+                 Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, UInt32, Ref{Info}),
+                H.ptr, Ref(o), dt, n_steps, ψw, obs, nf, e2, C_NULL, C_NULL, 0, info))
+    return [(t=obs[i].t, nf_mean=obs[i].nf_mean, nf_even=obs[i].nf_even, nf_odd=obs[i].nf_odd,
+             E2_mean=obs[i].E2_mean, nf_grid=reshape(nf[:, i], nx, ny),
+             E2_grid=reshape(e2[:, i], nx, ny))
+            for i in 1:R]
 end
 
 end # module

@@ -423,116 +423,111 @@ static void orc_coo_push(orc_coo* c, int64_t i, int64_t j, double v) {
 }
 
 /*
- * Builds the COO triplets in the reference's push order (0-based).  The
- * caller turns them into CSR/CSC, summing duplicates like SparseArrays'
- * sparse(Is, Js, Vs, N, N) (finite_ed.jl:321); this Hamiltonian has none.
- * Returns NULL on allocation failure or when a hopped state is missing
- * from the basis (which the Gauss law rules out).
+ * The body of the reference's loop over states (finite_ed.jl:262-319) for
+ * one state idx: its diagonal, its forward hops and (model PJW) its
+ * plaquette moves, each move pushing (jdx, idx) and (idx, jdx) as the
+ * reference does.  With only_row >= 0, only the triplets of that row are
+ * kept (the row-restricted build below).  Returns 0, or 1 when a moved
+ * state is missing from the basis (which the Gauss law rules out).
  */
-void* orc_ham_new(const void* hb, int model, double g, double t, double m) {
-    const orc_basis* b = (const orc_basis*)hb;
+static int orc_ham_state(const orc_basis* b, int model, double g, double t, double m,
+                         int64_t idx, int64_t only_row, orc_coo* c) {
     int nx = b->nx, ny = b->ny, dg = b->dg;
     int ns = nx * ny, nr = (nx - 1) * ny, nu = nx * (ny - 1);
-    orc_coo* c = (orc_coo*)calloc(1, sizeof(orc_coo));
-    if (!c) return NULL;
     int8_t wnf[ORC_MAX_SITES], weR[ORC_MAX_SITES], weU[ORC_MAX_SITES];
     const double invg2 = 1.0 / (2.0 * (g * g)); /* matter_gauge_entanglement_pjw.jl:131 */
-    for (int64_t idx = 0; idx < b->n && !c->err; idx++) {
-        const int8_t* snf = b->nf + idx * ns;
-        const int8_t* seR = b->eR + idx * nr;
-        const int8_t* seU = b->eU + idx * nu;
-        /* Diagonal, finite_ed.jl:265-276: same loop, same rounding order. */
-        double E = 0.0;
-        for (int iy = 1; iy <= ny; iy++)
-            for (int ix = 1; ix <= nx; ix++) {
-                if (ix < nx) {
-                    double e = (double)ER(seR, ix, iy);
-                    E += ((g * g) / 2) * (e * e);
-                }
-                if (iy < ny) {
-                    double e = (double)EU(seU, ix, iy);
-                    E += ((g * g) / 2) * (e * e);
-                }
-                int stag = ((ix + iy) % 2 == 0) ? 1 : -1;
-                E += (m * stag) * (double)NF(snf, ix, iy);
+    const int8_t* snf = b->nf + idx * ns;
+    const int8_t* seR = b->eR + idx * nr;
+    const int8_t* seU = b->eU + idx * nu;
+#define ORC_PUSH(i, j, v) \
+    do { if (only_row < 0 || (i) == only_row) orc_coo_push(c, (i), (j), (v)); } while (0)
+    /* Diagonal, finite_ed.jl:265-276: same loop, same rounding order. */
+    double E = 0.0;
+    for (int iy = 1; iy <= ny; iy++)
+        for (int ix = 1; ix <= nx; ix++) {
+            if (ix < nx) {
+                double e = (double)ER(seR, ix, iy);
+                E += ((g * g) / 2) * (e * e);
             }
-        orc_coo_push(c, idx, idx, E);
-        /* Horizontal forward hops, finite_ed.jl:279-297 */
-        for (int iy = 1; iy <= ny; iy++)
-            for (int ix = 1; ix <= nx - 1; ix++) {
-                int e = ER(seR, ix, iy);
-                int nL = NF(snf, ix, iy), nR = NF(snf, ix + 1, iy);
-                if (nL == 0 && nR == 1 && e < dg) {
-                    memcpy(wnf, snf, (size_t)ns);
-                    memcpy(weR, seR, (size_t)nr);
-                    if (nu) memcpy(weU, seU, (size_t)nu);
-                    NF(wnf, ix, iy) = 1;
-                    NF(wnf, ix + 1, iy) = 0;
-                    ER(weR, ix, iy) = (int8_t)(e + 1);
-                    int64_t jdx = orc_map_get(&b->dict, orc_dict_key(b, wnf, weR, weU));
-                    if (jdx < 0) {
-                        c->err = 1;
-                        break;
-                    }
-                    double v = -t;
-                    if (model == ORC_MODEL_PJW) v = -t * orc_jw_sign(nx, ny, snf, ix, iy, ix + 1, iy);
-                    orc_coo_push(c, jdx, idx, v);
-                    orc_coo_push(c, idx, jdx, v);
-                }
+            if (iy < ny) {
+                double e = (double)EU(seU, ix, iy);
+                E += ((g * g) / 2) * (e * e);
             }
-        /* Vertical forward hops, finite_ed.jl:300-318 (chain-adjacent on the
-           column snake, so no Jordan-Wigner string in the PJW model) */
-        for (int iy = 1; iy <= ny - 1; iy++)
-            for (int ix = 1; ix <= nx; ix++) {
-                int e = EU(seU, ix, iy);
-                int nD = NF(snf, ix, iy), nU = NF(snf, ix, iy + 1);
-                if (nD == 0 && nU == 1 && e < dg) {
-                    memcpy(wnf, snf, (size_t)ns);
-                    if (nr) memcpy(weR, seR, (size_t)nr);
-                    memcpy(weU, seU, (size_t)nu);
-                    NF(wnf, ix, iy) = 1;
-                    NF(wnf, ix, iy + 1) = 0;
-                    EU(weU, ix, iy) = (int8_t)(e + 1);
-                    int64_t jdx = orc_map_get(&b->dict, orc_dict_key(b, wnf, weR, weU));
-                    if (jdx < 0) {
-                        c->err = 1;
-                        break;
-                    }
-                    double v = -t;
-                    if (model == ORC_MODEL_PJW) v = -t * orc_jw_sign(nx, ny, snf, ix, iy, ix, iy + 1);
-                    orc_coo_push(c, jdx, idx, v);
-                    orc_coo_push(c, idx, jdx, v);
-                }
-            }
-        /* Magnetic plaquette, matter_gauge_entanglement_pjw.jl:130-144:
-           -(1/2g^2)(W + W^dagger), W = U^dag on e_R(ix,iy) (bottom), U on
-           e_U(ix,iy) (left), U^dag on e_U(ix+1,iy) (right), U on e_R(ix,iy+1)
-           (top).  U|e> = |e+1>, zero at e = dg (u1_lgt_hamiltonian.jl:124-131).
-           W maps state idx to jdx; W^dagger maps jdx back, giving the mirrored
-           entry. */
-        if (model == ORC_MODEL_PJW) {
-            for (int iy = 1; iy <= ny - 1; iy++)
-                for (int ix = 1; ix <= nx - 1; ix++) {
-                    int eb = ER(seR, ix, iy), et = ER(seR, ix, iy + 1);
-                    int el = EU(seU, ix, iy), er = EU(seU, ix + 1, iy);
-                    if (eb - 1 < -dg || el + 1 > dg || er - 1 < -dg || et + 1 > dg) continue;
-                    memcpy(wnf, snf, (size_t)ns);
-                    memcpy(weR, seR, (size_t)nr);
-                    memcpy(weU, seU, (size_t)nu);
-                    ER(weR, ix, iy) = (int8_t)(eb - 1);
-                    EU(weU, ix, iy) = (int8_t)(el + 1);
-                    EU(weU, ix + 1, iy) = (int8_t)(er - 1);
-                    ER(weR, ix, iy + 1) = (int8_t)(et + 1);
-                    int64_t jdx = orc_map_get(&b->dict, orc_dict_key(b, wnf, weR, weU));
-                    if (jdx < 0) {
-                        c->err = 1;
-                        break;
-                    }
-                    orc_coo_push(c, jdx, idx, -invg2);
-                    orc_coo_push(c, idx, jdx, -invg2);
-                }
+            int stag = ((ix + iy) % 2 == 0) ? 1 : -1;
+            E += (m * stag) * (double)NF(snf, ix, iy);
         }
+    ORC_PUSH(idx, idx, E);
+    /* Horizontal forward hops, finite_ed.jl:279-297 */
+    for (int iy = 1; iy <= ny; iy++)
+        for (int ix = 1; ix <= nx - 1; ix++) {
+            int e = ER(seR, ix, iy);
+            int nL = NF(snf, ix, iy), nR = NF(snf, ix + 1, iy);
+            if (nL == 0 && nR == 1 && e < dg) {
+                memcpy(wnf, snf, (size_t)ns);
+                memcpy(weR, seR, (size_t)nr);
+                if (nu) memcpy(weU, seU, (size_t)nu);
+                NF(wnf, ix, iy) = 1;
+                NF(wnf, ix + 1, iy) = 0;
+                ER(weR, ix, iy) = (int8_t)(e + 1);
+                int64_t jdx = orc_map_get(&b->dict, orc_dict_key(b, wnf, weR, weU));
+                if (jdx < 0) return 1;
+                double v = -t;
+                if (model == ORC_MODEL_PJW) v = -t * orc_jw_sign(nx, ny, snf, ix, iy, ix + 1, iy);
+                ORC_PUSH(jdx, idx, v);
+                ORC_PUSH(idx, jdx, v);
+            }
+        }
+    /* Vertical forward hops, finite_ed.jl:300-318 (chain-adjacent on the
+       column snake, so no Jordan-Wigner string in the PJW model) */
+    for (int iy = 1; iy <= ny - 1; iy++)
+        for (int ix = 1; ix <= nx; ix++) {
+            int e = EU(seU, ix, iy);
+            int nD = NF(snf, ix, iy), nU = NF(snf, ix, iy + 1);
+            if (nD == 0 && nU == 1 && e < dg) {
+                memcpy(wnf, snf, (size_t)ns);
+                if (nr) memcpy(weR, seR, (size_t)nr);
+                memcpy(weU, seU, (size_t)nu);
+                NF(wnf, ix, iy) = 1;
+                NF(wnf, ix, iy + 1) = 0;
+                EU(weU, ix, iy) = (int8_t)(e + 1);
+                int64_t jdx = orc_map_get(&b->dict, orc_dict_key(b, wnf, weR, weU));
+                if (jdx < 0) return 1;
+                double v = -t;
+                if (model == ORC_MODEL_PJW) v = -t * orc_jw_sign(nx, ny, snf, ix, iy, ix, iy + 1);
+                ORC_PUSH(jdx, idx, v);
+                ORC_PUSH(idx, jdx, v);
+            }
+        }
+    /* Magnetic plaquette, matter_gauge_entanglement_pjw.jl:130-144:
+       -(1/2g^2)(W + W^dagger), W = U^dag on e_R(ix,iy) (bottom), U on
+       e_U(ix,iy) (left), U^dag on e_U(ix+1,iy) (right), U on e_R(ix,iy+1)
+       (top).  U|e> = |e+1>, zero at e = dg (u1_lgt_hamiltonian.jl:124-131).
+       W maps state idx to jdx; W^dagger maps jdx back, giving the mirrored
+       entry. */
+    if (model == ORC_MODEL_PJW) {
+        for (int iy = 1; iy <= ny - 1; iy++)
+            for (int ix = 1; ix <= nx - 1; ix++) {
+                int eb = ER(seR, ix, iy), et = ER(seR, ix, iy + 1);
+                int el = EU(seU, ix, iy), er = EU(seU, ix + 1, iy);
+                if (eb - 1 < -dg || el + 1 > dg || er - 1 < -dg || et + 1 > dg) continue;
+                memcpy(wnf, snf, (size_t)ns);
+                memcpy(weR, seR, (size_t)nr);
+                memcpy(weU, seU, (size_t)nu);
+                ER(weR, ix, iy) = (int8_t)(eb - 1);
+                EU(weU, ix, iy) = (int8_t)(el + 1);
+                EU(weU, ix + 1, iy) = (int8_t)(er - 1);
+                ER(weR, ix, iy + 1) = (int8_t)(et + 1);
+                int64_t jdx = orc_map_get(&b->dict, orc_dict_key(b, wnf, weR, weU));
+                if (jdx < 0) return 1;
+                ORC_PUSH(jdx, idx, -invg2);
+                ORC_PUSH(idx, jdx, -invg2);
+            }
     }
+#undef ORC_PUSH
+    return 0;
+}
+
+static void* orc_coo_done(orc_coo* c) {
     if (c->err) {
         free(c->I);
         free(c->J);
@@ -541,6 +536,110 @@ void* orc_ham_new(const void* hb, int model, double g, double t, double m) {
         return NULL;
     }
     return c;
+}
+
+/*
+ * Builds the COO triplets in the reference's push order (0-based).  The
+ * caller turns them into CSR/CSC, summing duplicates like SparseArrays'
+ * sparse(Is, Js, Vs, N, N) (finite_ed.jl:321); this Hamiltonian has none.
+ * Returns NULL on allocation failure or when a hopped state is missing
+ * from the basis (which the Gauss law rules out).
+ */
+void* orc_ham_new(const void* hb, int model, double g, double t, double m) {
+    const orc_basis* b = (const orc_basis*)hb;
+    orc_coo* c = (orc_coo*)calloc(1, sizeof(orc_coo));
+    if (!c) return NULL;
+    for (int64_t idx = 0; idx < b->n && !c->err; idx++)
+        if (orc_ham_state(b, model, g, t, m, idx, -1, c)) c->err = 1;
+    return orc_coo_done(c);
+}
+
+/*
+ * The triplets of the given rows only, without building the whole matrix
+ * (for sampled-row checks of sectors whose full matrix is too large to
+ * build in a test).  Row r receives triplets from the loop body of state r
+ * itself and of every state whose forward move lands on r; those are found
+ * by undoing each possible move of r and looking the result up in the
+ * dictionary, then the unchanged loop body (orc_ham_state) runs for each of
+ * them, keeping row r's triplets only.  Within a row the triplets come in
+ * the order of the sources visited (r first, then the undone moves), not
+ * in the full build's order; callers sum duplicates as sparse() would.
+ * Agreement with orc_ham_new row by row is checked in the CPU tests.
+ */
+void* orc_ham_rows(const void* hb, int model, double g, double t, double m, const int64_t* rows,
+                   int64_t nrows) {
+    const orc_basis* b = (const orc_basis*)hb;
+    int nx = b->nx, ny = b->ny, dg = b->dg;
+    int ns = nx * ny, nr = (nx - 1) * ny, nu = nx * (ny - 1);
+    orc_coo* c = (orc_coo*)calloc(1, sizeof(orc_coo));
+    if (!c) return NULL;
+    int8_t wnf[ORC_MAX_SITES], weR[ORC_MAX_SITES], weU[ORC_MAX_SITES];
+    for (int64_t q = 0; q < nrows && !c->err; q++) {
+        const int64_t r = rows[q];
+        if (r < 0 || r >= b->n) {
+            c->err = 1;
+            break;
+        }
+        if (orc_ham_state(b, model, g, t, m, r, r, c)) {
+            c->err = 1;
+            break;
+        }
+        const int8_t* snf = b->nf + r * ns;
+        const int8_t* seR = b->eR + r * nr;
+        const int8_t* seU = b->eU + r * nu;
+#define ORC_SOURCE()                                                                   \
+    do {                                                                               \
+        int64_t src = orc_map_get(&b->dict, orc_dict_key(b, wnf, weR, weU));           \
+        if (src >= 0 && orc_ham_state(b, model, g, t, m, src, r, c)) c->err = 1;       \
+    } while (0)
+        /* undone horizontal hops: r has the fermion on L, none on R, e > -dg */
+        for (int iy = 1; iy <= ny; iy++)
+            for (int ix = 1; ix <= nx - 1; ix++) {
+                int e = ER(seR, ix, iy);
+                if (NF(snf, ix, iy) == 1 && NF(snf, ix + 1, iy) == 0 && e > -dg) {
+                    memcpy(wnf, snf, (size_t)ns);
+                    memcpy(weR, seR, (size_t)nr);
+                    if (nu) memcpy(weU, seU, (size_t)nu);
+                    NF(wnf, ix, iy) = 0;
+                    NF(wnf, ix + 1, iy) = 1;
+                    ER(weR, ix, iy) = (int8_t)(e - 1);
+                    ORC_SOURCE();
+                }
+            }
+        /* undone vertical hops */
+        for (int iy = 1; iy <= ny - 1; iy++)
+            for (int ix = 1; ix <= nx; ix++) {
+                int e = EU(seU, ix, iy);
+                if (NF(snf, ix, iy) == 1 && NF(snf, ix, iy + 1) == 0 && e > -dg) {
+                    memcpy(wnf, snf, (size_t)ns);
+                    if (nr) memcpy(weR, seR, (size_t)nr);
+                    memcpy(weU, seU, (size_t)nu);
+                    NF(wnf, ix, iy) = 0;
+                    NF(wnf, ix, iy + 1) = 1;
+                    EU(weU, ix, iy) = (int8_t)(e - 1);
+                    ORC_SOURCE();
+                }
+            }
+        /* undone plaquette moves W (model PJW) */
+        if (model == ORC_MODEL_PJW) {
+            for (int iy = 1; iy <= ny - 1; iy++)
+                for (int ix = 1; ix <= nx - 1; ix++) {
+                    int eb = ER(seR, ix, iy), et = ER(seR, ix, iy + 1);
+                    int el = EU(seU, ix, iy), er = EU(seU, ix + 1, iy);
+                    if (eb + 1 > dg || el - 1 < -dg || er + 1 > dg || et - 1 < -dg) continue;
+                    memcpy(wnf, snf, (size_t)ns);
+                    memcpy(weR, seR, (size_t)nr);
+                    memcpy(weU, seU, (size_t)nu);
+                    ER(weR, ix, iy) = (int8_t)(eb + 1);
+                    EU(weU, ix, iy) = (int8_t)(el - 1);
+                    EU(weU, ix + 1, iy) = (int8_t)(er + 1);
+                    ER(weR, ix, iy + 1) = (int8_t)(et - 1);
+                    ORC_SOURCE();
+                }
+        }
+#undef ORC_SOURCE
+    }
+    return orc_coo_done(c);
 }
 
 int64_t orc_ham_ntriplets(const void* h) { return ((const orc_coo*)h)->n; }

@@ -66,6 +66,8 @@ def lib():
         L.orc_basis_free.argtypes = [vp]
         L.orc_ham_new.restype = vp
         L.orc_ham_new.argtypes = [vp, i32, dbl, dbl, dbl]
+        L.orc_ham_rows.restype = vp
+        L.orc_ham_rows.argtypes = [vp, i32, dbl, dbl, dbl, vp, i64]
         L.orc_ham_ntriplets.restype = i64
         L.orc_ham_ntriplets.argtypes = [vp]
         L.orc_ham_copy.restype = None
@@ -315,6 +317,34 @@ def build_hamiltonian(basis: OracleBasis, *, g: float, t: float, m: float, model
     H.sum_duplicates()
     H.sort_indices()
     return H
+
+
+def hamiltonian_rows(basis: OracleBasis, rows, *, g: float, t: float, m: float, model="ref"):
+    """Rows ``rows`` (0-based) of the matrix of ``build_hamiltonian``
+    without building the whole matrix (lgt_oracle.c:orc_ham_rows runs the
+    reference's per-state loop body for each row's sources only).  Returns
+    a scipy CSR matrix of shape (len(rows), N), duplicates summed as
+    sparse() would (finite_ed.jl:321)."""
+    import scipy.sparse as sp
+    L = lib()
+    rows = np.asarray(rows, dtype=np.int64)
+    uniq, inv = np.unique(rows, return_inverse=True)
+    h = L.orc_ham_rows(basis._h, _MODELS[model], float(g), float(t), float(m), _ptr(uniq),
+                       int(uniq.size))
+    if not h:
+        raise RuntimeError("oracle row construction failed")
+    try:
+        n = L.orc_ham_ntriplets(h)
+        I = np.zeros(n, np.int64)
+        J = np.zeros(n, np.int64)
+        V = np.zeros(n, np.float64)
+        L.orc_ham_copy(h, _ptr(I), _ptr(J), _ptr(V))
+    finally:
+        L.orc_ham_free(h)
+    H = sp.coo_matrix((V, (np.searchsorted(uniq, I), J)), shape=(uniq.size, basis.dim)).tocsr()
+    H.sum_duplicates()
+    H.sort_indices()
+    return H[inv]
 
 
 # --------------------------------------------------------------------------

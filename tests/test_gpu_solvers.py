@@ -105,6 +105,13 @@ def test_quench_4x3_batched(oracle, lgt, precision, tol_state, model):
         po, do = oracle.evolve(v0, Ho, ob, dt=0.05, n_steps=5)
         assert np.linalg.norm(psi[:, k] - po) <= tol_state
         assert abs(data[-1][k]["E2_mean"] - do[-1]["E2_mean"]) <= 10 * tol_state
+        # every step's record carries measure_ED's site grids (finite_ed.jl:409,421-422)
+        for step in (0, 2, 5):
+            for key in ("nf_grid", "E2_grid", "plaq_grid"):
+                assert data[step][k][key].shape == do[step][key].shape
+                np.testing.assert_allclose(data[step][k][key], do[step][key], rtol=0,
+                                           atol=10 * tol_state)
+            assert abs(data[step][k]["nf_mean"] - data[step][k]["nf_grid"].mean()) <= 1e-12
         e0 = np.vdot(v0, Ho @ v0).real
         e1 = np.vdot(psi[:, k], Ho @ psi[:, k]).real
         assert abs(e1 - e0) <= 100 * tol_state * abs(e0)

@@ -158,3 +158,24 @@ def test_oracle_matches_golden(oracle, path):
     np.testing.assert_array_equal(H.data, z["data"])
     E0, psi = oracle.ground_state(H)
     assert abs(E0 - float(z["E0"])) <= 1e-12 * abs(float(z["E0"]))
+
+
+@pytest.mark.parametrize("nx,ny,dg,kind", [(3, 2, 1, "stag"), (4, 2, 1, "stag"), (3, 3, 1, "stag"),
+                                            (3, 4, 1, "string"), (2, 2, 2, "stag"),
+                                            (3, 2, 2, "stag")])
+@pytest.mark.parametrize("model", ["ref", "pjw"])
+def test_row_restricted_build_equals_full_build(oracle, nx, ny, dg, kind, model):
+    """orc_ham_rows (the sampled-row oracle used at 4x4, where the whole
+    matrix is too large for a test) gives exactly the rows of the full
+    build: same columns, bitwise the same values, for every row and for a
+    random sample with repeats."""
+    g = oracle.staggered_charges(nx, ny) if kind == "stag" else oracle.string_charges(nx, ny)
+    b = oracle.build_basis(nx, ny, dg, g)
+    H = oracle.build_hamiltonian(b, g=0.9, t=1.1, m=0.37, model=model)
+    R = oracle.hamiltonian_rows(b, np.arange(b.dim), g=0.9, t=1.1, m=0.37, model=model)
+    np.testing.assert_array_equal(R.indptr, H.indptr)
+    np.testing.assert_array_equal(R.indices, H.indices)
+    np.testing.assert_array_equal(R.data, H.data)
+    rows = np.random.default_rng(5).integers(0, b.dim, 40)
+    S = oracle.hamiltonian_rows(b, rows, g=0.9, t=1.1, m=0.37, model=model)
+    assert (S != H[rows]).nnz == 0

@@ -7,7 +7,9 @@ observables with a fixed static device scratch instead of allocated buffers.
 Both entry points are called on the same device panels; the results must
 agree to 1e-11 relative (they differ only in the block partition of the
 reduction), on two calls in a row with different states, so that leftovers
-of the first call in the shared scratch cannot leak into the second.
+of the first call in the shared scratch cannot leak into the second.  The
+allocation-free calls run first on a fresh Hamiltonian, with free device
+memory checked to be unchanged across them.
 This file is collected last on purpose.
 """
 import ctypes
@@ -45,20 +47,37 @@ def test_noalloc_matches_observe_twice(nx, ny, K, ncomp, dtype):
     from lgt_gb300 import _capi as C
     lib = C.load()
     states, _ = L.build_basis(nx, ny, 1, L.staggered_charges(nx, ny), device=0)
-    H = L.build_hamiltonian(states, g=np.linspace(0.5, 2.0, K), t=1.0, m=0.5, model="pjw")
     N = len(states)
     tdt = torch.float64 if dtype == "fp64" else torch.float32
     prec = C.LGT_FP64 if dtype == "fp64" else C.LGT_FP32
     gen = torch.Generator(device="cuda").manual_seed(1234)
-    for call in range(2):  # two calls in a row, different states
+    psis = []
+    for _ in range(2):  # two states, one per call
         psi = torch.randn((N, K, ncomp), dtype=tdt, device="cuda", generator=gen)
         psi /= torch.linalg.vector_norm(psi.double(), dim=(0, 2), keepdim=True).to(tdt)
-        torch.cuda.synchronize()
-        ref = _observe(C, lib, H, psi.data_ptr(), ncomp, prec, "observe", nx, ny)
-        got = _observe(C, lib, H, psi.data_ptr(), ncomp, prec, "noalloc", nx, ny)
-        for a, b in zip(got, ref):
+        psis.append(psi)
+    g = np.linspace(0.5, 2.0, K)
+    # warm-up on a throw-away Hamiltonian: loads the module and looks up the
+    # scratch address (the one-time set-up of the first call on a device)
+    H0 = L.build_hamiltonian(states, g=g, t=1.0, m=0.5, model="pjw")
+    _observe(C, lib, H0, psis[0].data_ptr(), ncomp, prec, "noalloc", nx, ny)
+    H0.close()
+    # a fresh Hamiltonian whose own growable buffers have never been used:
+    # lgt_observe_noalloc runs on it first and must not change free device
+    # memory (no cudaMalloc, no fallback to the handle's buffers)
+    H = L.build_hamiltonian(states, g=g, t=1.0, m=0.5, model="pjw")
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info(0)[0]
+    got = [_observe(C, lib, H, p.data_ptr(), ncomp, prec, "noalloc", nx, ny) for p in psis]
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info(0)[0] == free0
+    for call in range(2):  # two calls in a row, different states
+        ref = _observe(C, lib, H, psis[call].data_ptr(), ncomp, prec, "observe", nx, ny)
+        again = _observe(C, lib, H, psis[call].data_ptr(), ncomp, prec, "noalloc", nx, ny)
+        for a, b, c in zip(got[call], ref, again):
             np.testing.assert_allclose(a, b, rtol=1e-11, atol=1e-13)
-        assert np.allclose(got[3][:, 6], 1.0, atol=1e-5)  # norm2 of normalised states
+            np.testing.assert_array_equal(a, c)  # the same partition: bitwise repeatable
+        assert np.allclose(got[call][3][:, 6], 1.0, atol=1e-5)  # norm2 of normalised states
     H.close()
     states.close()
 
