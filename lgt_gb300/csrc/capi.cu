@@ -518,7 +518,7 @@ lgt_status cta_solve(const std::vector<lgt_ham*>& hams, const KrylovParams& p,
       coef[i][k] = (g * g) / 2;
       coef[i][K + k] = m;
       coef[i][2 * K + k] = -t;
-      coef[i][3 * K + k] = -(1.0 / (2.0 * (g * g)));
+      coef[i][3 * K + k] = (h->model & LGT_MODEL_PLAQ) ? -(1.0 / (2.0 * (g * g))) : 0.0;
     }
     steps[i].assign(K, 0);
     rest[i].assign(K, 0);
@@ -543,6 +543,33 @@ lgt_status cta_solve(const std::vector<lgt_ham*>& hams, const KrylovParams& p,
   std::string m = small_ground_states(jobs, small_params(p), p.mixed, &h0->small,
                                       h0->b->B.stream, &secs);
   if (!m.empty()) return from_msg(m);
+  if (p.mixed && p.refine > 0) {
+    // FP64 correction: a short FP64 Lanczos per point (Krylov dimension
+    // refine_steps, restarted up to maxiter) started from the FP32-mixed
+    // solution, which the first launch left normalised in the panels; the
+    // energy becomes the FP64 Ritz value and the state FP64-accurate.
+    std::vector<std::vector<int>> steps2(hams.size()), rest2(hams.size());
+    for (size_t i = 0; i < hams.size(); ++i) {
+      steps2[i].assign(hams[i]->K, 0);
+      rest2[i].assign(hams[i]->K, 0);
+      jobs[i].steps = steps2[i].data();
+      jobs[i].restarts = rest2[i].data();
+    }
+    SmallParams q = small_params(p);
+    q.m = p.refine;
+    if (q.check_every > q.m) q.check_every = q.m;
+    q.start_given = 1;
+    q.rows_per_thread = 0;
+    double secs2 = 0.0;
+    m = small_ground_states(jobs, q, 0, &h0->small, h0->b->B.stream, &secs2);
+    if (!m.empty()) return from_msg(m);
+    secs += secs2;
+    for (size_t i = 0; i < hams.size(); ++i)
+      for (int k = 0; k < hams[i]->K; ++k) {
+        steps[i][k] += steps2[i][k];
+        rest[i][k] += rest2[i][k];
+      }
+  }
   int nconv = 0, maxsteps = 0, maxrest = 0;
   double maxr = 0.0;
   bool all = true;

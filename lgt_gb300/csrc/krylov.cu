@@ -29,6 +29,7 @@
 #include <tuple>
 #include <vector>
 
+#include "lgt_dfloat.cuh"
 #include "lgt_krylov.h"
 #include "lgt_tridiag.cuh"
 
@@ -109,7 +110,39 @@ template <typename S, int NC, int NQ>
 __device__ __forceinline__ void dots_chunk(const S* __restrict__ V, size_t vstride,
                                            const S* __restrict__ W, int64_t r0, int64_t r1,
                                            int rg, int RG, int c, int C, int i0, int J, int Jv,
-                                           bool act, double* red) {
+                                           bool act, double* red, bool dw) {
+  if (sizeof(S) == 4 && NC == 1 && dw) {
+    // FP32 panels: products of FP32 entries are exact as double-floats, and
+    // the running sums are double-floats (lgt_dfloat.cuh), so the dot is
+    // FP64-class while the FP64 pipe only sees the final conversion
+    df a[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) a[q] = df{0.f, 0.f};
+    if (act) {
+      const int ilast = (Jv > 0) ? Jv - 1 : 0;
+      for (int64_t row = r0 + rg; row < r1; row += RG) {
+        const size_t off = size_t(row) * C;
+        const float w = float(W[off + c]);
+        float v[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+          const int i = (i0 + q < Jv) ? i0 + q : ilast;
+          v[q] = float(V[size_t(i) * vstride + off + c]);
+        }
+#pragma unroll
+        for (int q = 0; q < NQ; ++q)
+          if (i0 + q < J) df_fma(a[q], (i0 + q < Jv) ? v[q] : w, w);
+      }
+    }
+    if (rg < RG) {
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        red[((rg * kIC + q) * 2 + 0) * C + c] = act ? widen(a[q].hi) + widen(a[q].lo) : 0.0;
+        red[((rg * kIC + q) * 2 + 1) * C + c] = 0.0;
+      }
+    }
+    return;
+  }
   constexpr int kB = (NC == 2) ? NQ : 1;  // imaginary parts (complex panels only)
   double a[NQ], b[kB];
 #pragma unroll
@@ -156,7 +189,8 @@ __global__ void __launch_bounds__(kT, sizeof(S) == 4 ? LGT_MD_MINB_F32 : LGT_MD_
                                                  const int* jstate, int jfixed,
                                                  const S* __restrict__ W, int64_t N, int C,
                                                  int64_t rpb, double* part, int Jmax,
-                                                 int self, const int* need, int ncomp) {
+                                                 int self, const int* need, int ncomp,
+                                                 int dw) {
   extern __shared__ double red[];  // [RG][kIC][2][C]
   const int Jv = jstate ? (*jstate + 1) : jfixed;
   const int J = Jv + self;
@@ -169,13 +203,13 @@ __global__ void __launch_bounds__(kT, sizeof(S) == 4 ? LGT_MD_MINB_F32 : LGT_MD_
     const int nq = (J - i0 < kIC) ? J - i0 : kIC;
     const int nq2 = nq <= 1 ? 1 : nq <= 2 ? 2 : nq <= 4 ? 4 : kIC;
     if (nq2 == 1)
-      dots_chunk<S, NC, 1>(V, vstride, W, r0, r1, rg, RG, c, C, i0, J, Jv, act, red);
+      dots_chunk<S, NC, 1>(V, vstride, W, r0, r1, rg, RG, c, C, i0, J, Jv, act, red, dw);
     else if (nq2 == 2)
-      dots_chunk<S, NC, 2>(V, vstride, W, r0, r1, rg, RG, c, C, i0, J, Jv, act, red);
+      dots_chunk<S, NC, 2>(V, vstride, W, r0, r1, rg, RG, c, C, i0, J, Jv, act, red, dw);
     else if (nq2 == 4)
-      dots_chunk<S, NC, 4>(V, vstride, W, r0, r1, rg, RG, c, C, i0, J, Jv, act, red);
+      dots_chunk<S, NC, 4>(V, vstride, W, r0, r1, rg, RG, c, C, i0, J, Jv, act, red, dw);
     else
-      dots_chunk<S, NC, kIC>(V, vstride, W, r0, r1, rg, RG, c, C, i0, J, Jv, act, red);
+      dots_chunk<S, NC, kIC>(V, vstride, W, r0, r1, rg, RG, c, C, i0, J, Jv, act, red, dw);
     __syncthreads();
     for (int q = threadIdx.x; q < nq2 * 2 * C; q += kT) {
       double s = 0.0;
@@ -345,6 +379,101 @@ __global__ void __launch_bounds__(kT) k_update(const S* __restrict__ V, size_t v
   red[threadIdx.x] = (rg < RG) ? nrm : 0.0;
   __syncthreads();
   if (threadIdx.x < C && !(need && need[threadIdx.x / ncomp] == 0)) {
+    double s = 0.0;
+    for (int g = 0; g < RG; ++g) s += red[g * C + threadIdx.x];
+    npart[size_t(blockIdx.x) * C + threadIdx.x] = s;
+  }
+}
+
+// k_update for FP32 real panels with double-float arithmetic: W -= sum_i
+// h_i V_i and the new |W|^2 partials, FP64-class (lgt_dfloat.cuh) with the
+// FP64 pipe used only to split the coefficients.  The block first splits
+// its columns' coefficients h into FP32 pairs hh + hl in shared memory
+// (sh: [J][C] pairs); each thread then runs two rows at a time with two
+// coefficient chains per row (even and odd i), four basis vectors per trip
+// with their loads issued first.  Same partition, skipping rules and
+// outputs as k_update.
+__global__ void __launch_bounds__(kT) k_update_df(const float* __restrict__ V, size_t vstride,
+                                                  const int* jstate, float* __restrict__ W,
+                                                  int64_t N, int C, const double* __restrict__ h,
+                                                  int K, const int* status, int64_t rpb,
+                                                  double* npart, const int* need) {
+  extern __shared__ float sh[];  // hh[J][C], then hl[J][C]
+  __shared__ double red[kT];
+  const int J = *jstate + 1;
+  float* s_hh = sh;
+  float* s_hl = sh + size_t(J) * C;
+  for (int idx = threadIdx.x; idx < J * C; idx += kT) {
+    const int i = idx / C, cc = idx - i * C;
+    const double hv = h[(size_t(i) * K + cc) * 2];
+    const float hh = narrow(hv);
+    s_hh[idx] = hh;
+    s_hl[idx] = narrow(hv - widen(hh));
+  }
+  __syncthreads();
+  const int RG = kT / C;
+  const int c = threadIdx.x % C, rg = threadIdx.x / C;
+  const int k = c;
+  const bool act = rg < RG && (!status || status[k] == kActive) && !(need && need[k] == 0);
+  const int64_t r0 = int64_t(blockIdx.x) * rpb;
+  const int64_t r1 = (r0 + rpb < N) ? r0 + rpb : N;
+  df nrm{0.f, 0.f};
+  if (act) {
+    int64_t row = r0 + rg;
+    for (; row + RG < r1; row += 2 * int64_t(RG)) {
+      const size_t oa = size_t(row) * C + c, ob = oa + size_t(RG) * C;
+      df a0{W[oa], 0.f}, b0{W[ob], 0.f}, a1{0.f, 0.f}, b1{0.f, 0.f};
+      const float* va = V + oa;
+      const float* vb = V + ob;
+      int i = 0;
+      for (; i + 3 < J; i += 4) {
+        float x[4], y[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          x[u] = __ldg(va + size_t(i + u) * vstride);
+          y[u] = __ldg(vb + size_t(i + u) * vstride);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const float hh = s_hh[(i + u) * C + c], hl = s_hl[(i + u) * C + c];
+          df_sub_prod((u & 1) ? a1 : a0, hh, hl, x[u]);
+          df_sub_prod((u & 1) ? b1 : b0, hh, hl, y[u]);
+        }
+      }
+      for (; i < J; ++i) {
+        const float hh = s_hh[i * C + c], hl = s_hl[i * C + c];
+        df_sub_prod(a0, hh, hl, __ldg(va + size_t(i) * vstride));
+        df_sub_prod(b0, hh, hl, __ldg(vb + size_t(i) * vstride));
+      }
+      const float sa = df_round(df_add(a0, a1)), sb = df_round(df_add(b0, b1));
+      W[oa] = sa;
+      W[ob] = sb;
+      df_fma(nrm, sa, sa);
+      df_fma(nrm, sb, sb);
+    }
+    for (; row < r1; row += RG) {
+      const size_t oa = size_t(row) * C + c;
+      df a0{W[oa], 0.f}, a1{0.f, 0.f};
+      const float* va = V + oa;
+      int i = 0;
+      for (; i + 3 < J; i += 4) {
+        float x[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) x[u] = __ldg(va + size_t(i + u) * vstride);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          df_sub_prod((u & 1) ? a1 : a0, s_hh[(i + u) * C + c], s_hl[(i + u) * C + c], x[u]);
+      }
+      for (; i < J; ++i)
+        df_sub_prod(a0, s_hh[i * C + c], s_hl[i * C + c], __ldg(va + size_t(i) * vstride));
+      const float sa = df_round(df_add(a0, a1));
+      W[oa] = sa;
+      df_fma(nrm, sa, sa);
+    }
+  }
+  red[threadIdx.x] = (rg < RG) ? widen(nrm.hi) + widen(nrm.lo) : 0.0;
+  __syncthreads();
+  if (threadIdx.x < C && !(need && need[threadIdx.x] == 0)) {
     double s = 0.0;
     for (int g = 0; g < RG; ++g) s += red[g * C + threadIdx.x];
     npart[size_t(blockIdx.x) * C + threadIdx.x] = s;
@@ -927,19 +1056,35 @@ cudaError_t launch_multidot(Work<S>& w, const SV* V, size_t vstride, const int* 
                             const int* need = nullptr) {
   const int RG = kT / w.C;
   const size_t sh = sizeof(double) * size_t(RG) * kIC * 2 * w.C;
+  const int dw = df_reductions_enabled() ? 1 : 0;
   if (w.ncomp == 1)
     k_multidot<SV, 1><<<w.red.nblk, kT, sh, s>>>(V, vstride, jstate, jfixed, Wp, w.N, w.C,
                                                  w.red.rpb, w.part, w.ldT, self, need,
-                                                 w.ncomp), lgt::note_launch();
+                                                 w.ncomp, dw), lgt::note_launch();
   else
     k_multidot<SV, 2><<<w.red.nblk, kT, sh, s>>>(V, vstride, jstate, jfixed, Wp, w.N, w.C,
                                                  w.red.rpb, w.part, w.ldT, self, need,
-                                                 w.ncomp), lgt::note_launch();
+                                                 w.ncomp, dw), lgt::note_launch();
   return cudaGetLastError();
 }
 
+// Shared memory of k_update_df's coefficient split for the largest step of
+// a Work (m + 1 vectors); above this budget the FP64 update runs.
+constexpr size_t kUpdDfSmemMax = 96 * 1024;
+
 template <typename S>
 cudaError_t launch_update(Work<S>& w, S* Wp, cudaStream_t s, const int* need = nullptr) {
+  if constexpr (sizeof(S) == 4) {
+    const size_t sh = size_t(w.ldT) * size_t(w.C) * 2 * sizeof(float);
+    if (w.ncomp == 1 && df_reductions_enabled() && sh <= kUpdDfSmemMax) {
+      cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(k_update_df), int(sh));
+      if (e != cudaSuccess) return e;
+      k_update_df<<<w.red.nblk, kT, sh, s>>>(w.V, w.vstride, w.jstate, Wp, w.N, w.C, w.h, w.K,
+                                             w.status, w.red.rpb, w.npart, need),
+          lgt::note_launch();
+      return cudaGetLastError();
+    }
+  }
   if (w.ncomp == 1)
     k_update<S, 1><<<w.red.nblk, kT, 0, s>>>(w.V, w.vstride, w.jstate, 0, Wp, w.N, w.C, w.ncomp,
                                              w.h, w.K, w.status, w.red.rpb, w.npart,

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <string>
@@ -34,6 +35,15 @@ inline cudaError_t raise_smem_limit(const void* func, int bytes) {
   e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess) have = bytes;
   return e;
+}
+
+// The FP32-mixed Krylov reductions (Gram-Schmidt dots and updates, norms)
+// run in double-float arithmetic on the FP32 pipe; LGT_DF_REDUCTIONS=0 in
+// the environment runs the panel drivers' reductions in FP64 instead
+// (cross-checks).  Read at every launch configuration.
+inline bool df_reductions_enabled() {
+  const char* e = getenv("LGT_DF_REDUCTIONS");
+  return !(e && e[0] == '0');
 }
 
 // Two timing events destroyed with the scope, whatever path leaves it.

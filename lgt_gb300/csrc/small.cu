@@ -29,6 +29,7 @@
 #include <tuple>
 #include <vector>
 
+#include "lgt_dfloat.cuh"
 #include "lgt_moves.cuh"
 #include "lgt_rank.cuh"
 #include "lgt_small.h"
@@ -172,6 +173,35 @@ __device__ double block_sum(double v, double* red, double* out) {
   return block_sum(v, red, out, [](double) {});
 }
 
+__device__ __forceinline__ df shfl_xor_df(df v, int o) {
+  return df{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+}
+
+// x += (h + l)^2 for a double-float h + l: the leading square exactly, the
+// cross term rounded (l^2 is below the pair's precision).
+__device__ __forceinline__ void df_sq2(df& x, float h, float l) {
+  float p, e;
+  two_prod(h, h, p, e);
+  e = df_fma_rn(df_add_rn(h, h), l, e);
+  df_acc(x, p, e);
+}
+
+// The reduce-scatter of four per-lane double-float partial sums over a warp
+// (as the FP64 version in k_lanczos_cta): afterwards lanes 0, 8, 16 and 24
+// hold the warp totals of values 0..3, as doubles.
+__device__ __forceinline__ double warp_scatter4_df(const df* p, int lane) {
+  const bool b4 = lane & 16, b3 = lane & 8;
+  const df r0 = shfl_xor_df(b4 ? p[0] : p[2], 16);
+  const df r1 = shfl_xor_df(b4 ? p[1] : p[3], 16);
+  const df k0 = df_add(b4 ? p[2] : p[0], r0), k1 = df_add(b4 ? p[3] : p[1], r1);
+  const df r2 = shfl_xor_df(b3 ? k0 : k1, 8);
+  df kk = df_add(b3 ? k1 : k0, r2);
+  kk = df_add(kk, shfl_xor_df(kk, 4));
+  kk = df_add(kk, shfl_xor_df(kk, 2));
+  kk = df_add(kk, shfl_xor_df(kk, 1));
+  return widen(kk.hi) + widen(kk.lo);
+}
+
 // One ground-state solve per CTA.  S: storage/matvec precision of the
 // Krylov basis (double, or float for the FP32-mixed path); R: rows per
 // thread held in registers (N <= R * 512).
@@ -199,6 +229,14 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
   const double tiny_rel = fp32 ? 1e-6 : 1e-12;
   const double tol = fp32 ? fmax(prm.tol, 2e-5) : prm.tol;
 
+  // The FP32-mixed path (S = float) keeps the Lanczos residual as
+  // double-float pairs and runs its Gram-Schmidt dots, updates and norms in
+  // double-float arithmetic on the FP32 pipe (lgt_dfloat.cuh): FP64-class
+  // sums without GB300's narrow FP64 pipe.  The FP64 path is unchanged.
+  constexpr bool kDF = sizeof(S) == 4;
+  __shared__ float s_hh[kMaxM + 1], s_hl[kMaxM + 1];  // s_h split into FP32 pairs (kDF)
+  __shared__ float s_rb[2];                           // 1 / beta split likewise (kDF)
+  float wh[R], wl[R];  // this thread's residual rows as double-float pairs (kDF)
   double w[R];  // this thread's rows of the current residual vector
   // start vector: normal(seed, k) into V_0, normalised
   double nrm = 0.0;
@@ -249,9 +287,19 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
             const S c = (kind == kPlaq) ? cp : ((kind == kHopNeg) ? -ch : ch);
             acc = fma(c, vj[e >> 2], acc);
           }
-          w[i] = widen(acc);
+          if constexpr (kDF) {
+            wh[i] = float(acc);
+            wl[i] = 0.f;
+          } else {
+            w[i] = widen(acc);
+          }
         } else {
-          w[i] = 0.0;
+          if constexpr (kDF) {
+            wh[i] = 0.f;
+            wl[i] = 0.f;
+          } else {
+            w[i] = 0.0;
+          }
         }
       }
       // Classical Gram-Schmidt against the whole basis V_0..V_j (which also
@@ -266,6 +314,25 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
       for (int pass = 0; pass < prm.reorth; ++pass) {
         const int jd = (pass == 0) ? j + 1 : j;
         for (int b0 = 0; b0 <= jd; b0 += 4) {
+          if constexpr (kDF) {
+            df pd[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll
+            for (int i = 0; i < R; ++i) {
+              const int r = tid + i * nthr;
+              if (r < N) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                  if (b0 + q <= j)
+                    df_fma2(pd[q], float(V[size_t(b0 + q) * N + r]), wh[i], wl[i]);
+                  else if (b0 + q == jd)
+                    df_sq2(pd[q], wh[i], wl[i]);
+              }
+            }
+            const double kk = warp_scatter4_df(pd, lane);
+            const int qv = lane >> 3;  // lanes 0, 8, 16, 24 hold values 0..3
+            if ((lane & 7) == 0 && b0 + qv <= jd) s_part[b0 + qv][wid] = kk;
+            continue;
+          }
           double p[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
           for (int i = 0; i < R; ++i) {
@@ -306,10 +373,37 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
           const double sum = s0 + s1;
           s_h[tid] = sum;
           if (tid == j) s_alpha[j] = (pass == 0) ? sum : s_alpha[j] + sum;
+          if (kDF) {  // the update's coefficients as FP32 pairs, once per block
+            const float hh = narrow(sum);
+            s_hh[tid] = hh;
+            s_hl[tid] = narrow(sum - widen(hh));
+          }
         }
         __syncthreads();
         if (pass == 0) nb = ss = s_h[j + 1];
-        for (int b0 = 0; b0 <= j; b0 += 4) {
+        if constexpr (kDF) {
+          for (int b0 = 0; b0 <= j; b0 += 4) {
+            float hh[4], hl[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              hh[q] = (b0 + q <= j) ? s_hh[b0 + q] : 0.f;
+              hl[q] = (b0 + q <= j) ? s_hl[b0 + q] : 0.f;
+            }
+#pragma unroll
+            for (int i = 0; i < R; ++i) {
+              const int r = tid + i * nthr;
+              if (r < N) {
+                df x{wh[i], wl[i]};
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                  if (b0 + q <= j) df_sub_prod(x, hh[q], hl[q], float(V[size_t(b0 + q) * N + r]));
+                wh[i] = x.hi;
+                wl[i] = x.lo;
+              }
+            }
+          }
+        }
+        for (int b0 = 0; !kDF && b0 <= j; b0 += 4) {
           double h4[4];
 #pragma unroll
           for (int q = 0; q < 4; ++q) h4[q] = (b0 + q <= j) ? s_h[b0 + q] : 0.0;
@@ -324,8 +418,15 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
           }
         }
         double s1 = 0.0;
+        if constexpr (kDF) {
+          df n2{0.f, 0.f};
 #pragma unroll
-        for (int i = 0; i < R; ++i) s1 = fma(w[i], w[i], s1);
+          for (int i = 0; i < R; ++i) df_sq2(n2, wh[i], wl[i]);
+          s1 = widen(n2.hi) + widen(n2.lo);
+        } else {
+#pragma unroll
+          for (int i = 0; i < R; ++i) s1 = fma(w[i], w[i], s1);
+        }
         // beta = ||w||, 1 / beta and the exhaustion test of this step, by
         // thread 0 (alpha_j is final: the pass's reduction synchronised)
         ss = block_sum(s1, s_red, s_sum, [&](double sv) {
@@ -333,6 +434,11 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
           const double b = sv * rs;
           s_sum[1] = b;
           s_sum[2] = rs;
+          if (kDF) {
+            const float rh = narrow(rs);
+            s_rb[0] = rh;
+            s_rb[1] = narrow(rs - widen(rh));
+          }
           double scl = fabs(s_alpha[j]);
           if (j > 0) scl = fmax(scl, s_beta[j - 1]);
           s_exh = (b > tiny_rel * fmax(scl, 1.0)) ? 0 : 1;
@@ -354,7 +460,15 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
 #pragma unroll
         for (int i = 0; i < R; ++i) {
           const int r = tid + i * nthr;
-          if (r < N) vn[r] = to_storage<S>(w[i] * rbeta);
+          if constexpr (kDF) {
+            // (wh + wl)(rh + rl) to FP32: the leading product and the two
+            // cross terms, one final rounding
+            if (r < N)
+              vn[r] = S(df_fma_rn(wh[i], s_rb[0],
+                                  df_fma_rn(wh[i], s_rb[1], df_mul_rn(wl[i], s_rb[0]))));
+          } else {
+            if (r < N) vn[r] = to_storage<S>(w[i] * rbeta);
+          }
         }
       }
       // first check after 2 * check_every steps, then every check_every

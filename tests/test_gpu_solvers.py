@@ -137,3 +137,26 @@ def test_cta_basis_placement(oracle, lgt, monkeypatch, smem, precision, krylovdi
         assert abs(E0[k] - E0o) <= 1e-10 * abs(E0o), (k, E0[k], E0o)
         assert abs(abs(np.dot(psi[:, k], psio)) - 1.0) <= 1e-8
     H.close()
+
+
+@pytest.mark.parametrize("solver,nx,ny", [("cta", 4, 2), ("cta", 3, 3), ("panel", 4, 3)])
+@pytest.mark.parametrize("model", ["ref", "pjw"])
+def test_mixed_with_fp64_refinement(oracle, lgt, solver, nx, ny, model):
+    """FP32-mixed solve followed by the FP64 correction (refine_steps: a
+    short FP64 Lanczos started from the FP32 solution): observables within
+    1e-10 of the FP64 oracle (the unrefined mixed path leaves ~1e-7),
+    energies within 1e-12 relative."""
+    ob, gb = _basis(oracle, lgt, nx, ny)
+    gs, ms = np.array([0.8, 1.5]), np.array([0.3, 0.6])
+    H = lgt.build_hamiltonian(gb, g=gs, t=1.0, m=ms, model=model)
+    E0, psi = lgt.find_ground_state(H, tol=1e-12, precision="fp32_mixed", solver=solver,
+                                    refine_steps=20, as_complex=False)
+    obs = lgt.measure_ED(psi, gb)
+    for k in range(2):
+        Ho = oracle.build_hamiltonian(ob, g=gs[k], t=1.0, m=ms[k], model=model)
+        E0o, psio = oracle.ground_state(Ho)
+        mo = oracle.measure(psio, ob)
+        assert abs(E0[k] - E0o) <= 1e-12 * abs(E0o), (k, E0[k], E0o)
+        for key in ("E2_mean", "n_stag", "plaq_mean", "nf_even"):
+            assert abs(obs[k][key] - mo[key]) <= 1e-10, (k, key, obs[k][key] - mo[key])
+    H.close()
