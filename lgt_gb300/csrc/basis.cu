@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(kThreads) k_compact_count(Pred p, uint32_t* bl
 
 template <class Pred, class Out>
 __global__ void __launch_bounds__(kThreads) k_compact_write(Pred p, const uint64_t* block_off,
-                                                            Out* out) {
+                                                            Out* out, uint64_t cap, int* err) {
   __shared__ uint32_t warp_cnt[kThreads / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const uint64_t base = uint64_t(blockIdx.x) * kTile;
@@ -130,7 +130,11 @@ __global__ void __launch_bounds__(kThreads) k_compact_write(Pred p, const uint64
       before += (w < wid) ? c : 0u;
       total += c;
     }
-    if (ok) out[running + before + __popc(bal & ((1u << lane) - 1u))] = Out(v);
+    if (ok) {
+      const uint64_t at = running + before + __popc(bal & ((1u << lane) - 1u));
+      if (at < cap) out[at] = Out(v);
+      else raise_err(err, kDevErrBounds);
+    }
     running += total;
     __syncthreads();
   }
@@ -371,37 +375,53 @@ __global__ void k_tab_check(RankView R, int* bad) {
     if (e_ != cudaSuccess) return std::string(#call ": ") + cudaGetErrorString(e_); \
   } while (0)
 
-// Ordered compaction driver: counts, scans, writes.
+// Ordered compaction driver: counts, scans, writes.  The output holds
+// `expected` entries when the caller knows the count (no read-back; the
+// write is bounds-checked into `err`), else an upper bound (every
+// candidate) when that is small, the count then read back once; only a
+// large candidate space reads the count before allocating.  Temporaries and
+// the output come from the library's stream-ordered pool.
+constexpr uint64_t kUpperBoundBytes = 64ull << 20;
 template <class Pred, class Out>
-std::string compact(const Pred& p, Out** out, int64_t* count, cudaStream_t s) {
+std::string compact(const Pred& p, Out** out, int64_t* count, int* err, cudaStream_t s,
+                    int64_t expected = -1) {
+  *out = nullptr;
+  *count = 0;
   const uint64_t nblk64 = (p.total + kTile - 1) / kTile;
-  if (nblk64 == 0) {
-    *out = nullptr;
-    *count = 0;
-    return std::string();
-  }
+  if (nblk64 == 0) return std::string();
   if (nblk64 > 0x7fffffffull) return "candidate space too large for the enumerator";
   const int nblk = int(nblk64);
   uint32_t* counts = nullptr;
   uint64_t* offs = nullptr;
-  CK(cudaMallocAsync(&counts, sizeof(uint32_t) * nblk, s));
-  CK(cudaMallocAsync(&offs, sizeof(uint64_t) * (nblk + 1), s));
+  CK(dev_alloc_n(&counts, size_t(nblk), s));
+  CK(dev_alloc_n(&offs, size_t(nblk) + 1, s));
   k_compact_count<<<nblk, kThreads, 0, s>>>(p, counts), lgt::note_launch();
   CK(cudaGetLastError());
   k_scan_counts<<<1, 1024, 0, s>>>(counts, nblk, offs), lgt::note_launch();
   CK(cudaGetLastError());
-  uint64_t total = 0;
-  CK(cudaMemcpyAsync(&total, offs + nblk, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
+  uint64_t total = 0, cap = 0;
+  const bool small = p.total * sizeof(Out) <= kUpperBoundBytes;
+  if (expected >= 0) {
+    total = cap = uint64_t(expected);
+  } else if (small) {
+    cap = p.total;
+  } else {
+    CK(cudaMemcpyAsync(&total, offs + nblk, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    cap = total;
+  }
   Out* o = nullptr;
-  if (total > 0) {
-    CK(cudaMalloc(&o, sizeof(Out) * total));
-    k_compact_write<<<nblk, kThreads, 0, s>>>(p, offs, o), lgt::note_launch();
+  if (cap > 0) {
+    CK(dev_alloc_n(&o, size_t(cap), s));
+    k_compact_write<<<nblk, kThreads, 0, s>>>(p, offs, o, cap, err), lgt::note_launch();
     CK(cudaGetLastError());
   }
-  CK(cudaFreeAsync(counts, s));
-  CK(cudaFreeAsync(offs, s));
-  CK(cudaStreamSynchronize(s));
+  if (expected < 0 && small) {
+    CK(cudaMemcpyAsync(&total, offs + nblk, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  }
+  CK(dev_free(counts, s));
+  CK(dev_free(offs, s));
   *out = o;
   *count = int64_t(total);
   return std::string();
@@ -489,9 +509,9 @@ std::string build_rank_tables(BasisDev* B) {
   uint32_t* tab = nullptr;
   uint32_t* L = nullptr;
   int* bad = nullptr;
-  CK(cudaMalloc(&tab, sizeof(uint32_t) * size_t(tot)));
-  CK(cudaMalloc(&L, sizeof(uint32_t) * size_t(nlast * F)));
-  CK(cudaMalloc(&bad, sizeof(int)));
+  CK(dev_alloc_n(&tab, size_t(tot), s));
+  CK(dev_alloc_n(&L, size_t(nlast * F), s));
+  CK(dev_alloc_n(&bad, 1, s));
   CK(cudaMemsetAsync(bad, 0, sizeof(int), s));
   k_tab_last<<<unsigned((nlast * F + 255) / 256), 256, 0, s>>>(G, F, L), lgt::note_launch();
   for (int r = nrows - 1; r >= 0; --r) {
@@ -510,11 +530,11 @@ std::string build_rank_tables(BasisDev* B) {
   k_tab_check<<<unsigned((B->dim + 255) / 256), 256, 0, s>>>(B->view(), bad), lgt::note_launch();
   int hbad = 0;
   CK(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(dev_free(L, s));
+  CK(dev_free(bad, s));
   CK(cudaStreamSynchronize(s));
-  cudaFree(L);
-  cudaFree(bad);
   if (hbad) {  // keep the binary-search ranking
-    cudaFree(B->tab);
+    dev_free(B->tab, s);
     B->tab = nullptr;
     B->tab_F = 0;
     return "rank tables failed their self-check";
@@ -525,16 +545,19 @@ std::string build_rank_tables(BasisDev* B) {
 std::string build_basis_device(BasisDev* B) {
   const Geom& G = B->G;
   cudaStream_t s = B->stream;
-  CK(cudaMalloc(&B->err, sizeof(int)));
+  CK(dev_alloc_n(&B->err, 1, s));
   CK(cudaMemsetAsync(B->err, 0, sizeof(int), s));
-  CK(cudaMalloc(&B->binom, sizeof(uint32_t) * 32 * 33));
+  CK(dev_alloc_n(&B->binom, 32 * 33, s));
   k_binom<<<1, 32, 0, s>>>(B->binom), lgt::note_launch();
   CK(cudaGetLastError());
 
-  // 1. masks with N_f set bits, ascending
+  // 1. masks with N_f set bits, ascending: C(ns, N_f) of them (the write is
+  //    bounds-checked into the error word against that count)
   MaskPred mp{G.nf_target, 1ull << G.ns};
+  int64_t expect = 1;
+  for (int j = 0; j < G.nf_target; ++j) expect = expect * (G.ns - j) / (j + 1);
   int64_t nmasks = 0;
-  std::string err = compact(mp, &B->masks, &nmasks, s);
+  std::string err = compact(mp, &B->masks, &nmasks, B->err, s, expect);
   if (!err.empty()) return err;
   B->nmasks = int(nmasks);
 
@@ -552,7 +575,7 @@ std::string build_basis_device(BasisDev* B) {
 #define LGT_ENUM_CASE(D)                                                 \
   case D: {                                                              \
     CandPred<D> cp{G, B->masks, nfree, uint64_t(nmasks) * nfree};        \
-    err = compact(cp, &B->keys, &dim, s);                                \
+    err = compact(cp, &B->keys, &dim, B->err, s);                        \
     break;                                                               \
   }
       LGT_ENUM_CASE(1)
@@ -572,30 +595,30 @@ std::string build_basis_device(BasisDev* B) {
   B->dim = dim;
 
   // 3. ranking tables
-  CK(cudaMalloc(&B->segc, sizeof(uint32_t) * (nmasks + 1)));
+  CK(dev_alloc_n(&B->segc, size_t(nmasks) + 1, s));
   k_segments<<<int((nmasks + 1 + 255) / 256), 256, 0, s>>>(B->keys, dim, B->masks, int(nmasks),
                                                           G.ushift, B->segc), lgt::note_launch();
   CK(cudaGetLastError());
   if (G.ushift <= 32 && dim > 0) {
-    CK(cudaMalloc(&B->low, sizeof(uint32_t) * dim));
+    CK(dev_alloc_n(&B->low, size_t(dim), s));
     k_low_parts<<<int((dim + 255) / 256), 256, 0, s>>>(B->keys, dim, G.ushift, B->low), lgt::note_launch();
     CK(cudaGetLastError());
   }
-  CK(cudaStreamSynchronize(s));
   err = build_rank_tables(B);
   if (!err.empty()) return err;
   return std::string();
 }
 
 void free_basis_device(BasisDev* B) {
-  cudaFree(B->tab);
+  cudaStream_t s = B->stream;
+  dev_free(B->tab, s);
   B->tab = nullptr;
-  cudaFree(B->keys);
-  cudaFree(B->low);
-  cudaFree(B->segc);
-  cudaFree(B->masks);
-  cudaFree(B->binom);
-  cudaFree(B->err);
+  dev_free(B->keys, s);
+  dev_free(B->low, s);
+  dev_free(B->segc, s);
+  dev_free(B->masks, s);
+  dev_free(B->binom, s);
+  dev_free(B->err, s);
   B->keys = nullptr;
   B->low = nullptr;
   B->segc = nullptr;

@@ -198,11 +198,11 @@ lgt_status lgt_basis_keys(const lgt_basis* b, int64_t first, int64_t count, uint
                                  cudaMemcpyDeviceToHost, s));
   if (ref_keys) {
     uint64_t* d = nullptr;
-    CUDA_OR_FAIL(cudaMallocAsync(&d, sizeof(uint64_t) * count, s));
+    CUDA_OR_FAIL(dev_alloc_n(&d, size_t(count), s));
     launch_ref_keys(b->B, first, count, d, s);
     CUDA_OR_FAIL(cudaGetLastError());
     CUDA_OR_FAIL(cudaMemcpyAsync(ref_keys, d, sizeof(uint64_t) * count, cudaMemcpyDeviceToHost, s));
-    CUDA_OR_FAIL(cudaFreeAsync(d, s));
+    CUDA_OR_FAIL(dev_free(d, s));
   }
   CUDA_OR_FAIL(cudaStreamSynchronize(s));
   return LGT_OK;
@@ -219,13 +219,13 @@ lgt_status lgt_basis_states(const lgt_basis* b, int64_t first, int64_t count, in
   cudaStream_t s = b->B.stream;
   const size_t a = size_t(count) * G.ns, r = size_t(count) * G.nR, u = size_t(count) * G.nU;
   int8_t* d = nullptr;
-  CUDA_OR_FAIL(cudaMallocAsync(&d, a + r + u + 3, s));
+  CUDA_OR_FAIL(dev_alloc_n(&d, a + r + u + 3, s));
   launch_decode_states(b->B, first, count, d, d + a, d + a + r, s);
   CUDA_OR_FAIL(cudaGetLastError());
   if (n_f) CUDA_OR_FAIL(cudaMemcpyAsync(n_f, d, a, cudaMemcpyDeviceToHost, s));
   if (e_R && r) CUDA_OR_FAIL(cudaMemcpyAsync(e_R, d + a, r, cudaMemcpyDeviceToHost, s));
   if (e_U && u) CUDA_OR_FAIL(cudaMemcpyAsync(e_U, d + a + r, u, cudaMemcpyDeviceToHost, s));
-  CUDA_OR_FAIL(cudaFreeAsync(d, s));
+  CUDA_OR_FAIL(dev_free(d, s));
   CUDA_OR_FAIL(cudaStreamSynchronize(s));
   return LGT_OK;
 }
@@ -242,15 +242,15 @@ static lgt_status rank_common(const lgt_basis* b, const void* keys, int64_t n, i
   cudaStream_t s = b->B.stream;
   uint64_t* din = nullptr;
   int64_t* dout = nullptr;
-  CUDA_OR_FAIL(cudaMallocAsync(&din, sizeof(uint64_t) * n, s));
-  CUDA_OR_FAIL(cudaMallocAsync(&dout, sizeof(int64_t) * n, s));
+  CUDA_OR_FAIL(dev_alloc_n(&din, size_t(n), s));
+  CUDA_OR_FAIL(dev_alloc_n(&dout, size_t(n), s));
   CUDA_OR_FAIL(cudaMemcpyAsync(din, keys, sizeof(uint64_t) * n, cudaMemcpyHostToDevice, s));
   if (ref) launch_rank_ref_keys(b->B, din, n, dout, s);
   else launch_rank_order_keys(b->B, din, n, dout, s);
   CUDA_OR_FAIL(cudaGetLastError());
   CUDA_OR_FAIL(cudaMemcpyAsync(out, dout, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, s));
-  CUDA_OR_FAIL(cudaFreeAsync(din, s));
-  CUDA_OR_FAIL(cudaFreeAsync(dout, s));
+  CUDA_OR_FAIL(dev_free(din, s));
+  CUDA_OR_FAIL(dev_free(dout, s));
   CUDA_OR_FAIL(cudaStreamSynchronize(s));
   return LGT_OK;
 }
@@ -271,7 +271,8 @@ namespace {
 void release_basis(lgt_basis* b) {
   if (!b || b->refs.fetch_sub(1) != 1) return;
   cudaSetDevice(b->device);
-  cudaStreamSynchronize(b->B.stream);
+  // stream-ordered frees; the basis' own stream is released once its work
+  // has completed
   free_basis_device(&b->B);
   cudaStreamDestroy(b->own_stream);
   delete b;
@@ -317,8 +318,8 @@ lgt_status lgt_ham_create(const lgt_basis* b, int32_t K, const double* g, const 
   h->t.assign(t, t + K);
   h->m.assign(m, m + K);
   h->seg_smem = hpsi_seg_smem_default(b->B.nmasks);
-  cudaError_t e = cudaMalloc(&h->coef_d, sizeof(double) * 4 * K);
-  if (e == cudaSuccess) e = cudaMalloc(&h->coef_f, sizeof(float) * 4 * K);
+  cudaError_t e = dev_alloc_n(&h->coef_d, 4 * size_t(K), b->B.stream);
+  if (e == cudaSuccess) e = dev_alloc_n(&h->coef_f, 4 * size_t(K), b->B.stream);
   if (e != cudaSuccess) {
     lgt_ham_destroy(h);
     return cuda_fail(e, "lgt_ham_create");
@@ -357,11 +358,11 @@ lgt_status lgt_ham_nnz(const lgt_ham* h, int64_t* nnz) {
   const int64_t N = h->b->B.dim;
   cudaStream_t s = h->b->B.stream;
   int64_t* d = nullptr;
-  CUDA_OR_FAIL(cudaMallocAsync(&d, sizeof(int64_t) * (N + 1), s));
+  CUDA_OR_FAIL(dev_alloc_n(&d, size_t(N) + 1, s));
   CUDA_OR_FAIL(launch_row_nnz(h->b->B.G, h->b->B.view(), h->model, d, s));
   std::vector<int64_t> c(N);
   if (N) CUDA_OR_FAIL(cudaMemcpyAsync(c.data(), d, sizeof(int64_t) * N, cudaMemcpyDeviceToHost, s));
-  CUDA_OR_FAIL(cudaFreeAsync(d, s));
+  CUDA_OR_FAIL(dev_free(d, s));
   CUDA_OR_FAIL(cudaStreamSynchronize(s));
   int64_t tot = 0;
   for (int64_t v : c) tot += v;
@@ -378,7 +379,7 @@ lgt_status lgt_ham_export_csr(const lgt_ham* h, int32_t k, int64_t* rowptr, int3
   const int64_t N = h->b->B.dim;
   cudaStream_t s = h->b->B.stream;
   int64_t* dcnt = nullptr;
-  CUDA_OR_FAIL(cudaMallocAsync(&dcnt, sizeof(int64_t) * (N + 1), s));
+  CUDA_OR_FAIL(dev_alloc_n(&dcnt, size_t(N) + 1, s));
   CUDA_OR_FAIL(launch_row_nnz(h->b->B.G, h->b->B.view(), h->model, dcnt, s));
   std::vector<int64_t> c(N + 1, 0);
   if (N) CUDA_OR_FAIL(cudaMemcpyAsync(c.data(), dcnt, sizeof(int64_t) * N, cudaMemcpyDeviceToHost, s));
@@ -389,17 +390,17 @@ lgt_status lgt_ham_export_csr(const lgt_ham* h, int32_t k, int64_t* rowptr, int3
   int32_t* dcol = nullptr;
   double* dval = nullptr;
   CUDA_OR_FAIL(cudaMemcpyAsync(dcnt, rowptr, sizeof(int64_t) * (N + 1), cudaMemcpyHostToDevice, s));
-  CUDA_OR_FAIL(cudaMallocAsync(&dcol, sizeof(int32_t) * (nnz + 1), s));
-  CUDA_OR_FAIL(cudaMallocAsync(&dval, sizeof(double) * (nnz + 1), s));
+  CUDA_OR_FAIL(dev_alloc_n(&dcol, size_t(nnz) + 1, s));
+  CUDA_OR_FAIL(dev_alloc_n(&dval, size_t(nnz) + 1, s));
   CUDA_OR_FAIL(launch_row_fill(h->b->B.G, h->b->B.view(), h->model, dcnt, h->g[k], h->t[k],
                                h->m[k], dcol, dval, h->b->B.err, s));
   if (nnz) {
     CUDA_OR_FAIL(cudaMemcpyAsync(colidx, dcol, sizeof(int32_t) * nnz, cudaMemcpyDeviceToHost, s));
     CUDA_OR_FAIL(cudaMemcpyAsync(values, dval, sizeof(double) * nnz, cudaMemcpyDeviceToHost, s));
   }
-  CUDA_OR_FAIL(cudaFreeAsync(dcnt, s));
-  CUDA_OR_FAIL(cudaFreeAsync(dcol, s));
-  CUDA_OR_FAIL(cudaFreeAsync(dval, s));
+  CUDA_OR_FAIL(dev_free(dcnt, s));
+  CUDA_OR_FAIL(dev_free(dcol, s));
+  CUDA_OR_FAIL(dev_free(dval, s));
   CUDA_OR_FAIL(cudaStreamSynchronize(s));
   return check_device_errors(h->b);
 }
@@ -420,8 +421,8 @@ lgt_status lgt_matvec(const lgt_ham* hc, const void* x, void* y, int32_t ncomp, 
   const void* dx = x;
   void* dy = y;
   if (!on_device(flags)) {
-    CUDA_OR_FAIL(h->x.need(bytes));
-    CUDA_OR_FAIL(h->y.need(bytes));
+    CUDA_OR_FAIL(h->x.need(bytes, h->b->B.stream));
+    CUDA_OR_FAIL(h->y.need(bytes, h->b->B.stream));
     CUDA_OR_FAIL(cudaMemcpyAsync(h->x.p, x, bytes, cudaMemcpyHostToDevice, s));
     dx = h->x.p;
     dy = h->y.p;
@@ -478,7 +479,7 @@ lgt_status ensure_pattern(lgt_ham* h) {
   if (h->pattern.rowptr) return LGT_OK;
   std::string m = build_pattern(h->b->B, h->model, &h->pattern, h->b->B.stream);
   if (!m.empty()) {
-    free_pattern(&h->pattern);
+    free_pattern(&h->pattern, h->b->B.stream);
     return from_msg(m);
   }
   return LGT_OK;
@@ -616,7 +617,7 @@ lgt_status lgt_ground_state(lgt_ham* h, const lgt_krylov_opts* opts, double* E0,
   if (psi && on_device(flags)) {
     X = static_cast<double*>(psi);
   } else {
-    CUDA_OR_FAIL(h->x.need(bytes));
+    CUDA_OR_FAIL(h->x.need(bytes, h->b->B.stream));
     X = static_cast<double*>(h->x.p);
     if (p.start_given) CUDA_OR_FAIL(cudaMemcpyAsync(X, psi, bytes, cudaMemcpyHostToDevice, s));
   }
@@ -677,7 +678,7 @@ lgt_status lgt_ground_state_batch(int32_t nham, lgt_ham* const* hams, const lgt_
     if (use_cta(h, opts, p)) {
       double* X = (psi && psi[i]) ? static_cast<double*>(psi[i]) : nullptr;
       if (!X) {
-        CUDA_OR_FAIL(h->x.need(bytes));
+        CUDA_OR_FAIL(h->x.need(bytes, h->b->B.stream));
         X = static_cast<double*>(h->x.p);
       }
       small.push_back(h);
@@ -768,8 +769,8 @@ lgt_status observe_dev(lgt_ham* h, const T* x, int ncomp, std::vector<double>* f
   int nblk;
   int64_t rpb;
   observe_plan(h->b->B.dim, &nblk, &rpb);
-  CUDA_OR_FAIL(h->part.need(sizeof(double) * size_t(nblk) * h->K * nf));
-  CUDA_OR_FAIL(h->out.need(sizeof(double) * size_t(h->K) * nf));
+  CUDA_OR_FAIL(h->part.need(sizeof(double) * size_t(nblk) * h->K * nf, h->b->B.stream));
+  CUDA_OR_FAIL(h->out.need(sizeof(double) * size_t(h->K) * nf, h->b->B.stream));
   cudaStream_t s = h->b->B.stream;
   cudaError_t e = launch_observe<T>(G, h->b->B.view(), x, h->K, ncomp,
                                     static_cast<double*>(h->part.p), static_cast<double*>(h->out.p),
@@ -839,7 +840,7 @@ lgt_status lgt_expm_steps_grids(lgt_ham* h, const lgt_krylov_opts* opts, double 
   if (on_device(flags)) {
     X = static_cast<double*>(psi);
   } else {
-    CUDA_OR_FAIL(h->y.need(bytes));
+    CUDA_OR_FAIL(h->y.need(bytes, h->b->B.stream));
     X = static_cast<double*>(h->y.p);
     CUDA_OR_FAIL(cudaMemcpyAsync(X, psi, bytes, cudaMemcpyHostToDevice, s));
   }
@@ -884,7 +885,7 @@ lgt_status lgt_observe(const lgt_ham* hc, const void* psi, int32_t ncomp, int32_
   cudaStream_t s = h->b->B.stream;
   const void* dx = psi;
   if (!on_device(flags)) {
-    CUDA_OR_FAIL(h->x.need(bytes));
+    CUDA_OR_FAIL(h->x.need(bytes, h->b->B.stream));
     CUDA_OR_FAIL(cudaMemcpyAsync(h->x.p, psi, bytes, cudaMemcpyHostToDevice, s));
     dx = h->x.p;
   }
@@ -914,11 +915,10 @@ lgt_status lgt_energy(const lgt_ham* hc, const void* psi, int32_t ncomp, uint32_
   const int64_t N = h->b->B.dim;
   const size_t bytes = size_t(N) * h->K * ncomp * sizeof(double);
   cudaStream_t s = h->b->B.stream;
-  CUDA_OR_FAIL(h->y.need(bytes));
+  CUDA_OR_FAIL(h->y.need(bytes, h->b->B.stream));
   const double* dx = static_cast<const double*>(psi);
-  DevBuf tmp;
   if (!on_device(flags)) {
-    CUDA_OR_FAIL(h->x.need(bytes));
+    CUDA_OR_FAIL(h->x.need(bytes, h->b->B.stream));
     CUDA_OR_FAIL(cudaMemcpyAsync(h->x.p, psi, bytes, cudaMemcpyHostToDevice, s));
     dx = static_cast<const double*>(h->x.p);
   }
@@ -954,20 +954,21 @@ lgt_status lgt_autotune(lgt_ham* h, int32_t ncomp, int32_t precision, lgt_tuning
 
 void lgt_ham_destroy(lgt_ham* h) {
   if (!h) return;
-  if (h->b) {
-    cudaSetDevice(h->b->device);
-    cudaStreamSynchronize(h->b->B.stream);
-  }
+  // pool buffers are freed in stream order on the basis' stream; the Krylov
+  // workspaces and the neighbour tables (plain device allocations) are freed
+  // by cudaFree, which waits for the device
+  cudaStream_t s = h->b ? h->b->B.stream : nullptr;
+  if (h->b) cudaSetDevice(h->b->device);
   krylov_cache_free(h->cache);
-  h->x.release();
-  h->y.release();
-  h->part.release();
-  h->out.release();
-  free_pattern(&h->pattern);
+  h->x.release(s);
+  h->y.release(s);
+  h->part.release(s);
+  h->out.release(s);
+  free_pattern(&h->pattern, s);
   free_nbr_table(&h->table);
-  cudaFree(h->small.base);
-  cudaFree(h->coef_d);
-  cudaFree(h->coef_f);
+  dev_free(h->small.base, s);
+  dev_free(h->coef_d, s);
+  dev_free(h->coef_f, s);
   lgt_basis* b = const_cast<lgt_basis*>(h->b);
   delete h;
   release_basis(b);

@@ -1,0 +1,70 @@
+// devmem.cu -- the library's stream-ordered device memory.
+//
+// Handles (bases, Hamiltonians, their lookup tables and scratch) take their
+// device memory from one memory pool per device, allocated and freed in
+// stream order (cudaMallocFromPoolAsync / cudaFreeAsync on the handle's
+// stream).  The pool keeps freed memory, up to kRetainBytes, for the next
+// allocation instead of returning it to the driver at every
+// synchronisation, so a sweep that builds and drops bases and Hamiltonians
+// per batch of coupling points does not pay a driver allocation and an
+// implicit device synchronisation per buffer.  The large Krylov workspaces
+// of the panel drivers (allocated once per shape and kept), the stored
+// neighbour tables and the allocation-free observables entry point do not
+// use it.
+#include <mutex>
+
+#include "lgt_internal.h"
+
+namespace lgt {
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+constexpr unsigned long long kRetainBytes = 4ull << 30;  // kept for reuse per device
+
+std::mutex g_pool_mu;
+cudaMemPool_t g_pool[kMaxDevices] = {};
+
+cudaError_t pool_of(int dev, cudaMemPool_t* out) {
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_pool_mu);
+  if (!g_pool[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t p = nullptr;
+    cudaError_t e = cudaMemPoolCreate(&p, &props);
+    if (e != cudaSuccess) return e;
+    unsigned long long keep = kRetainBytes;
+    e = cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+    if (e != cudaSuccess) {
+      cudaMemPoolDestroy(p);
+      return e;
+    }
+    g_pool[dev] = p;
+  }
+  *out = g_pool[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+cudaError_t dev_alloc(void** p, size_t bytes, cudaStream_t s) {
+  *p = nullptr;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  cudaMemPool_t pool = nullptr;
+  e = pool_of(dev, &pool);
+  if (e != cudaSuccess) return e;
+  return cudaMallocFromPoolAsync(p, bytes ? bytes : 16, pool, s);
+}
+
+cudaError_t dev_free(void* p, cudaStream_t s) {
+  if (!p) return cudaSuccess;
+  return cudaFreeAsync(p, s);
+}
+
+}  // namespace lgt

@@ -14,21 +14,22 @@
 
 namespace lgt {
 
-// Device buffer owned by a handle, grown on demand.
+// Device buffer owned by a handle, grown on demand, in stream order on the
+// handle's stream (library pool, devmem.cu).
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
-  cudaError_t need(size_t b) {
+  cudaError_t need(size_t b, cudaStream_t s) {
     if (b <= bytes) return cudaSuccess;
-    cudaFree(p);
+    dev_free(p, s);
     p = nullptr;
     bytes = 0;
-    cudaError_t e = cudaMalloc(&p, b);
+    cudaError_t e = dev_alloc(&p, b, s);
     if (e == cudaSuccess) bytes = b;
     return e;
   }
-  void release() {
-    cudaFree(p);
+  void release(cudaStream_t s) {
+    dev_free(p, s);
     p = nullptr;
     bytes = 0;
   }

@@ -46,6 +46,16 @@ inline bool df_reductions_enabled() {
   return !(e && e[0] == '0');
 }
 
+// Stream-ordered device memory from the library's per-device pool
+// (devmem.cu): the allocation is usable by work enqueued on `s` after the
+// call; a free takes effect after the work enqueued on `s` before it.
+cudaError_t dev_alloc(void** p, size_t bytes, cudaStream_t s);
+cudaError_t dev_free(void* p, cudaStream_t s);
+template <typename T>
+cudaError_t dev_alloc_n(T** p, size_t n, cudaStream_t s) {
+  return dev_alloc(reinterpret_cast<void**>(p), n * sizeof(T), s);
+}
+
 // Two timing events destroyed with the scope, whatever path leaves it.
 struct EventPair {
   cudaEvent_t a = nullptr, b = nullptr;

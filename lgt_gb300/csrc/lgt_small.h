@@ -74,7 +74,7 @@ struct SmallWork {
 };
 
 std::string build_pattern(const BasisDev& B, uint32_t model, Pattern* P, cudaStream_t s);
-void free_pattern(Pattern* P);
+void free_pattern(Pattern* P, cudaStream_t s);
 
 // All (job, point) units in one launch, largest sectors first.
 std::string small_ground_states(const std::vector<SmallJob>& jobs, const SmallParams& prm,

@@ -646,13 +646,18 @@ std::string build_pattern(const BasisDev& B, uint32_t model, Pattern* P, cudaStr
   if (N > kSmallMaxN) return "sector too large for the per-CTA solver";
   P->N = int(N);
   P->model = model;
-  SCK(cudaMalloc(&P->rowptr, sizeof(int) * (N + 1)));
-  SCK(cudaMalloc(&P->e2, sizeof(int16_t) * (N + 1)));
-  SCK(cudaMalloc(&P->stag, sizeof(int16_t) * (N + 1)));
-  int* counts = nullptr;
-  SCK(cudaMalloc(&counts, sizeof(int) * (N + 1)));
-  const unsigned blocks = unsigned((N + 255) / 256);
+  // Stream-ordered: the neighbour array is sized for the most moves a row can
+  // have (at most kSmallMaxN rows, so a few MB at most) instead of reading
+  // the exact count back; the fill kernel checks its bounds.
   const Geom& G = B.G;
+  const size_t cap = size_t(N) * size_t(G.max_moves > 0 ? G.max_moves : 1);
+  SCK(dev_alloc_n(&P->rowptr, size_t(N) + 1, s));
+  SCK(dev_alloc_n(&P->e2, size_t(N) + 1, s));
+  SCK(dev_alloc_n(&P->stag, size_t(N) + 1, s));
+  SCK(dev_alloc_n(&P->nbr, cap + 1, s));
+  int* counts = nullptr;
+  SCK(dev_alloc_n(&counts, size_t(N) + 1, s));
+  const unsigned blocks = unsigned((N + 255) / 256);
   const RankView R = B.view();
   const bool plaq = model & kModelPlaq, jw = model & kModelJW;
   if (plaq && jw) k_pattern_count<true, true><<<blocks, 256, 0, s>>>(G, R, N, counts), lgt::note_launch();
@@ -660,11 +665,7 @@ std::string build_pattern(const BasisDev& B, uint32_t model, Pattern* P, cudaStr
   else if (jw) k_pattern_count<false, true><<<blocks, 256, 0, s>>>(G, R, N, counts), lgt::note_launch();
   else k_pattern_count<false, false><<<blocks, 256, 0, s>>>(G, R, N, counts), lgt::note_launch();
   k_scan_rows<<<1, 1024, 0, s>>>(counts, N, P->rowptr), lgt::note_launch();
-  int nnz = 0;
-  SCK(cudaMemcpyAsync(&nnz, P->rowptr + N, sizeof(int), cudaMemcpyDeviceToHost, s));
-  SCK(cudaStreamSynchronize(s));
-  P->nnz = nnz;
-  SCK(cudaMalloc(&P->nbr, sizeof(uint32_t) * (nnz + 1)));
+  P->nnz = -1;  // on the device (rowptr[N]); not needed on the host
   if (plaq && jw)
     k_pattern_fill<true, true><<<blocks, 256, 0, s>>>(G, R, N, P->rowptr, P->nbr, P->e2, P->stag, B.err), lgt::note_launch();
   else if (plaq)
@@ -674,16 +675,15 @@ std::string build_pattern(const BasisDev& B, uint32_t model, Pattern* P, cudaStr
   else
     k_pattern_fill<false, false><<<blocks, 256, 0, s>>>(G, R, N, P->rowptr, P->nbr, P->e2, P->stag, B.err), lgt::note_launch();
   SCK(cudaGetLastError());
-  SCK(cudaFreeAsync(counts, s));
-  SCK(cudaStreamSynchronize(s));
+  SCK(dev_free(counts, s));
   return std::string();
 }
 
-void free_pattern(Pattern* P) {
-  cudaFree(P->rowptr);
-  cudaFree(P->nbr);
-  cudaFree(P->e2);
-  cudaFree(P->stag);
+void free_pattern(Pattern* P, cudaStream_t s) {
+  dev_free(P->rowptr, s);
+  dev_free(P->nbr, s);
+  dev_free(P->e2, s);
+  dev_free(P->stag, s);
   *P = Pattern();
 }
 
@@ -719,10 +719,10 @@ std::string small_ground_states(const std::vector<SmallJob>& jobs, const SmallPa
   const size_t need = vbytes + xbytes + nunits * (sizeof(SmallUnit) + 8 * sizeof(double)) +
                       probs.size() * sizeof(SmallProblem) + 4096;
   if (ws->bytes < need) {
-    cudaFree(ws->base);
+    dev_free(ws->base, s);
     ws->base = nullptr;
     ws->bytes = 0;
-    SCK(cudaMalloc(&ws->base, need));
+    SCK(dev_alloc(&ws->base, need, s));
     ws->bytes = need;
   }
   char* base = static_cast<char*>(ws->base);
