@@ -77,8 +77,10 @@ enum {
   LGT_DEVICE_PTRS = 1, /* amplitude pointers are device pointers                  */
   LGT_ASYNC = 2,       /* with LGT_DEVICE_PTRS: lgt_matvec returns without waiting
                           for the kernel (stream-ordered; no self-check read)   */
-  LGT_GENERIC_KERNELS = 4 /* lgt_matvec: use the run-time-geometry H*psi kernel
+  LGT_GENERIC_KERNELS = 4, /* lgt_matvec: use the run-time-geometry H*psi kernel
                           even where a fixed-shape one exists (cross-checks)    */
+  LGT_ROW_ORDER = 8       /* lgt_matvec with LGT_DEVICE_PTRS: x and y are in the
+                          row order of lgt_ham_row_order (stored-table kernel) */
 };
 
 typedef struct lgt_basis lgt_basis;
@@ -207,6 +209,16 @@ LGT_API lgt_status lgt_ham_export_csr(const lgt_ham* h, int32_t k, int64_t* rowp
    precision LGT_FP64 (double) or LGT_FP32 (float). */
 LGT_API lgt_status lgt_matvec(const lgt_ham* h, const void* x, void* y, int32_t ncomp, int32_t precision,
                       uint32_t flags);
+
+/* The locality row order of the stored-table H*psi (no counterpart in the
+   reference): the rows in breadth-first order of the Hamiltonian's hop
+   graph, which the Krylov drivers use internally for their basis vectors
+   (the x gathers of a product then mostly hit L2).  Builds the neighbour
+   table and its renumbered copy on first use (LGT_ERR_UNSUPPORTED where the
+   table is not available).  perm: N int32 (may be NULL), perm[n] = the
+   0-based basis index of row n of that order.  lgt_matvec with
+   LGT_ROW_ORDER applies H to device panels kept in this order. */
+LGT_API lgt_status lgt_ham_row_order(lgt_ham* h, int32_t* perm);
 
 /* find_ground_state (finite_ed.jl:333-341) for all K points: lowest
    eigenpair by Lanczos with full reorthogonalisation.  E0: K doubles.  psi:

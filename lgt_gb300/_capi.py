@@ -38,6 +38,7 @@ LGT_SOLVER_CTA = 2
 LGT_DEVICE_PTRS = 1
 LGT_ASYNC = 2
 LGT_GENERIC_KERNELS = 4
+LGT_ROW_ORDER = 8
 
 # every symbol include/lgt_ed.h declares
 EXPORTS = (
@@ -46,6 +47,7 @@ EXPORTS = (
     "lgt_basis_lookup", "lgt_basis_rank", "lgt_basis_destroy", "lgt_basis_set_stream",
     "lgt_launch_count",
     "lgt_ham_create", "lgt_ham_set_couplings", "lgt_ham_nnz", "lgt_ham_export_csr",
+    "lgt_ham_row_order",
     "lgt_matvec", "lgt_ground_state", "lgt_ground_state_batch", "lgt_expm_steps",
     "lgt_expm_steps_grids", "lgt_observe",
     "lgt_observe_noalloc", "lgt_energy", "lgt_autotune", "lgt_ham_destroy",
@@ -152,6 +154,7 @@ def load(build_if_missing: bool = True):
         "lgt_ham_set_couplings": (i32, [vp, vp, vp, vp]),
         "lgt_ham_nnz": (i32, [vp, ctypes.POINTER(ctypes.c_int64)]),
         "lgt_ham_export_csr": (i32, [vp, i32, vp, vp, vp]),
+        "lgt_ham_row_order": (i32, [vp, vp]),
         "lgt_matvec": (i32, [vp, vp, vp, i32, i32, u32]),
         "lgt_ground_state": (i32, [vp, ctypes.POINTER(KrylovOpts), vp, vp, vp, u32,
                                    ctypes.POINTER(Info)]),

@@ -429,7 +429,19 @@ lgt_status lgt_matvec(const lgt_ham* hc, const void* x, void* y, int32_t ncomp, 
   }
   OpDev op = h->op();
   op.force_generic = (flags & LGT_GENERIC_KERNELS) ? 1 : 0;
-  if (!op.force_generic) {  // the autotuner's kernel for this shape (timed on first use)
+  if (flags & LGT_ROW_ORDER) {
+    if (!on_device(flags) || op.force_generic)
+      return fail(LGT_ERR_ARG, "LGT_ROW_ORDER needs LGT_DEVICE_PTRS and the table kernel");
+    // the tuner's load mode when it chose the table kernel, else the built-in one
+    std::string m =
+        (precision == LGT_FP64)
+            ? hpsi_choose_d(&op, static_cast<const double*>(dx), static_cast<double*>(dy), ncomp, s)
+            : hpsi_choose_f(&op, static_cast<const float*>(dx), static_cast<float*>(dy), ncomp, s);
+    if (!m.empty()) return from_msg(m);
+    if (!op.use_table) op.vpl = 0;
+    m = ensure_row_order(&op, s);
+    if (!m.empty()) return fail(LGT_ERR_UNSUPPORTED, m);
+  } else if (!op.force_generic) {  // the autotuner's kernel for this shape (timed on first use)
     std::string m =
         (precision == LGT_FP64)
             ? hpsi_choose_d(&op, static_cast<const double*>(dx), static_cast<double*>(dy), ncomp, s)
@@ -443,6 +455,22 @@ lgt_status lgt_matvec(const lgt_ham* hc, const void* x, void* y, int32_t ncomp, 
   if (on_device(flags) && (flags & LGT_ASYNC)) return LGT_OK;
   if (!on_device(flags)) CUDA_OR_FAIL(cudaMemcpyAsync(y, dy, bytes, cudaMemcpyDeviceToHost, s));
   CUDA_OR_FAIL(cudaStreamSynchronize(s));
+  return check_device_errors(h->b);
+}
+
+lgt_status lgt_ham_row_order(lgt_ham* h, int32_t* perm) {
+  if (!h) return fail(LGT_ERR_ARG, "null argument");
+  lgt_status st = set_device(h->b);
+  if (st) return st;
+  OpDev op = h->op();
+  cudaStream_t s = h->b->B.stream;
+  std::string m = ensure_row_order(&op, s);
+  if (!m.empty()) return fail(LGT_ERR_UNSUPPORTED, m);
+  if (perm) {
+    CUDA_OR_FAIL(cudaMemcpyAsync(perm, h->table_ord.perm, sizeof(int32_t) * h->b->B.dim,
+                                 cudaMemcpyDeviceToHost, s));
+    CUDA_OR_FAIL(cudaStreamSynchronize(s));
+  }
   return check_device_errors(h->b);
 }
 
@@ -966,6 +994,7 @@ void lgt_ham_destroy(lgt_ham* h) {
   h->out.release(s);
   free_pattern(&h->pattern, s);
   free_nbr_table(&h->table);
+  free_nbr_table(&h->table_ord);
   dev_free(h->small.base, s);
   dev_free(h->coef_d, s);
   dev_free(h->coef_f, s);

@@ -275,6 +275,7 @@ cudaError_t launch_hpsi(HpsiArgs<T> a, uint32_t model, cudaStream_t s) {
   const Geom& G = a.G;
   if (a.use_table && !a.force_generic && table_load_mode(a, nullptr))
     return launch_hpsi_table(a, model, s);
+  if (a.table_order) return cudaErrorInvalidValue;  // no other kernel knows that order
   if (!a.force_generic && hpsi_fixed_applies(a, nullptr)) {
     if (G.nx == 4 && G.ny == 4) return launch_hpsi_4x4(a, model, s);
     if (G.nx == 4 && G.ny == 3) return launch_hpsi_4x3(a, model, s);

@@ -531,7 +531,7 @@ __global__ void k_finish_norm(const double* npart, int nblk, int K, int C, int n
 template <typename SI, typename SO>
 __global__ void k_scale(const SI* src, SO* dstbase, size_t vstride, const int* jstate, int dst_off,
                         int64_t N, int C, int ncomp, const double* bnorm, const int* status,
-                        int sel) {
+                        int sel, const int* gather) {
   SO* dst = dstbase + size_t((jstate ? *jstate : 0) + dst_off) * vstride;
   const int RG = kT / C;
   const int c = threadIdx.x % C, rg = threadIdx.x / C;
@@ -543,10 +543,12 @@ __global__ void k_scale(const SI* src, SO* dstbase, size_t vstride, const int* j
   const float invf = float(inv);
   for (int64_t row = int64_t(blockIdx.x) * RG + rg; row < N; row += int64_t(gridDim.x) * RG) {
     const size_t i = size_t(row) * C + c;
+    // gather: row `row` of the destination is row gather[row] of the source
+    const size_t si = gather ? size_t(gather[row]) * C + c : i;
     if (sizeof(SI) == 4 && sizeof(SO) == 4)
-      dst[i] = SO(float(src[i]) * invf);
+      dst[i] = SO(float(src[si]) * invf);
     else
-      dst[i] = SO(double(src[i]) * inv);
+      dst[i] = SO(double(src[si]) * inv);
   }
 }
 
@@ -747,7 +749,7 @@ __global__ void k_check_expm(const double* alpha, const double* beta, int ldT, i
 template <typename S, int NC>
 __global__ void k_combine(const S* __restrict__ V, size_t vstride, const double* coef, int ldT,
                           const int* len, const int* status, int sel, double* out, int64_t N,
-                          int C, int ncomp) {
+                          int C, int ncomp, const int* scatter) {
   const int64_t n = N * C;
   for (int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; idx < n;
        idx += int64_t(gridDim.x) * blockDim.x) {
@@ -769,7 +771,8 @@ __global__ void k_combine(const S* __restrict__ V, size_t vstride, const double*
         acc += (c & 1) ? (cr * v + ci * vp) : (cr * v - ci * vp);
       }
     }
-    out[off + c] = acc;
+    // scatter: row `row` of the basis is row scatter[row] of the output
+    out[(scatter ? size_t(scatter[row]) * C : off) + c] = acc;
   }
 }
 
@@ -778,7 +781,8 @@ __global__ void k_combine(const S* __restrict__ V, size_t vstride, const double*
 // tridiagonal): psi_k = sum_i c^re_i V_i[2k] + i sum_i c^im_i V_i[2k+1].
 template <typename S>
 __global__ void k_combine_split(const S* __restrict__ V, size_t vstride, const double* coef,
-                                int ldT, const int* len, double* out, int64_t N, int K) {
+                                int ldT, const int* len, double* out, int64_t N, int K,
+                                const int* scatter) {
   const int C = 2 * K;
   const int64_t n = N * C;
   for (int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; idx < n;
@@ -799,7 +803,7 @@ __global__ void k_combine_split(const S* __restrict__ V, size_t vstride, const d
                              : -coef[(size_t(cb) * ldT + i) * 2 + 1];
       acc = fma(cf, widen(V[size_t(i) * vstride + off + cb]), acc);
     }
-    out[off + c] = acc;
+    out[(scatter ? size_t(scatter[row]) * C : off) + c] = acc;
   }
 }
 
@@ -899,6 +903,7 @@ struct Work {
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0, graph_reorth = 0;
   double graph_tiny = 0.0;
+  uint64_t graph_op = 0;
   int graph_nodes = 0;
 
   std::string ensure(int64_t N_, int C_, int K_, int ncomp_, int m_, int hcomp_ = 0,
@@ -989,7 +994,9 @@ cudaError_t apply_h(const OpDev& op, const S* x, const int* xsel, size_t xstride
 
 template <typename S>
 void set_table(const OpDev& op, HpsiArgs<S>* a) {
-  const NbrTable* T = op.table;
+  const bool ord = op.krylov_order && op.table_ord && op.table_ord->state == 1;
+  const NbrTable* T = ord ? op.table_ord : op.table;
+  a->table_order = ord ? 1 : 0;
   if (!op.use_table || !T || T->state != 1) return;
   a->t_meta = T->meta;
   a->t_off = T->tile_off;
@@ -1048,6 +1055,21 @@ cudaError_t apply_h<float>(const OpDev& op, const float* x, const int* xsel, siz
   a.vpl = op.vpl;
   set_table(op, &a);
   return launch_hpsi<float>(a, op.model, s);
+}
+
+// Whether the table kernel accepts the driver's H*psi panels (the Krylov
+// basis with its device-resident panel offset): the condition for keeping
+// the Krylov vectors in the table's row order.
+template <typename S>
+bool table_serves(const OpDev& op, const Work<S>& w) {
+  HpsiArgs<S> a;
+  a.x = w.V;
+  a.y = w.W;
+  a.C = op.K * w.hcomp;
+  a.xsel = w.jstate;
+  a.xstride = w.vstride;
+  a.t_meta = op.table_ord ? op.table_ord->meta : nullptr;
+  return table_load_mode(a, nullptr);
 }
 
 template <typename S, typename SV>
@@ -1126,7 +1148,7 @@ cudaError_t lanczos_step(const OpDev& op, Work<S>& w, int reorth, double tiny_re
                                                tiny_rel, 1), lgt::note_launch();
   k_scale<S, S><<<grid_for(int64_t(w.vstride)), kT, 0, s>>>(w.W, w.V, w.vstride, w.jstate, 1, w.N,
                                                             w.C, w.ncomp, w.bnorm, w.status,
-                                                            kActive), lgt::note_launch();
+                                                            kActive, nullptr), lgt::note_launch();
   k_advance<<<1, 1, 0, s>>>(w.jstate), lgt::note_launch();
   return cudaGetLastError();
 }
@@ -1232,7 +1254,25 @@ bool ensure_table(OpDev* op, cudaStream_t s) {
     T->state = -1;
     return false;
   }
+  // the renumbered copy for the Krylov drivers (LGT_TABLE_ORDER=0: none),
+  // when a second table fits the same budget
+  NbrTable* T2 = op->table_ord;
+  if (T2 && T2->state == 0) {
+    const char* eo = getenv("LGT_TABLE_ORDER");
+    if ((eo && eo[0] == '0') || 2 * bound > cap) {
+      T2->state = -1;
+    } else if (!build_table_order(*T, T2, s).empty()) {
+      free_nbr_table(T2);
+      T2->state = -1;
+    }
+  }
   return true;
+}
+
+// Whether the Krylov drivers keep their vectors in the table's row order:
+// the table kernel is chosen and its renumbered copy exists.
+bool use_krylov_order(const OpDev& op) {
+  return op.use_table && op.table_ord && op.table_ord->state == 1 && op.table_ord->perm;
 }
 
 // The H*psi variant forced by LGT_HPSI_VARIANT (1..7), or 0.
@@ -1321,6 +1361,7 @@ std::string tune_hpsi(OpDev* op, const S* x, S* y, int C, int hcomp, cudaStream_
   for (int v : cand) {
     OpDev o = *op;
     apply_variant(&o, v);
+    o.krylov_order = use_krylov_order(o) ? 1 : 0;  // the table the drivers will use
     e = apply_h<S>(o, x, nullptr, 0, y, hcomp, s);  // warm-up
     if (e == cudaSuccess) e = cudaEventRecord(e0, s);
     for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = apply_h<S>(o, x, nullptr, 0, y, hcomp, s);
@@ -1468,8 +1509,12 @@ template <typename S>
 std::string run_steps(const OpDev& op, Work<S>& w, const KrylovParams& p, int steps,
                       double tiny_rel, cudaStream_t s, int64_t* matvecs) {
   if (steps <= 0) return std::string();
+  // a captured sequence is replayed only for the same step count, passes,
+  // threshold and operator (kernel variant, row order)
+  const uint64_t opkey = (uint64_t(op.krylov_order) << 8) ^ (uint64_t(op.use_table) << 9) ^
+                         (uint64_t(op.force_generic) << 10) ^ (uint64_t(op.vpl) << 11);
   const bool cached = w.graph && w.graph_steps == steps && w.graph_reorth == p.reorth &&
-                      w.graph_tiny == tiny_rel;
+                      w.graph_tiny == tiny_rel && w.graph_op == opkey;
   if (p.use_graph && steps == p.check_every && cached) {
     KCK(cudaGraphLaunch(w.graph, s));
     note_launch(w.graph_nodes);
@@ -1478,6 +1523,7 @@ std::string run_steps(const OpDev& op, Work<S>& w, const KrylovParams& p, int st
     if (p.use_graph && steps == p.check_every) {
       std::string err = capture_steps<S>(op, w, steps, p.reorth, tiny_rel, s);
       if (!err.empty()) return err;
+      w.graph_op = opkey;
     }
   }
   *matvecs += steps;
@@ -1485,12 +1531,14 @@ std::string run_steps(const OpDev& op, Work<S>& w, const KrylovParams& p, int st
 }
 
 // V_0 = X / ||X|| for active points (X double, storage S); rho = ||X||.
+// perm: the Krylov row order (V_0 row n = X row perm[n]), or null.
 template <typename S>
-std::string start_from(Work<S>& w, const double* X, cudaStream_t s) {
+std::string start_from(Work<S>& w, const double* X, cudaStream_t s, const int* perm) {
   std::string err = colnorms_double<S>(w, X, w.rho, s);
   if (!err.empty()) return err;
   k_scale<double, S><<<grid_for(int64_t(w.vstride)), kT, 0, s>>>(
-      X, w.V, w.vstride, nullptr, 0, w.N, w.C, w.ncomp, w.rho, w.status, kActive), lgt::note_launch();
+      X, w.V, w.vstride, nullptr, 0, w.N, w.C, w.ncomp, w.rho, w.status, kActive, perm),
+      lgt::note_launch();
   KCK(cudaGetLastError());
   return std::string();
 }
@@ -1523,6 +1571,11 @@ std::string ground_state_impl(const OpDev& op_in, const KrylovParams& p, Work<S>
   }
   err = autotune<S>(&op, w, s, nullptr);
   if (!err.empty()) return err;
+  // the Krylov vectors in the table's row order when its kernel was chosen
+  // and serves these panels: X is gathered into V_0 and the combinations
+  // scattered back
+  op.krylov_order = (use_krylov_order(op) && table_serves(op, w)) ? 1 : 0;
+  const int* perm = op.krylov_order ? op.table_ord->perm : nullptr;
   const bool fp32 = sizeof(S) == 4;
   const double tiny_rel = fp32 ? 1e-6 : 1e-12;
   // FP32 panels cannot resolve residuals much below 1e-6 |H|: the inner
@@ -1542,7 +1595,7 @@ std::string ground_state_impl(const OpDev& op_in, const KrylovParams& p, Work<S>
   }
   err = reset_cycle<S>(w, s);
   if (!err.empty()) return err;
-  err = start_from<S>(w, X, s);
+  err = start_from<S>(w, X, s, perm);
   if (!err.empty()) return err;
 
   std::vector<int> st(K);
@@ -1570,14 +1623,14 @@ std::string ground_state_impl(const OpDev& op_in, const KrylovParams& p, Work<S>
       // keep the points that converged in this cycle, restart the others
       // from their current Ritz vectors
       k_combine<S, 1><<<grid_for(N * C), kT, 0, s>>>(w.V, w.vstride, w.coef, w.ldT, w.len,
-                                                     w.status, kConverged, X, N, C, ncomp), lgt::note_launch();
+                                                     w.status, kConverged, X, N, C, ncomp, perm), lgt::note_launch();
       k_set_int<<<(K + 127) / 128, 128, 0, s>>>(w.status, K, kWritten, w.status, kConverged), lgt::note_launch();
       k_combine<S, 1><<<grid_for(N * C), kT, 0, s>>>(w.V, w.vstride, w.coef, w.ldT, w.len,
-                                                     w.status, kActive, X, N, C, ncomp), lgt::note_launch();
+                                                     w.status, kActive, X, N, C, ncomp, perm), lgt::note_launch();
       KCK(cudaGetLastError());
       err = reset_cycle<S>(w, s);
       if (!err.empty()) return err;
-      err = start_from<S>(w, X, s);
+      err = start_from<S>(w, X, s, perm);
       if (!err.empty()) return err;
       j = 0;
       ++restarts;
@@ -1587,7 +1640,8 @@ std::string ground_state_impl(const OpDev& op_in, const KrylovParams& p, Work<S>
   k_set_int<<<(K + 127) / 128, 128, 0, s>>>(w.status, K, kConverged, w.status, kActive), lgt::note_launch();
   k_set_int<<<(K + 127) / 128, 128, 0, s>>>(w.status, K, kConverged, w.status, kExhausted), lgt::note_launch();
   k_combine<S, 1><<<grid_for(N * C), kT, 0, s>>>(w.V, w.vstride, w.coef, w.ldT, w.len, w.status,
-                                                 kConverged, X, N, C, ncomp), lgt::note_launch();
+                                                 kConverged, X, N, C, ncomp, perm),
+      lgt::note_launch();
   KCK(cudaGetLastError());
   std::vector<double> theta(K);
   KCK(cudaMemcpyAsync(theta.data(), w.theta, sizeof(double) * K, cudaMemcpyDeviceToHost, s));
@@ -1597,9 +1651,11 @@ std::string ground_state_impl(const OpDev& op_in, const KrylovParams& p, Work<S>
   err = colnorms_double<S>(w, X, w.rho, s);
   if (!err.empty()) return err;
   k_scale<double, double><<<grid_for(N * C), kT, 0, s>>>(X, X, 0, nullptr, 0, N, C, ncomp, w.rho,
-                                                          nullptr, 0), lgt::note_launch();
+                                                          nullptr, 0, nullptr), lgt::note_launch();
   KCK(cudaGetLastError());
-  KCK(apply_h<double>(op, X, nullptr, 0, w.R, ncomp, s));
+  OpDev op_ref = op;  // X is in the reference order here
+  op_ref.krylov_order = 0;
+  KCK(apply_h<double>(op_ref, X, nullptr, 0, w.R, ncomp, s));
   ++matvecs;
   std::vector<double> erq(K), r2(K);
   err = dots_ws<S>(w, X, w.R, erq.data(), s);
@@ -1661,6 +1717,11 @@ std::string expm_impl(const OpDev& op_in, const KrylovParams& p, Work<S>& w, dou
   }
   err = autotune<S>(&op, w, s, nullptr);
   if (!err.empty()) return err;
+  // the Krylov vectors in the table's row order when its kernel was chosen
+  // and serves these panels: X is gathered into V_0 and the combinations
+  // scattered back
+  op.krylov_order = (use_krylov_order(op) && table_serves(op, w)) ? 1 : 0;
+  const int* perm = op.krylov_order ? op.table_ord->perm : nullptr;
   const double tiny_rel = (sizeof(S) == 8) ? 1e-12 : 1e-6;
   const double tol = p.tol / sqrt(2.0);
   std::vector<int> st(Kc);
@@ -1696,7 +1757,7 @@ std::string expm_impl(const OpDev& op_in, const KrylovParams& p, Work<S>& w, dou
       if (!err.empty()) return err;
       // V_0 = column / ||column|| (a zero column, e.g. Im psi = 0, spans an
       // empty Krylov space: it is exhausted at once and contributes 0)
-      err = start_from<S>(w, X, s);
+      err = start_from<S>(w, X, s, perm);
       if (!err.empty()) return err;
       int j = 0;
       bool all = false;
@@ -1738,7 +1799,7 @@ std::string expm_impl(const OpDev& op_in, const KrylovParams& p, Work<S>& w, dou
       }
       KCK(cudaMemcpyAsync(errs.data(), w.resid, sizeof(double) * Kc, cudaMemcpyDeviceToHost, s));
       k_combine_split<S><<<grid_for(N * C), kT, 0, s>>>(w.V, w.vstride, w.coef, w.ldT, w.len, X, N,
-                                                        K), lgt::note_launch();
+                                                        K, perm), lgt::note_launch();
       KCK(cudaGetLastError());
       KCK(cudaStreamSynchronize(s));
       for (int k = 0; k < K; ++k) maxerr = fmax(maxerr, hypot(errs[2 * k], errs[2 * k + 1]));
@@ -1753,7 +1814,7 @@ std::string expm_impl(const OpDev& op_in, const KrylovParams& p, Work<S>& w, dou
                                                w.alpha, w.ldT, w.status, w.len, w.rho, 0.0,
                                                0), lgt::note_launch();
     k_scale<double, double><<<grid_for(N * C), kT, 0, s>>>(X, X, 0, nullptr, 0, N, C, 2, w.rho,
-                                                            nullptr, 0), lgt::note_launch();
+                                                            nullptr, 0, nullptr), lgt::note_launch();
     KCK(cudaGetLastError());
     if (drift) {
       KCK(cudaMemcpyAsync(nrm.data(), w.rho, sizeof(double) * K, cudaMemcpyDeviceToHost, s));
@@ -1821,6 +1882,16 @@ std::string krylov_autotune(const OpDev& op_in, KrylovCache* cache, int ncomp, i
     cache->tune_d.release();
   }
   return err;
+}
+
+std::string ensure_row_order(OpDev* op, cudaStream_t s) {
+  if (!ensure_table(op, s)) return "the stored neighbour table is not available for this basis";
+  if (!op->table_ord || op->table_ord->state != 1 || !op->table_ord->perm)
+    return "the table's row order is not available (LGT_TABLE_ORDER=0 or memory budget)";
+  op->use_table = 1;
+  op->force_generic = 0;
+  op->krylov_order = 1;
+  return std::string();
 }
 
 KrylovCache* krylov_cache_new() { return new KrylovCache(); }

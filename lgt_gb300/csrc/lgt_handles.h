@@ -108,6 +108,7 @@ struct lgt_ham {
   // neighbour table of the panel H*psi (built on demand by the autotuner;
   // mutable: op() hands out a pointer through which it is built)
   mutable lgt::NbrTable table;
+  mutable lgt::NbrTable table_ord;  // the same renumbered to its row order (order.cu)
   OpDev op() const {
     OpDev o;
     o.G = b->B.G;
@@ -125,6 +126,7 @@ struct lgt_ham {
     o.ch_f = coef_f + 2 * K;
     o.cp_f = coef_f + 3 * K;
     o.table = &table;
+    o.table_ord = &table_ord;
     return o;
   }
 };

@@ -37,6 +37,9 @@ struct HpsiArgs {
   const uint32_t* t_nbr = nullptr;
   int t_mm = 0;           // most entries a row can have
   int use_table = 0;
+  // the panels are in the table's own row order (a renumbered table): only
+  // the table kernel may run; anything else is an error, not a fallback
+  int table_order = 0;
 };
 
 // The neighbour ranks of every row of a basis for one model, kept in HBM
@@ -50,6 +53,10 @@ struct NbrTable {
   uint32_t* nbr = nullptr;
   size_t bytes = 0;
   int state = 0;  // 0 not built, 1 built, -1 declined (size or representability)
+  // A renumbered copy (order.cu) also holds its row order: perm[new] = old
+  // row, iperm[old] = new row.
+  int* perm = nullptr;
+  int* iperm = nullptr;
 };
 
 // Whether the basis fits the table format (N < 2^31, fewer than 2^32
@@ -59,6 +66,11 @@ bool nbr_table_eligible(const Geom& G, int64_t N, uint32_t model, size_t* bytes)
 std::string build_nbr_table(const Geom& G, const RankView& R, uint32_t model, int* err,
                             NbrTable* T, cudaStream_t s);
 void free_nbr_table(NbrTable* T);
+
+// T renumbered to the breadth-first row order of its hop graph (order.cu):
+// T2 receives the renumbered table with its perm / iperm.  One-time cost per
+// Hamiltonian (a host read per search level).
+std::string build_table_order(const NbrTable& T, NbrTable* T2, cudaStream_t s);
 
 // Whether the table kernel serves these arguments (table present, vector-
 // aligned panels) and its widest load mode (as hpsi_fixed_applies).

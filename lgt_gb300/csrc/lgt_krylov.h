@@ -23,6 +23,11 @@ struct OpDev {
   int vpl = 0;            // fixed-shape H*psi: vector loads per lane (0: by width)
   NbrTable* table = nullptr;  // the Hamiltonian's neighbour table (built on demand)
   int use_table = 0;          // H*psi from the stored table
+  // The table renumbered to its breadth-first row order (order.cu), built
+  // with the table; the Krylov drivers keep their basis vectors in that
+  // order (krylov_order = 1) when the table kernel is chosen.
+  NbrTable* table_ord = nullptr;
+  int krylov_order = 0;
 };
 
 struct KrylovParams {
@@ -106,6 +111,11 @@ struct StepObserver {
 std::string krylov_expm(const OpDev& op, const KrylovParams& p, KrylovCache* cache, double dt,
                         int n_steps, double* X, double* norm_drift, StepObserver* obs,
                         cudaStream_t s, KrylovReport* rep);
+
+// Builds (on first use) the stored neighbour table and its renumbered copy
+// and sets op to apply H in that row order (table kernel, krylov_order).
+// Returns an empty string, or why the order is not available.
+std::string ensure_row_order(OpDev* op, cudaStream_t s);
 
 // y = H x on a double or float panel (C = K * ncomp columns).
 cudaError_t apply_h_d(const OpDev& op, const double* x, double* y, int ncomp, cudaStream_t s);

@@ -284,6 +284,8 @@ void free_nbr_table(NbrTable* T) {
   cudaFree(T->meta);
   cudaFree(T->tile_off);
   cudaFree(T->nbr);
+  cudaFree(T->perm);
+  cudaFree(T->iperm);
   *T = NbrTable();
 }
 

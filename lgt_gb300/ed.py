@@ -350,10 +350,21 @@ class Hamiltonian:
             y = py
         return y.reshape(xin.shape)
 
+    def row_order(self) -> np.ndarray:
+        """The locality row order of the stored-table product (rows in
+        breadth-first order of the hop graph): perm[n] is the basis index of
+        row n of that order.  The Krylov drivers keep their vectors in it."""
+        perm = np.zeros(self.basis.dim, np.int32)
+        C.check(C.load().lgt_ham_row_order(self._h, _p(perm)))
+        return perm
+
     def matvec_device(self, x_ptr: int, y_ptr: int, ncomp: int = 1, precision="fp64",
-                      generic=False):
-        """y = H x on device panels [N][K][ncomp] (raw device pointers)."""
+                      generic=False, row_order=False):
+        """y = H x on device panels [N][K][ncomp] (raw device pointers);
+        row_order: the panels are in the order of row_order()."""
         flags = C.LGT_DEVICE_PTRS | (C.LGT_GENERIC_KERNELS if generic else 0)
+        if row_order:
+            flags |= C.LGT_ROW_ORDER
         C.check(C.load().lgt_matvec(self._h, ctypes.c_void_p(x_ptr), ctypes.c_void_p(y_ptr),
                                     ncomp, _PREC[precision], flags))
 
