@@ -188,11 +188,13 @@ def gpu_workloads(args, rank, world):
     E_ref = np.array([O.ground_state(O.build_hamiltonian(ob, g=g, t=T_HOP, m=MASS))[0]
                       for g in gs])
 
-    def run_gs(H, precision, psi_dev, steps, warmup, count_launches=False, clocks=None):
+    def run_gs(H, precision, psi_dev, steps, warmup, count_launches=False, clocks=None,
+               refine=0):
         """Timed batched solves: ground state + observables, device panels."""
         o = C.defaults(False)
         o.precision = {"fp64": C.LGT_FP64, "mixed": C.LGT_FP32_MIXED}[precision]
         o.seed = 0
+        o.refine_steps = refine
         E0 = np.zeros(H.K)
         info = C.Info()
         summ = (C.Obs * H.K)()
@@ -215,6 +217,7 @@ def gpu_workloads(args, rank, world):
             if it >= warmup:
                 times.append(e0.elapsed_time(e1) * 1e-3)
         launches = C.launch_count() - l0
+        run_gs.last_obs = np.frombuffer(summ, dtype=np.float64).reshape(H.K, 8).copy()
         return times, E0.copy(), launches, info
 
     # ---- headline: batched FP32-mixed, reference model -----------------------
@@ -224,6 +227,18 @@ def gpu_workloads(args, rank, world):
         t_mix, E_mix, launches, info_mix = run_gs(H, "mixed", psi, args.steps, args.warmup)
     clocks = clk.summary()
     dE_mix = float(np.max(np.abs(E_mix - E_ref) / np.abs(E_ref)))
+
+    obs_mix = run_gs.last_obs
+    # the same with the FP64 correction (a short FP64 Lanczos from the FP32
+    # solution): its cost, and the observables' error against the oracle
+    t_mref, E_mref, _, _ = run_gs(H, "mixed", psi, max(3, args.steps // 4), 2, refine=12)
+    obs_mref = run_gs.last_obs
+    dE_mref = float(np.max(np.abs(E_mref - E_ref) / np.abs(E_ref)))
+    o_ref = [O.measure(O.ground_state(O.build_hamiltonian(ob, g=g, t=T_HOP, m=MASS))[1], ob)
+             for g in gs[:16]]
+    okeys = ((4, "E2_mean"), (5, "plaq_mean"))  # lgt_obs fields
+    dobs_mix = max(abs(obs_mix[k, c] - o_ref[k][q]) for k in range(16) for c, q in okeys)
+    dobs_mref = max(abs(obs_mref[k, c] - o_ref[k][q]) for k in range(16) for c, q in okeys)
 
     # ---- batched FP64 and plain (one point per solve) FP64 -------------------
     t_b64, E_b64, _, info_b64 = run_gs(H, "fp64", psi, max(3, args.steps // 4), 2)
@@ -292,6 +307,7 @@ def gpu_workloads(args, rank, world):
                 t_pjw=t_pjw, dE_pjw=dE_pjw, e2e_times=e2e_times, e2e_reuse=e2e_reuse,
                 h2d=h2d, d2h=d2h,
                 dE_e2e=dE_e2e, basis_ms=basis_ms, N=N, rf=rf, quench=qn,
+                t_mref=t_mref, dE_mref=dE_mref, dobs_mix=dobs_mix, dobs_mref=dobs_mref,
                 matvecs_mix=info_mix.matvecs, restarts_mix=info_mix.restarts)
 
 
@@ -452,9 +468,11 @@ def extra_configs(L, pool, dev, reps=3):
     c3 = {}
     for model in ("ref", "pjw"):
         H = L.build_hamiltonian(b, kd, 4, 3, 1, g=0.8, t=1.0, m=0.3, model=model)
-        for prec in ("fp64", "fp32_mixed"):
+        for prec in ("fp64", "fp32_mixed", "fp32_mixed_refined"):
             t0 = time.perf_counter()
-            E, psi = L.find_ground_state(H, precision=prec, as_complex=False)
+            E, psi = L.find_ground_state(H, precision=prec.replace("_refined", ""),
+                                         refine_steps=12 if prec.endswith("refined") else 0,
+                                         as_complex=False)
             o = L.measure_ED(psi, b, 4, 3, 1, 0.0)
             c3["%s_%s" % (model, prec)] = {"E0": E, "E2_mean": o["E2_mean"],
                                            "n_stag": o["n_stag"],
@@ -492,7 +510,7 @@ def extra_configs(L, pool, dev, reps=3):
     c3e = {}
     for q, model in enumerate(("ref", "pjw")):
         E0o, E2o, nso = ref[1 + q]
-        for prec in ("fp64", "fp32_mixed"):
+        for prec in ("fp64", "fp32_mixed", "fp32_mixed_refined"):
             r = c3["%s_%s" % (model, prec)]
             c3e["%s_%s" % (model, prec)] = {
                 "rel_dE0": abs(r["E0"] - E0o) / abs(E0o), "abs_dE2": abs(r["E2_mean"] - E2o),
@@ -552,7 +570,7 @@ def roofline(L, C, lib, torch, stream, dev, reps=10, only=None):
     out = {"N": N, "basis_build_s": basis_s}
     # variants: the autotuner's choice, and each kernel family forced
     # (LGT_HPSI_VARIANT: 3 fixed shape, 6 stored table; two vectors per lane)
-    forced = {"": None, "_generic": None, "_fixed": "3", "_table": "6"}
+    forced = {"": None, "_generic": None, "_fixed": "3", "_table": "6", "_table_ordered": "6"}
     models, precs = ("ref", "pjw"), (("fp64", torch.float64, 16), ("fp32", torch.float32, 8))
     if only is not None:
         sfx = "" if only == "auto" else "_" + only
@@ -566,16 +584,24 @@ def roofline(L, C, lib, torch, stream, dev, reps=10, only=None):
         # stored table: meta word per row, offset per 32 rows, 4 bytes per
         # off-diagonal entry (the CSR count less the diagonal)
         table_bytes = 4 * (N + (N + 31) // 32 + 1 + (nnz.value - N))
+        perm = None
         for prec, dtype, s in precs:
             for suffix, var in forced.items():
                 generic = suffix == "_generic"
+                ordered = suffix == "_table_ordered"
                 if var is None:
                     os.environ.pop("LGT_HPSI_VARIANT", None)
                 else:
                     os.environ["LGT_HPSI_VARIANT"] = var
                 x = torch.randn((N, RF_K, 2), dtype=dtype, device="cuda")
+                if ordered:  # the panel kept in the table's row order (as the Krylov drivers do)
+                    if perm is None:
+                        perm = torch.from_numpy(H.row_order().astype(np.int64)).cuda()
+                    x = x[perm].contiguous()
                 y = torch.empty_like(x)
                 flags = C.LGT_DEVICE_PTRS | C.LGT_ASYNC | (C.LGT_GENERIC_KERNELS if generic else 0)
+                if ordered:
+                    flags |= C.LGT_ROW_ORDER
                 code = C.LGT_FP64 if prec == "fp64" else C.LGT_FP32
                 ts = []
                 for it in range(reps + 2):
@@ -592,6 +618,8 @@ def roofline(L, C, lib, torch, stream, dev, reps=10, only=None):
                 t = statistics.mean(ts)
                 if generic:
                     kernel = "generic"
+                elif ordered:
+                    kernel = "table_ordered_vpl2"
                 elif var is not None:
                     kernel = "fixed_vpl2" if var == "3" else "table_vpl2"
                 else:  # the autotuner's kernel for this shape (chosen at the first call)
@@ -634,7 +662,8 @@ def main():
     ap.add_argument("--detail", default=None,
                     help="also write every measured figure (roofline variants, per-config "
                          "detail, quench trajectories' summaries) to this JSON file")
-    ap.add_argument("--hpsi-only", default=None, choices=["auto", "generic", "fixed", "table"],
+    ap.add_argument("--hpsi-only", default=None,
+                    choices=["auto", "generic", "fixed", "table", "table_ordered"],
                     help="--part hpsi: time one kernel family on the reference FP32 panel")
     ap.add_argument("--part", default="all", choices=["all", "hpsi", "gs", "quench"],
                     help="hpsi: only the 4x4 H*psi roofline loop; gs: only the headline "
@@ -731,8 +760,12 @@ def main():
     extra = extra_configs(L, pool, int(os.environ.get("LOCAL_RANK", "0")))
     pool.close()
     rf = r["rf"]
+    # the dominant kernel: the FP32 product the mixed quench runs -- the
+    # autotuner's choice, in the table's row order when that is the table
     dom = rf["ref_fp32"]
     fam = "table" if dom["kernel"].startswith("table") else "fixed"
+    if fam == "table" and "ref_fp32_table_ordered" in rf:
+        dom, fam = rf["ref_fp32_table_ordered"], "table_ordered"
     traffic = RF_TRAFFIC_BYTES.get(fam) if dom["kernel"] != "generic" else None
     e2e_val = KPTS / statistics.mean(r["e2e_times"])
     qn = r["quench"]
@@ -750,7 +783,7 @@ def main():
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "basis_build_ms": _r(r["basis_ms"])},
         "roofline": {"kernel": "k_hpsi_%s (%s), 4x4 N=8563545 K=8 complex FP32, ref model"
-                               % (fam, dom["kernel"]),
+                               % ("table" if fam.startswith("table") else "fixed", dom["kernel"]),
                      "bound": "hbm", "achieved": _r(dom["gbs"]), "peak": rf["peak"],
                      "unit": "GB/s", "frac": _r(dom["frac"]), "traffic": traffic,
                      "algo_bytes_per_launch": dom["algo_bytes"], "ms_per_launch": _r(dom["ms"]),
@@ -771,7 +804,7 @@ def main():
             "c1_rel_dE": _r(extra["c1_3x2_fp64_tol1e-12"]["rel_dE"]),
             "c3_4x3": {k: [_r(v["rel_dE0"]), _r(v["abs_dE2"]), _r(v["abs_dn_stag"])]
                        for k, v in c3.items()},
-            "c3_cols": "rel dE0, abs dE2, abs dn_stag vs FP64 oracle",
+            "c3_cols": "rel dE0, abs dE2, abs dn_stag vs FP64 oracle; refined: 12 FP64 steps",
             "c4_gs_per_s": _r(c4["gs_per_s_incl_host_copies"]),
             "c4_min_max": [_r(v) for v in c4["gs_per_s_min_max"]],
             "c4_cpu_gs_per_s": _r(c4["cpu_baseline_gs_per_s"]),
@@ -784,12 +817,16 @@ def main():
                                         for p in ("fp64", "fp32_mixed")},
                        "mixed_vs_fp64": {k: _r(v) for k, v in qn["mixed_vs_fp64_max_abs"].items()}},
         "accuracy": {"max_rel_dE_fp32_mixed": _r(r["dE_mix"]),
+                     "max_abs_dobs_mixed_16pts": _r(r["dobs_mix"]),
+                     "max_rel_dE_mixed_refined": _r(r["dE_mref"]),
+                     "max_abs_dobs_mixed_refined_16pts": _r(r["dobs_mref"]),
                      "max_rel_dE_fp64_batched": _r(r["dE_b64"]),
                      "max_rel_dE_fp64_plain": _r(r["dE_plain"]),
                      "max_rel_dE_pjw_mixed_8pts": _r(r["dE_pjw"]),
                      "max_rel_dE_e2e": _r(r["dE_e2e"]), "vs": "FP64 oracle, dense eigh"},
         "arms": {
             "fp32_mixed_batched_gs_per_s": _r(value),
+            "fp32_mixed_refined_gs_per_s": _r(KPTS / statistics.mean(r["t_mref"])),
             "fp64_batched_gs_per_s": _r(KPTS / statistics.mean(r["t_b64"])),
             "fp64_plain_gs_per_s": _r(1.0 / statistics.mean(r["plain_times"])),
             "speedup_vs_plain_fp64": _r(value * statistics.mean(r["plain_times"])),
