@@ -1254,16 +1254,23 @@ bool ensure_table(OpDev* op, cudaStream_t s) {
     T->state = -1;
     return false;
   }
-  // the renumbered copy for the Krylov drivers (LGT_TABLE_ORDER=0: none),
-  // when a second table fits the same budget
+  // the renumbered copy for the Krylov drivers, when a second table fits the
+  // same budget: mask segments in breadth-first order (default),
+  // LGT_TABLE_ORDER=row the row-level order, LGT_TABLE_ORDER=0 none
   NbrTable* T2 = op->table_ord;
   if (T2 && T2->state == 0) {
     const char* eo = getenv("LGT_TABLE_ORDER");
-    if ((eo && eo[0] == '0') || 2 * bound > cap) {
+    const bool none = eo && eo[0] == '0';
+    const bool rows = eo && eo[0] == 'r';
+    if (none || 2 * bound > cap) {
       T2->state = -1;
-    } else if (!build_table_order(*T, T2, s).empty()) {
-      free_nbr_table(T2);
-      T2->state = -1;
+    } else {
+      const std::string e2 = rows ? build_table_order(*T, T2, s)
+                                  : build_table_mask_order(*T, op->G, op->R, T2, s);
+      if (!e2.empty()) {
+        free_nbr_table(T2);
+        T2->state = -1;
+      }
     }
   }
   return true;

@@ -71,6 +71,10 @@ void free_nbr_table(NbrTable* T);
 // T2 receives the renumbered table with its perm / iperm.  One-time cost per
 // Hamiltonian (a host read per search level).
 std::string build_table_order(const NbrTable& T, NbrTable* T2, cudaStream_t s);
+// The same with the fermion-mask segments ordered breadth-first over the
+// mask graph and the rows of a segment kept in order (order.cu).
+std::string build_table_mask_order(const NbrTable& T, const Geom& G, const RankView& R,
+                                   NbrTable* T2, cudaStream_t s);
 
 // Whether the table kernel serves these arguments (table present, vector-
 // aligned panels) and its widest load mode (as hpsi_fixed_applies).

@@ -19,13 +19,25 @@
 // boundary by a gather when a Krylov space is started and a scatter when the
 // result is combined, so callers only ever see the reference order.
 //
+// The row-level order above scatters the gathers of neighbouring lanes
+// (the rows a warp handles no longer have structured neighbours), and the
+// table kernel is bound by L1/TEX transactions more than by DRAM misses; so
+// the default is the same search one level up: the fermion-mask segments
+// (whose rows keep their reference order inside) are ordered breadth-first
+// over the mask graph, two masks being adjacent when one hop moves a
+// fermion across a bond between them (LRU model: 2.1 misses per row at
+// 100 MB against 4.3).  LGT_TABLE_ORDER=row selects the row-level order,
+// LGT_TABLE_ORDER=0 none.
+//
 // Everything runs on the device, level-synchronous: per level one pass
 // claims the undiscovered neighbours of the level's rows (the smallest
 // (discoverer position, entry slot) key wins), one counts each row's claimed
 // children, a scan turns the counts into offsets and one pass places the
 // children.  The host reads one count per level.
+#include <algorithm>
 #include <climits>
 #include <cstdlib>
+#include <vector>
 
 #include "lgt_hpsi.h"
 
@@ -210,6 +222,11 @@ __global__ void k_place_unplaced(const int* level, int64_t N, const uint32_t* of
   }
 }
 
+__global__ void k_invert(const int* perm, int64_t N, int* iperm) {
+  const int64_t n = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (n < N) iperm[perm[n]] = int(n);
+}
+
 __global__ void k_seed(int* perm, int* iperm, int* level, int64_t at, int row, int L) {
   perm[at] = row;
   iperm[row] = int(at);
@@ -264,6 +281,38 @@ std::string scan_counts(const uint32_t* in, int64_t n, uint32_t* out, uint32_t* 
   OCK(dev_free(sums, s));
   OCK(dev_free(sums_off, s));
   return std::string();
+}
+
+// The renumbered table T2 of T under perm (T2's perm and iperm are set).
+std::string renumber(const NbrTable& T, const int* perm, const int* iperm,
+                     const uint32_t* row_off, NbrTable* T2, cudaStream_t s) {
+  const int64_t N = T.N;
+  const unsigned nblk = unsigned((N + kOT - 1) / kOT);
+  const int64_t tiles = (N + 31) / 32;
+  uint32_t* tile_cnt = nullptr;
+  OCK(cudaMalloc(&T2->meta, sizeof(uint32_t) * N));
+  OCK(cudaMalloc(&T2->tile_off, sizeof(uint32_t) * (tiles + 1)));
+  OCK(cudaMalloc(&T2->nbr, sizeof(uint32_t) * (size_t(T.nnz) + 1)));
+  OCK(dev_alloc_n(&tile_cnt, size_t(tiles) + 1, s));
+  k_perm_meta<<<nblk, kOT, 0, s>>>(T.meta, perm, N, T2->meta, tile_cnt), lgt::note_launch();
+  {
+    std::string e = scan_counts(tile_cnt, tiles, T2->tile_off, T2->tile_off + tiles, s);
+    if (!e.empty()) return e;
+  }
+  k_perm_fill<<<nblk, kOT, 0, s>>>(T2->meta, T2->tile_off, row_off, T.nbr, perm, iperm, N,
+                                   T2->nbr), lgt::note_launch();
+  OCK(cudaGetLastError());
+  OCK(dev_free(tile_cnt, s));
+  return std::string();
+}
+
+void finish(const NbrTable& T, NbrTable* T2) {
+  T2->N = T.N;
+  T2->nnz = T.nnz;
+  T2->model = T.model;
+  T2->mm = T.mm;
+  T2->bytes = T.bytes + sizeof(int) * 2 * size_t(T.N);
+  T2->state = 1;
 }
 
 }  // namespace
@@ -338,22 +387,10 @@ std::string build_table_order(const NbrTable& T, NbrTable* T2, cudaStream_t s) {
     seed = h;
     ++L;
   }
-  // the renumbered table
-  const int64_t tiles = (N + 31) / 32;
-  uint32_t* tile_cnt = nullptr;
-  OCK(cudaMalloc(&T2->meta, sizeof(uint32_t) * N));
-  OCK(cudaMalloc(&T2->tile_off, sizeof(uint32_t) * (tiles + 1)));
-  OCK(cudaMalloc(&T2->nbr, sizeof(uint32_t) * (size_t(T.nnz) + 1)));
-  OCK(dev_alloc_n(&tile_cnt, size_t(tiles) + 1, s));
-  k_perm_meta<<<nblk, kOT, 0, s>>>(T.meta, perm, N, T2->meta, tile_cnt), lgt::note_launch();
   {
-    std::string e = scan_counts(tile_cnt, tiles, T2->tile_off, T2->tile_off + tiles, s);
+    std::string e = renumber(T, perm, iperm, row_off, T2, s);
     if (!e.empty()) return e;
   }
-  k_perm_fill<<<nblk, kOT, 0, s>>>(T2->meta, T2->tile_off, row_off, T.nbr, perm, iperm, N,
-                                   T2->nbr), lgt::note_launch();
-  OCK(cudaGetLastError());
-  OCK(dev_free(tile_cnt, s));
   OCK(dev_free(level, s));
   OCK(dev_free(key, s));
   OCK(dev_free(row_off, s));
@@ -362,12 +399,75 @@ std::string build_table_order(const NbrTable& T, NbrTable* T2, cudaStream_t s) {
   OCK(dev_free(total, s));
   OCK(dev_free(first, s));
   OCK(cudaStreamSynchronize(s));
-  T2->N = N;
-  T2->nnz = T.nnz;
-  T2->model = T.model;
-  T2->mm = T.mm;
-  T2->bytes = T.bytes + sizeof(int) * 2 * size_t(N);
-  T2->state = 1;
+  finish(T, T2);
+  return std::string();
+}
+std::string build_table_mask_order(const NbrTable& T, const Geom& G, const RankView& R,
+                                   NbrTable* T2, cudaStream_t s) {
+  const int64_t N = T.N;
+  if (T.state != 1 || N <= 0) return "no neighbour table to reorder";
+  if (G.ns > 26) return "too many sites for the host mask search";
+  free_nbr_table(T2);
+  // the sector's masks, ascending (the segment order of the basis)
+  std::vector<uint32_t> masks;
+  for (uint32_t m = 0; m < (1u << G.ns); ++m)
+    if (__builtin_popcount(m) == G.nf_target) masks.push_back(m);
+  if (int64_t(masks.size()) != int64_t(R.nmasks)) return "mask count differs from the basis";
+  std::vector<uint32_t> segc(masks.size() + 1);
+  OCK(cudaMemcpyAsync(segc.data(), R.segc, sizeof(uint32_t) * segc.size(),
+                      cudaMemcpyDeviceToHost, s));
+  OCK(cudaStreamSynchronize(s));
+  // bonds (site pairs) of the lattice: a hop across one moves a fermion
+  std::vector<std::pair<int, int>> bonds;
+  for (int iy = 0; iy < G.ny; ++iy)
+    for (int ix = 0; ix + 1 < G.nx; ++ix) bonds.push_back({iy * G.nx + ix, iy * G.nx + ix + 1});
+  for (int iy = 0; iy + 1 < G.ny; ++iy)
+    for (int ix = 0; ix < G.nx; ++ix) bonds.push_back({iy * G.nx + ix, (iy + 1) * G.nx + ix});
+  const size_t M = masks.size();
+  std::vector<int> order;
+  order.reserve(M);
+  std::vector<char> seen(M, 0);
+  for (size_t start = 0; start < M; ++start) {  // every component, first mask first
+    if (seen[start]) continue;
+    seen[start] = 1;
+    size_t head = order.size();
+    order.push_back(int(start));
+    while (head < order.size()) {
+      const uint32_t m = masks[order[head++]];
+      for (const auto& b : bonds) {
+        const uint32_t ba = 1u << b.first, bb = 1u << b.second;
+        if (((m & ba) != 0) == ((m & bb) != 0)) continue;
+        const uint32_t n = m ^ ba ^ bb;
+        const size_t q = size_t(std::lower_bound(masks.begin(), masks.end(), n) - masks.begin());
+        if (q < M && masks[q] == n && !seen[q]) {
+          seen[q] = 1;
+          order.push_back(int(q));
+        }
+      }
+    }
+  }
+  std::vector<int> hperm;
+  hperm.reserve(size_t(N));
+  for (int q : order)
+    for (uint32_t r = segc[q]; r < segc[q + 1]; ++r) hperm.push_back(int(r));
+  if (int64_t(hperm.size()) != N) return "mask segments do not cover the basis";
+  int *perm = nullptr, *iperm = nullptr;
+  uint32_t* row_off = nullptr;
+  OCK(cudaMalloc(&perm, sizeof(int) * N));
+  T2->perm = perm;
+  OCK(cudaMalloc(&iperm, sizeof(int) * N));
+  T2->iperm = iperm;
+  OCK(cudaMemcpyAsync(perm, hperm.data(), sizeof(int) * N, cudaMemcpyHostToDevice, s));
+  const unsigned nblk = unsigned((N + kOT - 1) / kOT);
+  k_invert<<<nblk, kOT, 0, s>>>(perm, N, iperm), lgt::note_launch();
+  OCK(dev_alloc_n(&row_off, size_t(N), s));
+  k_row_offsets<<<nblk, kOT, 0, s>>>(T.meta, T.tile_off, N, row_off), lgt::note_launch();
+  OCK(cudaGetLastError());
+  std::string e = renumber(T, perm, iperm, row_off, T2, s);
+  if (!e.empty()) return e;
+  OCK(dev_free(row_off, s));
+  OCK(cudaStreamSynchronize(s));
+  finish(T, T2);
   return std::string();
 }
 

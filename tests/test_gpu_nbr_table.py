@@ -134,12 +134,14 @@ def test_table_ground_states(oracle, lgt, model, monkeypatch):
 @pytest.mark.parametrize("nx,ny,model", [(4, 3, "ref"), (3, 4, "pjw"), (4, 4, "ref"),
                                           (4, 4, "pjw"), (2, 2, "ref")])
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
-def test_row_order_product_bitwise(lgt, nx, ny, model, prec):
+@pytest.mark.parametrize("order", ["mask", "row"])
+def test_row_order_product_bitwise(lgt, monkeypatch, nx, ny, model, prec, order):
     """The renumbered table (breadth-first row order of the hop graph, used
     by the Krylov drivers): the order is a permutation, and H applied to a
     panel kept in that order equals, bit for bit, the reordered product in
     the reference order (same entries, same summation order per row)."""
     torch = pytest.importorskip("torch")
+    monkeypatch.setenv("LGT_TABLE_ORDER", order)
     st, _ = lgt.build_basis(nx, ny, 1, lgt.staggered_charges(nx, ny))
     N = len(st)
     gs, ts, ms = (np.array(v) for v in zip(*COUPLINGS[:2]))
@@ -163,14 +165,15 @@ def test_row_order_product_bitwise(lgt, nx, ny, model, prec):
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32_mixed"])
 def test_krylov_row_order_matches_reference_order(lgt, monkeypatch, precision):
-    """Krylov drivers with their vectors in the table's row order
-    (default) and in the reference order (LGT_TABLE_ORDER=0), stored-table
-    kernel forced: same ground states and evolved states."""
+    """Krylov drivers with their vectors in the table's mask-segment order
+    (default), its row-level order and the reference order
+    (LGT_TABLE_ORDER=0), stored-table kernel forced: same ground states and
+    evolved states."""
     monkeypatch.setenv("LGT_HPSI_VARIANT", "6")
     st, _ = lgt.build_basis(4, 3, 1, lgt.staggered_charges(4, 3))
     v0 = lgt.staggered_product_state(st)
     res = {}
-    for flag in ("1", "0"):
+    for flag in ("mask", "row", "0"):
         monkeypatch.setenv("LGT_TABLE_ORDER", flag)
         H = lgt.build_hamiltonian(st, g=[0.7, 1.3, 0.9, 1.1], t=1.0, m=0.5, model="pjw")
         E0, psi = lgt.find_ground_state(H, tol=1e-12, solver="panel", precision=precision,
@@ -180,8 +183,10 @@ def test_krylov_row_order_matches_reference_order(lgt, monkeypatch, precision):
         res[flag] = (E0, psi, ps)
         H.close()
     tol = 1e-12 if precision == "fp64" else 1e-10
-    np.testing.assert_allclose(res["1"][0], res["0"][0], rtol=tol)
-    ov = np.abs(np.sum(res["1"][1] * res["0"][1], axis=0))
-    assert np.all(ov > 1 - (1e-12 if precision == "fp64" else 1e-8))
-    assert np.max(np.abs(res["1"][2] - res["0"][2])) <= (1e-10 if precision == "fp64" else 1e-6)
+    for flag in ("mask", "row"):
+        np.testing.assert_allclose(res[flag][0], res["0"][0], rtol=tol)
+        ov = np.abs(np.sum(res[flag][1] * res["0"][1], axis=0))
+        assert np.all(ov > 1 - (1e-12 if precision == "fp64" else 1e-8))
+        assert np.max(np.abs(res[flag][2] - res["0"][2])) <= (1e-10 if precision == "fp64"
+                                                               else 1e-6)
     st.close()
