@@ -152,10 +152,11 @@ def test_row_order_product_bitwise(lgt, monkeypatch, nx, ny, model, prec, order)
     gen = torch.Generator(device="cuda").manual_seed(nx * 10 + ny)
     x = torch.randn((N, 2, 2), dtype=dt, device="cuda", generator=gen)
     y = torch.empty_like(x)
-    H.matvec_device(x.data_ptr(), y.data_ptr(), 2, prec)
     p = torch.from_numpy(perm.astype(np.int64)).cuda()
     xo = x[p].contiguous()
     yo = torch.empty_like(xo)
+    torch.cuda.synchronize()  # the library works on the basis' own stream
+    H.matvec_device(x.data_ptr(), y.data_ptr(), 2, prec)
     H.matvec_device(xo.data_ptr(), yo.data_ptr(), 2, prec, row_order=True)
     torch.cuda.synchronize()
     assert torch.equal(yo, y[p])

@@ -56,6 +56,7 @@ def test_noalloc_matches_observe_twice(nx, ny, K, ncomp, dtype):
         psi = torch.randn((N, K, ncomp), dtype=tdt, device="cuda", generator=gen)
         psi /= torch.linalg.vector_norm(psi.double(), dim=(0, 2), keepdim=True).to(tdt)
         psis.append(psi)
+    torch.cuda.synchronize()  # the library works on the basis' own stream
     g = np.linspace(0.5, 2.0, K)
     # warm-up on a throw-away Hamiltonian: loads the module and looks up the
     # scratch address (the one-time set-up of the first call on a device)
