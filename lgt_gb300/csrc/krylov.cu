@@ -389,10 +389,9 @@ __global__ void __launch_bounds__(kT) k_update(const S* __restrict__ V, size_t v
 // h_i V_i and the new |W|^2 partials, FP64-class (lgt_dfloat.cuh) with the
 // FP64 pipe used only to split the coefficients.  The block first splits
 // its columns' coefficients h into FP32 pairs hh + hl in shared memory
-// (sh: [J][C] pairs); each thread then runs two rows at a time with two
-// coefficient chains per row (even and odd i), four basis vectors per trip
-// with their loads issued first.  Same partition, skipping rules and
-// outputs as k_update.
+// (sh: [J][C] pairs); each thread then runs four rows at a time, four basis
+// vectors per trip with their loads issued first.  Same partition,
+// skipping rules and outputs as k_update.
 __global__ void __launch_bounds__(kT) k_update_df(const float* __restrict__ V, size_t vstride,
                                                   const int* jstate, float* __restrict__ W,
                                                   int64_t N, int C, const double* __restrict__ h,
@@ -419,54 +418,75 @@ __global__ void __launch_bounds__(kT) k_update_df(const float* __restrict__ V, s
   const int64_t r1 = (r0 + rpb < N) ? r0 + rpb : N;
   df nrm{0.f, 0.f};
   if (act) {
+    // four rows at a time, four basis vectors per trip: sixteen loads in
+    // flight before the arithmetic.  Each row's sum is Dot2-style (Ogita,
+    // Rump, Oishi): the leading parts by TwoSum, the trailing parts added in
+    // FP32 -- at most J + 1 terms per entry, so its error stays at the
+    // FP32 rounding of the result plus J^2 2^-48 of the terms' sizes.
+    constexpr int kRows = 4;
     int64_t row = r0 + rg;
-    for (; row + RG < r1; row += 2 * int64_t(RG)) {
-      const size_t oa = size_t(row) * C + c, ob = oa + size_t(RG) * C;
-      df a0{W[oa], 0.f}, b0{W[ob], 0.f}, a1{0.f, 0.f}, b1{0.f, 0.f};
-      const float* va = V + oa;
-      const float* vb = V + ob;
-      int i = 0;
-      for (; i + 3 < J; i += 4) {
-        float x[4], y[4];
+    for (; row + (kRows - 1) * int64_t(RG) < r1; row += kRows * int64_t(RG)) {
+      size_t o[kRows];
+      float hi[kRows], lo[kRows];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          x[u] = __ldg(va + size_t(i + u) * vstride);
-          y[u] = __ldg(vb + size_t(i + u) * vstride);
-        }
+      for (int q = 0; q < kRows; ++q) {
+        o[q] = size_t(row + q * int64_t(RG)) * C + c;
+        hi[q] = W[o[q]];
+        lo[q] = 0.f;
+      }
+      const float* vi = V;
+      int i = 0;
+      for (; i + 3 < J; i += 4, vi += 4 * vstride) {
+        float x[4][kRows];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int q = 0; q < kRows; ++q) x[u][q] = __ldg(vi + u * vstride + o[q]);
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           const float hh = s_hh[(i + u) * C + c], hl = s_hl[(i + u) * C + c];
-          df_sub_prod((u & 1) ? a1 : a0, hh, hl, x[u]);
-          df_sub_prod((u & 1) ? b1 : b0, hh, hl, y[u]);
+#pragma unroll
+          for (int q = 0; q < kRows; ++q) {
+            float p, e, t;
+            two_prod(hh, x[u][q], p, e);
+            e = df_fma_rn(hl, x[u][q], e);
+            two_sum(hi[q], -p, hi[q], t);
+            lo[q] = df_add_rn(lo[q], df_sub_rn(t, e));
+          }
         }
       }
-      for (; i < J; ++i) {
+      for (; i < J; ++i, vi += vstride) {
         const float hh = s_hh[i * C + c], hl = s_hl[i * C + c];
-        df_sub_prod(a0, hh, hl, __ldg(va + size_t(i) * vstride));
-        df_sub_prod(b0, hh, hl, __ldg(vb + size_t(i) * vstride));
+#pragma unroll
+        for (int q = 0; q < kRows; ++q) {
+          const float xv = __ldg(vi + o[q]);
+          float p, e, t;
+          two_prod(hh, xv, p, e);
+          e = df_fma_rn(hl, xv, e);
+          two_sum(hi[q], -p, hi[q], t);
+          lo[q] = df_add_rn(lo[q], df_sub_rn(t, e));
+        }
       }
-      const float sa = df_round(df_add(a0, a1)), sb = df_round(df_add(b0, b1));
-      W[oa] = sa;
-      W[ob] = sb;
-      df_fma(nrm, sa, sa);
-      df_fma(nrm, sb, sb);
+#pragma unroll
+      for (int q = 0; q < kRows; ++q) {
+        const float sa = df_add_rn(hi[q], lo[q]);
+        W[o[q]] = sa;
+        df_fma(nrm, sa, sa);
+      }
     }
     for (; row < r1; row += RG) {
       const size_t oa = size_t(row) * C + c;
-      df a0{W[oa], 0.f}, a1{0.f, 0.f};
-      const float* va = V + oa;
-      int i = 0;
-      for (; i + 3 < J; i += 4) {
-        float x[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) x[u] = __ldg(va + size_t(i + u) * vstride);
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-          df_sub_prod((u & 1) ? a1 : a0, s_hh[(i + u) * C + c], s_hl[(i + u) * C + c], x[u]);
+      float hi = W[oa], lo = 0.f;
+      const float* vi = V;
+      for (int i = 0; i < J; ++i, vi += vstride) {
+        const float xv = __ldg(vi + oa);
+        float p, e, t;
+        two_prod(s_hh[i * C + c], xv, p, e);
+        e = df_fma_rn(s_hl[i * C + c], xv, e);
+        two_sum(hi, -p, hi, t);
+        lo = df_add_rn(lo, df_sub_rn(t, e));
       }
-      for (; i < J; ++i)
-        df_sub_prod(a0, s_hh[i * C + c], s_hl[i * C + c], __ldg(va + size_t(i) * vstride));
-      const float sa = df_round(df_add(a0, a1));
+      const float sa = df_add_rn(hi, lo);
       W[oa] = sa;
       df_fma(nrm, sa, sa);
     }

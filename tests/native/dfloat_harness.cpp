@@ -17,21 +17,20 @@ double dfh_dot(const float* a, const float* b, int64_t n) {
 }
 
 // The Gram-Schmidt update of one entry, as k_update_df does it: w minus
-// sum_i h_i v_i with each h_i split into an FP32 pair, two coefficient
-// chains (even and odd i), rounded to FP32 at the end.
+// sum_i h_i v_i with each h_i split into an FP32 pair hh + hl, the leading
+// parts summed by TwoSum and the trailing parts in FP32 (Dot2 form),
+// rounded to FP32 at the end.
 float dfh_update(float w, const double* h, const float* v, int64_t J) {
-  df a0{w, 0.f}, a1{0.f, 0.f};
-  int64_t i = 0;
-  for (; i + 1 < J; i += 2) {
-    const float h0 = float(h[i]), h1 = float(h[i + 1]);
-    lgt::df_sub_prod(a0, h0, float(h[i] - double(h0)), v[i]);
-    lgt::df_sub_prod(a1, h1, float(h[i + 1] - double(h1)), v[i + 1]);
+  float hi = w, lo = 0.f;
+  for (int64_t i = 0; i < J; ++i) {
+    const float hh = float(h[i]), hl = float(h[i] - double(hh));
+    float p, e, t;
+    lgt::two_prod(hh, v[i], p, e);
+    e = lgt::df_fma_rn(hl, v[i], e);
+    lgt::two_sum(hi, -p, hi, t);
+    lo = lgt::df_add_rn(lo, lgt::df_sub_rn(t, e));
   }
-  if (i < J) {
-    const float h0 = float(h[i]);
-    lgt::df_sub_prod(a0, h0, float(h[i] - double(h0)), v[i]);
-  }
-  return lgt::df_round(lgt::df_add(a0, a1));
+  return lgt::df_add_rn(hi, lo);
 }
 
 // sum_i a_i (bh_i + bl_i), the per-CTA dot against a double-float residual.

@@ -5,13 +5,13 @@ results (math.fsum of exactly represented products, Fractions).
 
 Bars.  A dot of n terms: |error| <= 4 n 2^-48 sum |a_i b_i| (the bound of
 renormalised double-word sums), and on random data within sqrt(n) 2^-46
-sum |a_i b_i|.  A Gram-Schmidt update w - V h of FP32 data, rounded to
-FP32 as the mixed path stores it: its error is dominated by that final
-rounding, so it is within 1.5 times the error of the same update
-accumulated in FP64 (and within 0.51 FP32 ulp per entry plus 2^-46 of the
-terms' sizes), for well-conditioned passes and for passes that cancel
-three digits (the largest cancellation a pass is kept for; more triggers a
-second pass).
+sum |a_i b_i|.  A Gram-Schmidt update w - V h of FP32 data (J vectors),
+rounded to FP32 as the mixed path stores it: its error is dominated by
+that final rounding, so it is within 1.5 times the error of the same
+update accumulated in FP64 (and within 0.51 FP32 ulp per entry plus
+(J + 1)^2 2^-48 of the terms' sizes, the Dot2 bound), for well-conditioned
+passes and for passes that cancel three digits (the largest cancellation a
+pass is kept for; more triggers a second pass).
 """
 import ctypes
 import math
@@ -124,6 +124,7 @@ def test_update_rounds_like_fp64(dfh, J, cancel):
     terms = np.abs(w.astype(np.float64)) + np.abs(V.astype(np.float64)) @ np.abs(h)
     err = np.abs(got.astype(np.float64) - exact)
     ulp = np.spacing(np.abs(exact.astype(np.float32))).astype(np.float64)
-    assert np.all(err <= 0.51 * ulp + 2.0**-46 * terms)
+    bound = (J + 1) ** 2 * 2.0**-48  # Dot2: FP32 rounding of the result + (J u)^2 of the terms
+    assert np.all(err <= 0.51 * ulp + bound * terms)
     err64 = np.abs(ref64.astype(np.float64) - exact)
-    assert np.linalg.norm(err) <= 1.5 * np.linalg.norm(err64) + 2.0**-46 * np.linalg.norm(terms)
+    assert np.linalg.norm(err) <= 1.5 * np.linalg.norm(err64) + bound * np.linalg.norm(terms)
