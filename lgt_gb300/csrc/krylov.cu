@@ -97,7 +97,7 @@ __global__ void k_randn(S* out, int64_t N, int C, int ncomp, uint64_t seed) {
 #define LGT_MD_MINB 4  // resident blocks per SM the dot kernel's registers must allow (FP64)
 #endif
 #ifndef LGT_MD_MINB_F32
-#define LGT_MD_MINB_F32 4  // the same for FP32 panels (measured with chunks sized to the
+#define LGT_MD_MINB_F32 3  // the same for FP32 panels (measured with chunks sized to the
                            // vectors left: 4 without spills beats 5 with them)
 #endif
 // One chunk of a dot pass: the NQ basis vectors i0 .. i0 + NQ - 1 (those
@@ -120,18 +120,35 @@ __device__ __forceinline__ void dots_chunk(const S* __restrict__ V, size_t vstri
     for (int q = 0; q < NQ; ++q) a[q] = df{0.f, 0.f};
     if (act) {
       const int ilast = (Jv > 0) ? Jv - 1 : 0;
-      for (int64_t row = r0 + rg; row < r1; row += RG) {
-        const size_t off = size_t(row) * C;
-        const float w = float(W[off + c]);
-        float v[NQ];
+      const float* vq[NQ];
+#pragma unroll
+      for (int q = 0; q < NQ; ++q)
+        vq[q] = reinterpret_cast<const float*>(V) + size_t((i0 + q < Jv) ? i0 + q : ilast) * vstride + c;
+      const float* wp = reinterpret_cast<const float*>(W) + c;
+      // two rows per trip: 2 (NQ + 1) loads in flight before the arithmetic
+      int64_t row = r0 + rg;
+      for (; row + RG < r1; row += 2 * int64_t(RG)) {
+        const size_t oa = size_t(row) * C, ob = oa + size_t(RG) * C;
+        const float wa = __ldg(wp + oa), wb = __ldg(wp + ob);
+        float va[NQ], vb[NQ];
 #pragma unroll
         for (int q = 0; q < NQ; ++q) {
-          const int i = (i0 + q < Jv) ? i0 + q : ilast;
-          v[q] = float(V[size_t(i) * vstride + off + c]);
+          va[q] = __ldg(vq[q] + oa);
+          vb[q] = __ldg(vq[q] + ob);
         }
 #pragma unroll
         for (int q = 0; q < NQ; ++q)
-          if (i0 + q < J) df_fma(a[q], (i0 + q < Jv) ? v[q] : w, w);
+          if (i0 + q < J) {
+            df_fma(a[q], (i0 + q < Jv) ? va[q] : wa, wa);
+            df_fma(a[q], (i0 + q < Jv) ? vb[q] : wb, wb);
+          }
+      }
+      for (; row < r1; row += RG) {
+        const size_t off = size_t(row) * C;
+        const float w = __ldg(wp + off);
+#pragma unroll
+        for (int q = 0; q < NQ; ++q)
+          if (i0 + q < J) df_fma(a[q], (i0 + q < Jv) ? __ldg(vq[q] + off) : w, w);
       }
     }
     if (rg < RG) {
