@@ -39,9 +39,8 @@ namespace lgt {
 
 namespace {
 
-constexpr int kCta = 512;               // most threads per CTA with R >= 2 rows each
-constexpr int kCta1 = 1024;             // most threads per CTA with one row each
-constexpr int kWarpsCta = kCta1 / 32;
+constexpr int kCta = 512;               // most threads per CTA
+constexpr int kWarpsCta = kCta / 32;
 constexpr int kMaxM = 64;
 
 #define SCK(call)                                                                  \
@@ -207,12 +206,12 @@ __device__ __forceinline__ double warp_scatter4_df(const df* p, int lane) {
 // Krylov basis (double, or float for the FP32-mixed path); R: rows per
 // thread held in registers (N <= R * 512).
 template <typename S, int R>
-__global__ void __launch_bounds__(R == 1 ? kCta1 : kCta, 1) k_lanczos_cta(const SmallProblem* probs,
+__global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* probs,
                                                       const SmallUnit* units, SmallParams prm) {
   extern __shared__ __align__(16) unsigned char s_basis[];  // (m + 1) x N when prm.v_smem
   __shared__ double s_alpha[kMaxM + 1], s_beta[kMaxM + 1], s_h[kMaxM + 1], s_z[kMaxM + 1];
   __shared__ double s_part[kMaxM + 1][kWarpsCta];
-  __shared__ double s_red[kCta1];
+  __shared__ double s_red[kCta];
   __shared__ double s_sum[3];  // block_sum results: sum, sqrt, 1 / sqrt
   __shared__ int s_exh;        // the step's Krylov space is exhausted
   __shared__ double s_work[3 * kMaxM];
@@ -600,16 +599,13 @@ bool getenv_flag(const char* name, int def) {
   return e[0] != '0';
 }
 
-// Dynamic shared memory a CTA may take beside the kernel's static arrays
-// (about 30 KB; 227 KB in all per CTA).
-constexpr int kCtaSmemMax = 192 * 1024;
+// Dynamic shared memory a CTA may take beside the kernel's static arrays.
+constexpr int kCtaSmemMax = 200 * 1024;
 
 template <typename S>
 cudaError_t launch_cta(const SmallProblem* probs, const SmallUnit* units, int nunits, int maxN,
                        const SmallParams& prm_in, cudaStream_t s, int rows_per_thread) {
-  // one row per thread (up to 1024 threads) only when asked for
-  int R = (rows_per_thread == 1 && maxN <= kCta1) ? 1 : (maxN + kCta - 1) / kCta;
-  if (R < 1) R = 1;
+  int R = (maxN + kCta - 1) / kCta;
   if (rows_per_thread > R) R = rows_per_thread;
   auto threads_for = [&](int rr) {
     int t = ((maxN + rr - 1) / rr + 31) / 32 * 32;
@@ -797,7 +793,6 @@ std::string small_ground_states(const std::vector<SmallJob>& jobs, const SmallPa
       // to an instantiated case), each with at least 64 threads
       auto round_case = [](int r) { return r <= 3 ? r : (r <= 4 ? 4 : (r <= 8 ? 8 : 16)); };
       std::vector<int> cand;
-      if (r0 == 2 && maxN <= kCta1) cand.push_back(1);  // one row per thread, up to 1024 threads
       for (int r : {r0, r0 + 1, 2 * r0}) {
         const int rc = round_case(r);
         if (rc <= 16 && (maxN + rc - 1) / rc >= 64 &&
