@@ -41,10 +41,11 @@ NX, NY, DG, KPTS = 4, 2, 1, 64
 G_LO, G_HI, T_HOP, MASS = 0.5, 2.0, 1.0, 0.5
 RF_NX, RF_NY, RF_K = 4, 4, 8          # roofline panel (4x4 quench, K = 8 complex)
 # DRAM bytes of one such launch (FP32, reference model) per kernel family,
-# measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum, --set full,
-# one launch of each kernel on this panel)
+# measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum, one launch
+# of each kernel on this panel; the ordered table in the mask-BFS row order)
 RF_TRAFFIC_BYTES = {"fixed": int((2.903165 + 0.533069) * 1e9),
-                    "table": int((3.236144 + 0.532940) * 1e9)}
+                    "table": int((3.236144 + 0.532940) * 1e9),
+                    "table_ordered": int((2.525915 + 0.527390) * 1e9)}
 L2_FLUSH_BYTES = 512 << 20            # > 129 MB L2
 METRIC = "ground states/s, batched FP32-mixed Lanczos at |dE|/|E|<=1e-10"
 
@@ -348,10 +349,10 @@ def gs_only(args):
     return {"gs_per_s": KPTS / statistics.mean(ts), "ms_per_step": 1e3 * statistics.mean(ts)}
 
 
-def quench(L, C, lib, torch, stream, dev, n_steps=100):
-    """4x4 real-time quench panel: K = 8 points g ~ U[0.5, 1.5] (seed 0), m = 0.5,
-    t = 1, from the staggered product state, dt = 0.05; n_steps Krylov
-    exp(-iH dt) steps (100: t = 5) with observables every step, FP64 and
+def quench(L, C, lib, torch, stream, dev, n_steps=100, K=None):
+    """4x4 real-time quench panel: K points (8 unless given) g ~ U[0.5, 1.5]
+    (seed 0), m = 0.5, t = 1, from the staggered product state, dt = 0.05;
+    n_steps Krylov exp(-iH dt) steps (100: t = 5) with observables every step, FP64 and
     FP32-mixed.  Reports steps/s, the norm drift (max |1 - ||psi||| before
     each renormalisation), the energy drift at the end, and the largest
     difference between the FP32-mixed and FP64 trajectories of <E^2>,
@@ -360,26 +361,27 @@ def quench(L, C, lib, torch, stream, dev, n_steps=100):
     C.check(lib.lgt_basis_set_stream(b.handle, ctypes_ptr(stream.cuda_stream)))
     N = len(b)
     ns = RF_NX * RF_NY
-    gs = np.random.default_rng(0).uniform(0.5, 1.5, RF_K)
+    K = RF_K if K is None else K
+    gs = np.random.default_rng(0).uniform(0.5, 1.5, K)
     H = L.build_hamiltonian(b, g=gs, t=1.0, m=0.5, model="ref")
     v0 = L.staggered_product_state(b)
     i0 = int(np.argmax(np.abs(v0)))
-    out = {"N": N, "K": RF_K, "dt": 0.05, "steps_timed": n_steps, "t_end": 0.05 * n_steps}
+    out = {"N": N, "K": K, "dt": 0.05, "steps_timed": n_steps, "t_end": 0.05 * n_steps}
     traj = {}
     for prec, code in (("fp64", C.LGT_FP64), ("fp32_mixed", C.LGT_FP32_MIXED)):
-        psi = torch.zeros((N, RF_K, 2), dtype=torch.float64, device="cuda")
+        psi = torch.zeros((N, K, 2), dtype=torch.float64, device="cuda")
         psi[i0, :, 0] = 1.0
         torch.cuda.synchronize()  # the library runs on `stream`
-        e_before = np.zeros(RF_K)
+        e_before = np.zeros(K)
         C.check(lib.lgt_energy(H.handle, psi.data_ptr(), 2, C.LGT_DEVICE_PTRS, e_before.ctypes.data))
         tune = C.Tuning()  # the autotuner's one-time timing runs here, not in the timed step
         C.check(lib.lgt_autotune(H.handle, 2, code, ctypes_byref(tune)))
         o = C.defaults(True)
         o.precision = code
-        R = (n_steps + 1) * RF_K
+        R = (n_steps + 1) * K
         obs = (C.Obs * R)()
         nfg = np.zeros(R * ns)
-        drift = np.zeros(RF_K)
+        drift = np.zeros(K)
         info = C.Info()
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -392,10 +394,10 @@ def quench(L, C, lib, torch, stream, dev, n_steps=100):
             e1.record(stream)
         e1.synchronize()
         t = e0.elapsed_time(e1) * 1e-3
-        e_after = np.zeros(RF_K)
+        e_after = np.zeros(K)
         C.check(lib.lgt_energy(H.handle, psi.data_ptr(), 2, C.LGT_DEVICE_PTRS, e_after.ctypes.data))
-        sm = np.frombuffer(obs, dtype=np.float64).reshape(n_steps + 1, RF_K, 8)
-        traj[prec] = (sm, nfg.reshape(n_steps + 1, RF_K, ns))
+        sm = np.frombuffer(obs, dtype=np.float64).reshape(n_steps + 1, K, 8)
+        traj[prec] = (sm, nfg.reshape(n_steps + 1, K, ns))
         out[prec] = {"quench_steps_per_s": n_steps / t, "s_per_step": t / n_steps,
                      "matvecs_per_step": info.matvecs / n_steps,
                      "max_norm_drift": float(drift.max()),
@@ -659,6 +661,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quench-steps", type=int, default=100,
                     help="timed 4x4 quench steps (dt = 0.05; 100 reach t = 5)")
+    ap.add_argument("--quench-points", type=int, default=None,
+                    help="--part quench: coupling points in the panel (8 unless given)")
     ap.add_argument("--detail", default=None,
                     help="also write every measured figure (roofline variants, per-config "
                          "detail, quench trajectories' summaries) to this JSON file")
@@ -713,7 +717,8 @@ def main():
         import lgt_gb300 as L
         from lgt_gb300 import _capi as C
         torch.cuda.set_device(0)
-        q = quench(L, C, C.load(), torch, torch.cuda.Stream(), 0, n_steps=args.quench_steps)
+        q = quench(L, C, C.load(), torch, torch.cuda.Stream(), 0, n_steps=args.quench_steps,
+                   K=args.quench_points)
         print(json.dumps({"part": "quench", "quench": q}))
         return
 
