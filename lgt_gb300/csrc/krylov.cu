@@ -29,6 +29,7 @@
 #include <tuple>
 #include <vector>
 
+#include "lgt_bulk.cuh"
 #include "lgt_dfloat.cuh"
 #include "lgt_krylov.h"
 #include "lgt_tridiag.cuh"
@@ -233,6 +234,172 @@ __global__ void __launch_bounds__(kT, sizeof(S) == 4 ? LGT_MD_MINB_F32 : LGT_MD_
       for (int g = 0; g < RG; ++g) s += red[g * kIC * 2 * C + q];
       const int ii = q / (2 * C);
       if (i0 + ii < J) part[(size_t(blockIdx.x) * Jmax + i0) * 2 * C + q] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// Bulk-copy streaming of a block's panel rows (k_multidot_bulk,
+// k_update_bulk): tiles of kBulkTile values (kBulkTile / C rows, contiguous
+// in every panel) pass through a ring of kBulkStages shared-memory stages,
+// each refilled by one bulk copy once the block has consumed it.
+constexpr int kBulkStages = 4;
+constexpr int kBulkElems = 8;                  // values per thread and tile
+constexpr int kBulkTile = kT * kBulkElems;     // values per chunk (8 KB)
+
+// Basis vectors of dot group g (slots g kIC .. g kIC + kIC - 1 below Jv).
+__device__ __forceinline__ int bulk_group_vectors(int g, int Jv) {
+  const int i0 = g * kIC, i1 = (i0 + kIC < Jv) ? i0 + kIC : Jv;
+  return i1 > i0 ? i1 - i0 : 0;
+}
+
+// The next chunk a multidot block issues: group g, tile t, slot s (0: W,
+// s > 0: basis vector g kIC + s - 1), and the chunks issued so far.
+struct BulkCursor {
+  int g, t, s;
+  int64_t issued;
+  __device__ __forceinline__ void advance(int nt, int Jv) {
+    ++issued;
+    if (++s > bulk_group_vectors(g, Jv)) {
+      s = 0;
+      if (++t == nt) {
+        t = 0;
+        ++g;
+      }
+    }
+  }
+};
+
+// k_multidot's double-float FP32 pass with the rows streamed in bulk
+// copies.  Per group of up to kIC dot slots (basis vectors i0 .. i0 + nq - 1;
+// a slot at Jv is W against itself), every tile of the block's range sends
+// W_t, then V_{i0},t, ... through the stage ring; thread (c, g) keeps its
+// kBulkElems values of W_t (column c, rows g + RG e) in registers and adds
+// their products into one double-float per slot.  Rows and operations are
+// those of dots_chunk in the same order, so the partials are bitwise
+// k_multidot's.  Needs kT % C == 0 and 16-byte aligned chunks; a copy that
+// does not arrive within the bounded wait raises kDevErrSpin in `err`.
+__global__ void __launch_bounds__(kT, 3) k_multidot_bulk(const float* __restrict__ V, size_t vstride,
+                                                      const int* jstate, const float* W,
+                                                      int64_t N, int C, int64_t rpb,
+                                                      double* part, int Jmax, int self,
+                                                      const int* need, int* err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  float* s_buf = reinterpret_cast<float*>(smem_raw);  // [kBulkStages][kBulkTile]
+  uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_buf + kBulkStages * kBulkTile);
+  double* red = reinterpret_cast<double*>(s_bar + kBulkStages);  // [RG][kIC][2][C]
+  const int Jv = *jstate + 1;
+  const int J = Jv + self;
+  const int tid = threadIdx.x;
+  const int RG = kT / C;
+  const int c = tid % C, rg = tid / C;
+  const bool act = !need || need[c] != 0;
+  const int64_t r0 = int64_t(blockIdx.x) * rpb;
+  const int64_t r1 = (r0 + rpb < N) ? r0 + rpb : N;
+  const int TR = kBulkTile / C;
+  const int nt = (r1 > r0) ? int((r1 - r0 + TR - 1) / TR) : 0;
+  if (tid == 0) {
+    for (int st = 0; st < kBulkStages; ++st) mbar_init(s_bar + st, 1);
+    mbar_init_fence();
+  }
+  const int any = __syncthreads_or(act ? 1 : 0);
+  const int ngroups = (J + kIC - 1) / kIC;
+  int64_t total = 0;
+  if (any)
+    for (int g = 0; g < ngroups; ++g) total += int64_t(nt) * (1 + bulk_group_vectors(g, Jv));
+  // producer cursor (thread 0): next chunk to issue as (group, tile, slot)
+  BulkCursor cur{0, 0, 0, 0};
+  auto issue_next = [&]() {
+    const int64_t rs = r0 + int64_t(cur.t) * TR;
+    const int rows = int((r1 - rs < TR) ? (r1 - rs) : TR);
+    const float* src =
+        (cur.s == 0 ? W : V + size_t(cur.g * kIC + cur.s - 1) * vstride) + size_t(rs) * C;
+    const int st = int(cur.issued % kBulkStages);
+    const uint32_t bytes = uint32_t(rows) * uint32_t(C) * 4u;
+    mbar_arrive_expect_tx(s_bar + st, bytes);
+    bulk_g2s(s_buf + size_t(st) * kBulkTile, src, bytes, s_bar + st);
+    cur.advance(nt, Jv);
+  };
+  if (tid == 0)
+    while (cur.issued < total && cur.issued < kBulkStages) issue_next();
+  int64_t n = 0;  // chunks consumed
+  bool bad = false;
+  for (int g = 0; g < ngroups && !bad; ++g) {
+    const int i0 = g * kIC;
+    const int nq = (J - i0 < kIC) ? J - i0 : kIC;
+    const int nv = bulk_group_vectors(g, Jv);
+    df a[kIC];
+#pragma unroll
+    for (int q = 0; q < kIC; ++q) a[q] = df{0.f, 0.f};
+    float w[kBulkElems];
+    for (int t = 0; any && t < nt && !bad; ++t) {
+      const int64_t rs = r0 + int64_t(t) * TR;
+      const int vals = int((r1 - rs < TR) ? (r1 - rs) : TR) * C;
+      for (int sl = 0; sl <= nv; ++sl, ++n) {
+        const int st = int(n % kBulkStages);
+        if (!mbar_wait_bounded(s_bar + st, uint32_t(n / kBulkStages) & 1u)) bad = true;
+        const float* buf = s_buf + size_t(st) * kBulkTile;
+        if (!bad && act) {
+          if (sl == 0) {
+#pragma unroll
+            for (int e = 0; e < kBulkElems; ++e) {
+              const int idx = tid + kT * e;
+              w[e] = idx < vals ? buf[idx] : 0.f;
+            }
+          } else {
+            const int q = sl - 1;
+#pragma unroll
+            for (int qq = 0; qq < kIC; ++qq)
+              if (qq == q) {
+#pragma unroll
+                for (int e = 0; e < kBulkElems; ++e)
+                  if (tid + kT * e < vals) df_fma(a[qq], buf[tid + kT * e], w[e]);
+              }
+          }
+          // self slots of this group (W against itself) after its last vector
+          if (sl == nv) {
+#pragma unroll
+            for (int qq = 0; qq < kIC; ++qq)
+              if (qq >= nv && qq < nq) {
+#pragma unroll
+                for (int e = 0; e < kBulkElems; ++e)
+                  if (tid + kT * e < vals) df_fma(a[qq], w[e], w[e]);
+              }
+          }
+        }
+        if (__syncthreads_or(bad ? 1 : 0)) {
+          bad = true;
+          break;
+        }
+        if (tid == 0 && cur.issued < total) issue_next();
+      }
+    }
+    if (bad) break;
+    // red[rg][q][comp][c] as dots_chunk writes it, then the block's partials
+#pragma unroll
+    for (int q = 0; q < kIC; ++q) {
+      if (q < nq) {
+        red[((rg * kIC + q) * 2 + 0) * C + c] =
+            (act && any) ? widen(a[q].hi) + widen(a[q].lo) : 0.0;
+        red[((rg * kIC + q) * 2 + 1) * C + c] = 0.0;
+      }
+    }
+    __syncthreads();
+    const int nq2 = nq <= 1 ? 1 : nq <= 2 ? 2 : nq <= 4 ? 4 : kIC;
+    for (int q = tid; q < nq2 * 2 * C; q += kT) {
+      double s = 0.0;
+      for (int gg = 0; gg < RG; ++gg) s += red[gg * kIC * 2 * C + q];
+      const int ii = q / (2 * C);
+      if (i0 + ii < J) part[(size_t(blockIdx.x) * Jmax + i0) * 2 * C + q] = s;
+    }
+    __syncthreads();
+  }
+  if (bad) {
+    // copies issued and not consumed: chunks n .. issued - 1 (thread 0's count)
+    if (tid == 0) {
+      for (int64_t m = n; m < cur.issued; ++m)
+        mbar_wait_bounded(s_bar + (m % kBulkStages), uint32_t(m / kBulkStages) & 1u);
+      if (err) atomicOr(err, kDevErrSpin);
     }
     __syncthreads();
   }
@@ -514,6 +681,141 @@ __global__ void __launch_bounds__(kT) k_update_df(const float* __restrict__ V, s
     double s = 0.0;
     for (int g = 0; g < RG; ++g) s += red[g * C + threadIdx.x];
     npart[size_t(blockIdx.x) * C + threadIdx.x] = s;
+  }
+}
+
+// k_update_df with the panel rows streamed through shared memory by the
+// copy engine.  A block's row range is cut into tiles of kBulkTile values
+// (kBulkTile / C rows, contiguous in every panel); the chunks W_t, V_0,t,
+// ..., V_{J-1},t of tile t follow one another through a ring of
+// kBulkStages shared-memory stages, each refilled by one bulk copy as soon
+// as the block has consumed it, so kBulkStages - 1 chunks are in flight
+// while the block computes.  Thread (c, g) owns the values tid + kT e of a
+// tile (column c, rows g + RG e): the same rows in the same order as
+// k_update_df, with the same arithmetic, so W and the norm partials are
+// bitwise those of k_update_df.  Needs kT % C == 0 and 16-byte aligned
+// chunks (launch_update checks).  A copy that does not arrive within the
+// bounded wait raises kDevErrSpin in `err`; the block then waits (bounded)
+// for the copies it issued and leaves.
+
+__global__ void __launch_bounds__(kT) k_update_bulk(const float* __restrict__ V, size_t vstride,
+                                                    const int* jstate, float* W, int64_t N,
+                                                    int C, const double* __restrict__ h, int K,
+                                                    const int* status, int64_t rpb,
+                                                    double* npart, const int* need, int* err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  float* s_buf = reinterpret_cast<float*>(smem_raw);  // [kBulkStages][kBulkTile]
+  uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_buf + kBulkStages * kBulkTile);
+  __shared__ double red[kT];
+  const int J = *jstate + 1;
+  float* s_hh = reinterpret_cast<float*>(s_bar + kBulkStages);  // [J][C]
+  float* s_hl = s_hh + size_t(J) * C;
+  const int tid = threadIdx.x;
+  for (int idx = tid; idx < J * C; idx += kT) {
+    const int i = idx / C, cc = idx - i * C;
+    const double hv = h[(size_t(i) * K + cc) * 2];
+    const float hh = narrow(hv);
+    s_hh[idx] = hh;
+    s_hl[idx] = narrow(hv - widen(hh));
+  }
+  if (tid == 0) {
+    for (int st = 0; st < kBulkStages; ++st) mbar_init(s_bar + st, 1);
+    mbar_init_fence();
+  }
+  const int RG = kT / C;
+  const int c = tid % C;
+  const bool act = (!status || status[c] == kActive) && !(need && need[c] == 0);
+  const int64_t r0 = int64_t(blockIdx.x) * rpb;
+  const int64_t r1 = (r0 + rpb < N) ? r0 + rpb : N;
+  const int TR = kBulkTile / C;
+  const int nt = (r1 > r0) ? int((r1 - r0 + TR - 1) / TR) : 0;
+  // no active column in this pass: nothing to read (the partials of
+  // columns that need no pass keep their values)
+  const int any = __syncthreads_or(act ? 1 : 0);
+  const int nchunks = any ? nt * (J + 1) : 0;
+  auto issue = [&](int n) {  // thread 0: chunk n into its stage
+    const int t = n / (J + 1), i = n - t * (J + 1) - 1;
+    const int64_t rs = r0 + int64_t(t) * TR;
+    const int rows = int((r1 - rs < TR) ? (r1 - rs) : TR);
+    const float* src = (i < 0 ? W : V + size_t(i) * vstride) + size_t(rs) * C;
+    const int st = n % kBulkStages;
+    const uint32_t bytes = uint32_t(rows) * uint32_t(C) * 4u;
+    mbar_arrive_expect_tx(s_bar + st, bytes);
+    bulk_g2s(s_buf + size_t(st) * kBulkTile, src, bytes, s_bar + st);
+  };
+  const int pre = nchunks < kBulkStages ? nchunks : kBulkStages;
+  if (tid == 0)
+    for (int n = 0; n < pre; ++n) issue(n);
+  float hi[kBulkElems], lo[kBulkElems];
+  df nrm{0.f, 0.f};
+  int n = 0;
+  bool bad = false;
+  for (; n < nchunks; ++n) {
+    const int st = n % kBulkStages;
+    if (!mbar_wait_bounded(s_bar + st, uint32_t(n / kBulkStages) & 1u)) bad = true;
+    const int t = n / (J + 1), i = n - t * (J + 1) - 1;
+    const int64_t rs = r0 + int64_t(t) * TR;
+    const int vals = int((r1 - rs < TR) ? (r1 - rs) : TR) * C;
+    const float* buf = s_buf + size_t(st) * kBulkTile;
+    if (!bad) {
+      if (i < 0) {
+#pragma unroll
+        for (int e = 0; e < kBulkElems; ++e) {
+          const int idx = tid + kT * e;
+          hi[e] = idx < vals ? buf[idx] : 0.f;
+          lo[e] = 0.f;
+        }
+      } else if (act) {
+        const float hh = s_hh[i * C + c], hl = s_hl[i * C + c];
+#pragma unroll
+        for (int e = 0; e < kBulkElems; ++e) {
+          const int idx = tid + kT * e;
+          if (idx < vals) {
+            const float xv = buf[idx];
+            float p, q, t2;
+            two_prod(hh, xv, p, q);
+            q = df_fma_rn(hl, xv, q);
+            two_sum(hi[e], -p, hi[e], t2);
+            lo[e] = df_add_rn(lo[e], df_sub_rn(t2, q));
+          }
+        }
+      }
+      if (i == J - 1 && act) {
+        float* wout = W + size_t(rs) * C;
+#pragma unroll
+        for (int e = 0; e < kBulkElems; ++e) {
+          const int idx = tid + kT * e;
+          if (idx < vals) {
+            const float sa = df_add_rn(hi[e], lo[e]);
+            wout[idx] = sa;
+            df_fma(nrm, sa, sa);
+          }
+        }
+      }
+    }
+    // the stage is free once every thread has read it
+    if (__syncthreads_or(bad ? 1 : 0)) {
+      bad = true;
+      break;
+    }
+    if (tid == 0 && n + kBulkStages < nchunks) issue(n + kBulkStages);
+  }
+  if (bad) {
+    // copies issued and not consumed: chunks n .. min(n + kBulkStages, nchunks) - 1
+    if (tid == 0) {
+      const int last = (n + kBulkStages < nchunks) ? n + kBulkStages : nchunks;
+      for (int m = n; m < last; ++m)
+        mbar_wait_bounded(s_bar + (m % kBulkStages), uint32_t(m / kBulkStages) & 1u);
+      if (err) atomicOr(err, kDevErrSpin);
+    }
+    __syncthreads();
+  }
+  red[tid] = (tid / C < RG) ? widen(nrm.hi) + widen(nrm.lo) : 0.0;
+  __syncthreads();
+  if (tid < C && !(need && need[tid] == 0)) {
+    double s = 0.0;
+    for (int g = 0; g < RG; ++g) s += red[g * C + tid];
+    npart[size_t(blockIdx.x) * C + tid] = s;
   }
 }
 
@@ -1109,13 +1411,43 @@ bool table_serves(const OpDev& op, const Work<S>& w) {
   return table_load_mode(a, nullptr);
 }
 
+// Whether the bulk-copy kernels can stream this Work's panels: the block's column
+// mapping (kT % C == 0) and 16-byte aligned chunks (panel bases, the panel
+// stride, every block's first row and the end of the panel).
+// LGT_BULK_STREAM=0 in the environment keeps k_update_df (cross-checks).
+template <typename S>
+bool bulk_stream_ok(const Work<S>& w, const void* V, size_t vstride, const void* Wp,
+                    const int* err) {
+  const char* e = getenv("LGT_BULK_STREAM");
+  if (e && e[0] == '0') return false;
+  const size_t C = size_t(w.C);
+  return err && C > 0 && kT % w.C == 0 && (reinterpret_cast<uintptr_t>(V) % 16) == 0 &&
+         (reinterpret_cast<uintptr_t>(Wp) % 16) == 0 && (vstride % 4) == 0 &&
+         ((size_t(w.red.rpb) * C) % 4) == 0 && ((size_t(w.N) * C) % 4) == 0;
+}
+
 template <typename S, typename SV>
 cudaError_t launch_multidot(Work<S>& w, const SV* V, size_t vstride, const int* jstate, int jfixed,
                             const SV* Wp, cudaStream_t s, int self = 0,
-                            const int* need = nullptr) {
+                            const int* need = nullptr, int* err = nullptr) {
   const int RG = kT / w.C;
   const size_t sh = sizeof(double) * size_t(RG) * kIC * 2 * w.C;
   const int dw = df_reductions_enabled() ? 1 : 0;
+  if constexpr (sizeof(SV) == 4) {
+    // measured slower than k_multidot on the 4x4 quench panel (2.42 vs
+    // 1.72 ms against 15 vectors): opt in with LGT_BULK_DOTS=1
+    const char* bd = getenv("LGT_BULK_DOTS");
+    if (bd && bd[0] == '1' && w.ncomp == 1 && dw && jstate &&
+        bulk_stream_ok(w, V, vstride, Wp, err)) {
+      const size_t shb = sizeof(float) * kBulkStages * kBulkTile + 8 * kBulkStages + sh;
+      cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(k_multidot_bulk), int(shb));
+      if (e != cudaSuccess) return e;
+      k_multidot_bulk<<<w.red.nblk, kT, shb, s>>>(V, vstride, jstate, Wp, w.N, w.C, w.red.rpb,
+                                                  w.part, w.ldT, self, need, err),
+          lgt::note_launch();
+      return cudaGetLastError();
+    }
+  }
   if (w.ncomp == 1)
     k_multidot<SV, 1><<<w.red.nblk, kT, sh, s>>>(V, vstride, jstate, jfixed, Wp, w.N, w.C,
                                                  w.red.rpb, w.part, w.ldT, self, need,
@@ -1132,9 +1464,20 @@ cudaError_t launch_multidot(Work<S>& w, const SV* V, size_t vstride, const int* 
 constexpr size_t kUpdDfSmemMax = 96 * 1024;
 
 template <typename S>
-cudaError_t launch_update(Work<S>& w, S* Wp, cudaStream_t s, const int* need = nullptr) {
+cudaError_t launch_update(Work<S>& w, S* Wp, cudaStream_t s, const int* need = nullptr,
+                          int* err = nullptr) {
   if constexpr (sizeof(S) == 4) {
     const size_t sh = size_t(w.ldT) * size_t(w.C) * 2 * sizeof(float);
+    if (w.ncomp == 1 && df_reductions_enabled() && sh <= kUpdDfSmemMax &&
+        bulk_stream_ok(w, w.V, w.vstride, Wp, err)) {
+      const size_t shb = sizeof(float) * kBulkStages * kBulkTile + 8 * kBulkStages + sh;
+      cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(k_update_bulk), int(shb));
+      if (e != cudaSuccess) return e;
+      k_update_bulk<<<w.red.nblk, kT, shb, s>>>(w.V, w.vstride, w.jstate, Wp, w.N, w.C, w.h,
+                                                w.K, w.status, w.red.rpb, w.npart, need, err),
+          lgt::note_launch();
+      return cudaGetLastError();
+    }
     if (w.ncomp == 1 && df_reductions_enabled() && sh <= kUpdDfSmemMax) {
       cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(k_update_df), int(sh));
       if (e != cudaSuccess) return e;
@@ -1172,12 +1515,13 @@ cudaError_t lanczos_step(const OpDev& op, Work<S>& w, int reorth, double tiny_re
     if (pass > 0)
       k_need_pass<<<finish_blocks(w.K), 128, 0, s>>>(w.npart, w.red.nblk, w.K, w.C, w.ncomp,
                                                  w.status, w.nb, w.need), lgt::note_launch();
-    e = launch_multidot<S, S>(w, w.V, w.vstride, w.jstate, 0, w.W, s, pass == 0 ? 1 : 0, need);
+    e = launch_multidot<S, S>(w, w.V, w.vstride, w.jstate, 0, w.W, s, pass == 0 ? 1 : 0, need,
+                              op.err);
     if (e != cudaSuccess) return e;
     k_finish_dots<<<fdb, 128, 0, s>>>(w.part, w.red.nblk, w.ldT, w.jstate, 0, w.K, w.C, w.ncomp,
                                       w.h, w.alpha, w.ldT, pass == 0, w.status,
                                       pass == 0 ? 1 : 0, w.nb), lgt::note_launch();
-    e = launch_update<S>(w, w.W, s, need);
+    e = launch_update<S>(w, w.W, s, need, op.err);
     if (e != cudaSuccess) return e;
   }
   k_finish_norm<<<finish_blocks(w.K), 128, 0, s>>>(w.npart, w.red.nblk, w.K, w.C, w.ncomp, w.jstate,
@@ -1492,8 +1836,9 @@ std::string autotune(OpDev* op, Work<S>& w, cudaStream_t s, TuneChoice* out) {
         const int jj = (jv < J ? jv : J) - 1;  // step index: jj + 1 vectors
         KCK(cudaMemcpyAsync(w.jstate, &jj, sizeof(int), cudaMemcpyHostToDevice, s));
         t += timed([&] {
-          cudaError_t e = launch_multidot<S, S>(w, w.V, w.vstride, w.jstate, 0, w.W, s);
-          if (e == cudaSuccess) e = launch_update<S>(w, w.W, s);
+          cudaError_t e =
+              launch_multidot<S, S>(w, w.V, w.vstride, w.jstate, 0, w.W, s, 0, nullptr, op->err);
+          if (e == cudaSuccess) e = launch_update<S>(w, w.W, s, nullptr, op->err);
           return e;
         });
       }

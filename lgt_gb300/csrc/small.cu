@@ -29,6 +29,8 @@
 #include <tuple>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "lgt_dfloat.cuh"
 #include "lgt_moves.cuh"
 #include "lgt_rank.cuh"
@@ -173,6 +175,49 @@ __device__ double block_sum(double v, double* red, double* out) {
   return block_sum(v, red, out, [](double) {});
 }
 
+// The sum over a unit's CTAs of one double per thread.  CL = 1: block_sum.
+// CL = 2 (a cluster of two CTAs per unit, rows split between them): each
+// CTA's total goes into slot [par][rank] of both CTAs' `xch`, and after the
+// cluster barrier thread 0 of each CTA adds slot 0 and slot 1 in that order,
+// so both CTAs hold bitwise the same sum (their control flow, which depends
+// only on such sums, stays identical).  `par` flips at every call, so a CTA
+// running ahead never overwrites a slot that its peer has yet to read.
+template <int CL, class Root>
+__device__ double unit_sum(double v, double* red, double* out, double* xch, int& par, Root root) {
+  if constexpr (CL == 1) {
+    return block_sum(v, red, out, root);
+  } else {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const int tid = threadIdx.x;
+    const unsigned cr = cl.block_rank();
+    red[tid] = v;
+    __syncthreads();
+    if (tid < 32) {
+      double s = 0.0;
+      for (int i = tid; i < int(blockDim.x); i += 32) s += red[i];
+      s = warp_sum(s);
+      if (tid == 0) {
+        xch[par * 2 + cr] = s;
+        cl.map_shared_rank(xch, cr ^ 1u)[par * 2 + cr] = s;
+      }
+    }
+    cl.sync();
+    if (tid == 0) {
+      const double s = xch[par * 2] + xch[par * 2 + 1];
+      out[0] = s;
+      root(s);
+    }
+    par ^= 1;
+    __syncthreads();
+    return out[0];
+  }
+}
+template <int CL>
+__device__ double unit_sum(double v, double* red, double* out, double* xch, int& par) {
+  return unit_sum<CL>(v, red, out, xch, par, [](double) {});
+}
+
 __device__ __forceinline__ df shfl_xor_df(df v, int o) {
   return df{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
 }
@@ -202,10 +247,16 @@ __device__ __forceinline__ double warp_scatter4_df(const df* p, int lane) {
   return widen(kk.hi) + widen(kk.lo);
 }
 
-// One ground-state solve per CTA.  S: storage/matvec precision of the
-// Krylov basis (double, or float for the FP32-mixed path); R: rows per
-// thread held in registers (N <= R * 512).
-template <typename S, int R>
+// One ground-state solve per unit of CL CTAs.  S: storage/matvec precision
+// of the Krylov basis (double, or float for the FP32-mixed path); R: rows
+// per thread held in registers (N <= CL * R * 512).  CL = 2 runs a unit on
+// a cluster of two CTAs: CTA rank c owns rows c R nthr .. (c + 1) R nthr - 1,
+// every reduction adds the two CTAs' totals in rank order (unit_sum and the
+// dot exchange), so both CTAs take the same branches at every step; each
+// CTA keeps the whole basis (a new vector's rows are stored into both CTAs'
+// shared memory, or once into the unit's global basis) and the cluster
+// barrier after each store orders it before the next product.
+template <typename S, int R, int CL>
 __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* probs,
                                                       const SmallUnit* units, SmallParams prm) {
   extern __shared__ __align__(16) unsigned char s_basis[];  // (m + 1) x N when prm.v_smem
@@ -217,13 +268,36 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
   __shared__ double s_work[3 * kMaxM];
   __shared__ double s_theta, s_resid;
   __shared__ int s_flag, s_zwarm;
-  const SmallUnit U = units[blockIdx.x];
+  __shared__ double s_xch[4];                 // unit_sum exchange (CL = 2)
+  __shared__ double s_xh[2][2][kMaxM + 2];    // dot exchange [parity][rank][slot] (CL = 2)
+  int par_sum = 0, par_dot = 0;
+  const SmallUnit U = units[blockIdx.x / CL];
   const SmallProblem P = probs[U.prob];
   const int N = P.N;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const int nthr = blockDim.x, nwarps = nthr >> 5;  // rows r = tid + i * nthr, i < R
+  const int nthr = blockDim.x, nwarps = nthr >> 5;  // rows r = rbase + tid + i * nthr, i < R
   const int m = (prm.m < N) ? prm.m : N;
   S* V = reinterpret_cast<S*>(prm.v_smem ? static_cast<void*>(s_basis) : U.V);
+  unsigned cr = 0;  // the CTA's rank in its unit
+  S* Vpeer = nullptr;  // the peer CTA's copy of the basis (CL = 2, basis in shared memory)
+  if constexpr (CL == 2) {
+    cr = cooperative_groups::this_cluster().block_rank();
+    if (prm.v_smem) Vpeer = cooperative_groups::this_cluster().map_shared_rank(V, cr ^ 1u);
+    // both CTAs running before either touches the other's shared memory
+    cooperative_groups::this_cluster().sync();
+  }
+  const int rbase = int(cr) * nthr * R;
+  // a basis entry: into this CTA's basis and, with a split unit keeping the
+  // basis in shared memory, into the peer's copy
+  auto put_v = [&](size_t idx, S val) {
+    V[idx] = val;
+    if (CL == 2 && Vpeer) Vpeer[idx] = val;
+  };
+  // orders this unit's stores (basis, X) before any CTA of the unit reads them
+  auto unit_sync = [&]() {
+    if constexpr (CL == 2) cooperative_groups::this_cluster().sync();
+    else __syncthreads();
+  };
   const S cE = S(U.cE), cm = S(U.cm), ch = S(U.ch), cp = S(U.cp);
   const bool fp32 = sizeof(S) == 4;
   const double tiny_rel = fp32 ? 1e-6 : 1e-12;
@@ -242,7 +316,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
   double nrm = 0.0;
 #pragma unroll
   for (int i = 0; i < R; ++i) {
-    const int r = tid + i * nthr;
+    const int r = rbase + tid + i * nthr;
     w[i] = (r < N) ? (prm.start_given ? U.psi[size_t(r) * U.psi_stride]
                                       : start_normal(prm.seed, U.k, r))
                    : 0.0;
@@ -255,14 +329,14 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
     s_sum[1] = sv * rs;
     s_sum[2] = rs;
   };
-  block_sum(nrm, s_red, s_sum, norm_root);
+  unit_sum<CL>(nrm, s_red, s_sum, s_xch, par_sum, norm_root);
   nrm = s_sum[1];
 #pragma unroll
   for (int i = 0; i < R; ++i) {
-    const int r = tid + i * nthr;
-    if (r < N) V[r] = S(w[i] / nrm);
+    const int r = rbase + tid + i * nthr;
+    if (r < N) put_v(size_t(r), S(w[i] / nrm));
   }
-  __syncthreads();
+  unit_sync();
 
   int n = 0, restarts = 0, steps = 0;
   bool converged = false;
@@ -277,7 +351,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
       // w = H v_j (matvec in the storage precision)
 #pragma unroll
       for (int i = 0; i < R; ++i) {
-        const int r = tid + i * nthr;
+        const int r = rbase + tid + i * nthr;
         if (r < N) {
           S acc = (cE * S(P.e2[r]) + cm * S(P.stag[r])) * vj[r];
           const int q1 = P.rowptr[r + 1];
@@ -318,7 +392,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
             df pd[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
 #pragma unroll
             for (int i = 0; i < R; ++i) {
-              const int r = tid + i * nthr;
+              const int r = rbase + tid + i * nthr;
               if (r < N) {
 #pragma unroll
                 for (int q = 0; q < 4; ++q)
@@ -336,7 +410,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
           double p[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
           for (int i = 0; i < R; ++i) {
-            const int r = tid + i * nthr;
+            const int r = rbase + tid + i * nthr;
             if (r < N) {
 #pragma unroll
               for (int q = 0; q < 4; ++q)
@@ -362,15 +436,36 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
           if ((lane & 7) == 0 && b0 + qv <= jd) s_part[b0 + qv][wid] = kk;
         }
         __syncthreads();
-        if (tid <= jd) {
-          double s0 = 0.0, s1 = 0.0;
-          int ww = 0;
-          for (; ww + 1 < nwarps; ww += 2) {
-            s0 += s_part[tid][ww];
-            s1 += s_part[tid][ww + 1];
+        if constexpr (CL == 2) {
+          // this CTA's dot totals into slot [par][rank] of both CTAs
+          if (tid <= jd) {
+            double s0 = 0.0, s1 = 0.0;
+            int ww = 0;
+            for (; ww + 1 < nwarps; ww += 2) {
+              s0 += s_part[tid][ww];
+              s1 += s_part[tid][ww + 1];
+            }
+            if (ww < nwarps) s0 += s_part[tid][ww];
+            s_xh[par_dot][cr][tid] = s0 + s1;
+            cooperative_groups::this_cluster().map_shared_rank(&s_xh[par_dot][cr][tid],
+                                                               cr ^ 1u)[0] = s0 + s1;
           }
-          if (ww < nwarps) s0 += s_part[tid][ww];
-          const double sum = s0 + s1;
+          cooperative_groups::this_cluster().sync();
+        }
+        if (tid <= jd) {
+          double sum;
+          if constexpr (CL == 2) {
+            sum = s_xh[par_dot][0][tid] + s_xh[par_dot][1][tid];
+          } else {
+            double s0 = 0.0, s1 = 0.0;
+            int ww = 0;
+            for (; ww + 1 < nwarps; ww += 2) {
+              s0 += s_part[tid][ww];
+              s1 += s_part[tid][ww + 1];
+            }
+            if (ww < nwarps) s0 += s_part[tid][ww];
+            sum = s0 + s1;
+          }
           s_h[tid] = sum;
           if (tid == j) s_alpha[j] = (pass == 0) ? sum : s_alpha[j] + sum;
           if (kDF) {  // the update's coefficients as FP32 pairs, once per block
@@ -379,6 +474,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
             s_hl[tid] = narrow(sum - widen(hh));
           }
         }
+        par_dot ^= 1;
         __syncthreads();
         if (pass == 0) nb = ss = s_h[j + 1];
         if constexpr (kDF) {
@@ -391,7 +487,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
             }
 #pragma unroll
             for (int i = 0; i < R; ++i) {
-              const int r = tid + i * nthr;
+              const int r = rbase + tid + i * nthr;
               if (r < N) {
                 df x{wh[i], wl[i]};
 #pragma unroll
@@ -409,7 +505,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
           for (int q = 0; q < 4; ++q) h4[q] = (b0 + q <= j) ? s_h[b0 + q] : 0.0;
 #pragma unroll
           for (int i = 0; i < R; ++i) {
-            const int r = tid + i * nthr;
+            const int r = rbase + tid + i * nthr;
             if (r < N) {
 #pragma unroll
               for (int q = 0; q < 4; ++q)
@@ -429,7 +525,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
         }
         // beta = ||w||, 1 / beta and the exhaustion test of this step, by
         // thread 0 (alpha_j is final: the pass's reduction synchronised)
-        ss = block_sum(s1, s_red, s_sum, [&](double sv) {
+        ss = unit_sum<CL>(s1, s_red, s_sum, s_xch, par_sum, [&](double sv) {
           const double rs = (sv > 0.0) ? rsqrt(sv) : 0.0;
           const double b = sv * rs;
           s_sum[1] = b;
@@ -456,18 +552,18 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
       if (s_exh) {
         exhausted = true;
       } else if (j + 1 < m + 1) {
-        S* vn = V + size_t(j + 1) * N;
 #pragma unroll
         for (int i = 0; i < R; ++i) {
-          const int r = tid + i * nthr;
+          const int r = rbase + tid + i * nthr;
           if constexpr (kDF) {
             // (wh + wl)(rh + rl) to FP32: the leading product and the two
             // cross terms, one final rounding
             if (r < N)
-              vn[r] = S(df_fma_rn(wh[i], s_rb[0],
-                                  df_fma_rn(wh[i], s_rb[1], df_mul_rn(wl[i], s_rb[0]))));
+              put_v(size_t(j + 1) * N + r,
+                    S(df_fma_rn(wh[i], s_rb[0],
+                                df_fma_rn(wh[i], s_rb[1], df_mul_rn(wl[i], s_rb[0])))));
           } else {
-            if (r < N) vn[r] = to_storage<S>(w[i] * rbeta);
+            if (r < N) put_v(size_t(j + 1) * N + r, to_storage<S>(w[i] * rbeta));
           }
         }
       }
@@ -475,7 +571,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
       const bool check = exhausted || (j + 1 == m) ||
                          (j + 1 >= 2 * prm.check_every && (j + 1) % prm.check_every == 0);
       if (check) {
-        __syncthreads();
+        unit_sync();
         if (wid == 0) {
           const double th =
               fp32 ? warp_lowest_eig_f32(s_alpha, s_beta, n, s_z, s_work, s_zwarm != 0,
@@ -501,14 +597,14 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
           break;
         }
       } else {
-        __syncthreads();
+        unit_sync();
       }
       if (exhausted) break;
     }
     // Ritz vector x = sum z_i V_i (z of the last check, at size n)
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      const int r = tid + i * nthr;
+      const int r = rbase + tid + i * nthr;
       double xv = 0.0;
       if (r < N)
         for (int b = 0; b < n; ++b) xv = fma(s_z[b], widen(V[size_t(b) * N + r]), xv);
@@ -519,15 +615,16 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
     double s2 = 0.0;
 #pragma unroll
     for (int i = 0; i < R; ++i) s2 = fma(w[i], w[i], s2);
-    block_sum(s2, s_red, s_sum, norm_root);
+    unit_sum<CL>(s2, s_red, s_sum, s_xch, par_sum, norm_root);
     const double xn = s_sum[1];
-    __syncthreads();
+    // every CTA of the unit has formed its Ritz rows from the old basis
+    unit_sync();
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      const int r = tid + i * nthr;
-      if (r < N) V[r] = S(w[i] / xn);
+      const int r = rbase + tid + i * nthr;
+      if (r < N) put_v(size_t(r), S(w[i] / xn));
     }
-    __syncthreads();
+    unit_sync();
     ++restarts;
   }
 
@@ -535,21 +632,21 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
   double s2 = 0.0;
 #pragma unroll
   for (int i = 0; i < R; ++i) s2 = fma(w[i], w[i], s2);
-  block_sum(s2, s_red, s_sum, norm_root);
+  unit_sum<CL>(s2, s_red, s_sum, s_xch, par_sum, norm_root);
   const double xn = s_sum[1];
   double* X = U.x;
 #pragma unroll
   for (int i = 0; i < R; ++i) {
-    const int r = tid + i * nthr;
+    const int r = rbase + tid + i * nthr;
     w[i] /= xn;
     if (r < N) X[r] = w[i];
   }
-  __syncthreads();
+  unit_sync();
   double y[R];
   double ey = 0.0;
 #pragma unroll
   for (int i = 0; i < R; ++i) {
-    const int r = tid + i * nthr;
+    const int r = rbase + tid + i * nthr;
     y[i] = 0.0;
     if (r < N) {
       double acc = (U.cE * double(P.e2[r]) + U.cm * double(P.stag[r])) * X[r];
@@ -564,21 +661,21 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
     }
     ey = fma(w[i], y[i], ey);
   }
-  const double Erq = block_sum(ey, s_red, s_sum);
+  const double Erq = unit_sum<CL>(ey, s_red, s_sum, s_xch, par_sum);
   double rs = 0.0;
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const double d = y[i] - Erq * w[i];
     rs = fma(d, d, rs);
   }
-  block_sum(rs, s_red, s_sum, norm_root);
+  unit_sum<CL>(rs, s_red, s_sum, s_xch, par_sum, norm_root);
   const double rnorm = s_sum[1];
 #pragma unroll
   for (int i = 0; i < R; ++i) {
-    const int r = tid + i * nthr;
+    const int r = rbase + tid + i * nthr;
     if (r < N) U.psi[size_t(r) * U.psi_stride] = w[i];
   }
-  if (tid == 0) {
+  if (tid == 0 && cr == 0) {
     U.out[0] = fp32 ? Erq : theta;
     U.out[1] = rnorm;
     U.out[2] = double(steps);
@@ -586,6 +683,9 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
     U.out[4] = converged ? 1.0 : 0.0;
     U.out[5] = resid;
   }
+  // no CTA of a split unit leaves while its peer may still access its
+  // shared memory
+  if constexpr (CL == 2) cooperative_groups::this_cluster().sync();
 }
 
 // Rows per thread R (a template case: the rows live in registers) and just
@@ -602,13 +702,17 @@ bool getenv_flag(const char* name, int def) {
 // Dynamic shared memory a CTA may take beside the kernel's static arrays.
 constexpr int kCtaSmemMax = 200 * 1024;
 
+// CL = 2 splits every unit over a cluster of two CTAs (cluster launch); the
+// rows per thread then count half a sector.
 template <typename S>
 cudaError_t launch_cta(const SmallProblem* probs, const SmallUnit* units, int nunits, int maxN,
-                       const SmallParams& prm_in, cudaStream_t s, int rows_per_thread) {
-  int R = (maxN + kCta - 1) / kCta;
+                       const SmallParams& prm_in, cudaStream_t s, int rows_per_thread,
+                       int cl = 1) {
+  const int rowsN = (cl == 2) ? (maxN + 1) / 2 : maxN;  // rows a CTA holds
+  int R = (rowsN + kCta - 1) / kCta;
   if (rows_per_thread > R) R = rows_per_thread;
   auto threads_for = [&](int rr) {
-    int t = ((maxN + rr - 1) / rr + 31) / 32 * 32;
+    int t = ((rowsN + rr - 1) / rr + 31) / 32 * 32;
     return t < 64 ? 64 : t;  // the reduction of step j uses threads 0..j
   };
   // Krylov basis of every unit in shared memory when the largest fits
@@ -618,16 +722,36 @@ cudaError_t launch_cta(const SmallProblem* probs, const SmallUnit* units, int nu
   const bool smem = getenv_flag("LGT_CTA_BASIS_SMEM", 1) && vbytes <= size_t(kCtaSmemMax);
   prm.v_smem = smem ? 1 : 0;
   const int dyn = smem ? int((vbytes + 15) / 16 * 16) : 0;
-#define LGT_CTA_CASE(RR)                                                                    \
-  if (R <= RR) {                                                                            \
-    if (dyn > 0) { /* static + dynamic may pass 48 KB: opt in per device */                \
-      cudaError_t ea = lgt::raise_smem_limit(                                               \
-          reinterpret_cast<const void*>(k_lanczos_cta<S, RR>), kCtaSmemMax);                \
-      if (ea != cudaSuccess) return ea;                                                     \
-    }                                                                                       \
-    k_lanczos_cta<S, RR><<<nunits, threads_for(RR), dyn, s>>>(probs, units, prm),          \
-        lgt::note_launch();                                                                 \
-    return cudaGetLastError();                                                              \
+  auto go = [&](auto kern, int rr) -> cudaError_t {
+    if (dyn > 0) {  // static + dynamic may pass 48 KB: opt in per device
+      cudaError_t ea = lgt::raise_smem_limit(reinterpret_cast<const void*>(kern), kCtaSmemMax);
+      if (ea != cudaSuccess) return ea;
+    }
+    if (cl == 2) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(unsigned(nunits) * 2u);
+      cfg.blockDim = dim3(unsigned(threads_for(rr)));
+      cfg.dynamicSmemBytes = size_t(dyn);
+      cfg.stream = s;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = 2;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      cudaError_t e = cudaLaunchKernelEx(&cfg, kern, probs, units, prm);
+      lgt::note_launch();
+      if (e != cudaSuccess) return e;
+      return cudaGetLastError();
+    }
+    kern<<<nunits, threads_for(rr), dyn, s>>>(probs, units, prm), lgt::note_launch();
+    return cudaGetLastError();
+  };
+#define LGT_CTA_CASE(RR)                                                   \
+  if (R <= RR) {                                                           \
+    if (cl == 2) return go(k_lanczos_cta<S, RR, 2>, RR);                   \
+    return go(k_lanczos_cta<S, RR, 1>, RR);                                \
   }
   LGT_CTA_CASE(1)
   LGT_CTA_CASE(2)
@@ -768,61 +892,83 @@ std::string small_ground_states(const std::vector<SmallJob>& jobs, const SmallPa
   EventPair evp;
   SCK(evp.create());
   cudaEvent_t e0 = evp.a, e1 = evp.b;
-  auto launch = [&](int rows) {
-    return mixed ? launch_cta<float>(d_probs, d_units, int(nunits), maxN, prm, s, rows)
-                 : launch_cta<double>(d_probs, d_units, int(nunits), maxN, prm, s, rows);
+  auto launch = [&](int rows, int cl) {
+    return mixed ? launch_cta<float>(d_probs, d_units, int(nunits), maxN, prm, s, rows, cl)
+                 : launch_cta<double>(d_probs, d_units, int(nunits), maxN, prm, s, rows, cl);
   };
+  // LGT_CTA_CLUSTER=1 or 2 fixes the CTAs per unit; unset, the tuner decides
+  int cl_env = 0;
+  if (const char* ce = getenv("LGT_CTA_CLUSTER")) cl_env = (ce[0] == '2') ? 2 : (ce[0] == '1' ? 1 : 0);
   int rows = prm.rows_per_thread;
-  if (rows == 0 && !prm.start_given) {
-    // Autotuner: rows per thread R0 (the fewest that fit 512 threads), R0 + 1
-    // or 2 R0 (fewer warps: fewer FP64 instructions per basis vector, less
-    // latency hiding), timed on this batch once per (largest sector, CTAs,
-    // precision); the solve then runs with the fastest.
-    static std::mutex mu;
-    static std::map<std::tuple<int, int, int>, int> cache;
-    const auto key = std::make_tuple(maxN, int(nunits), mixed ? 1 : 0);
+  int cl = cl_env ? cl_env : 1;
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int, int>, std::pair<int, int>> cache;
+  const auto key = std::make_tuple(maxN, int(nunits), mixed ? 1 : 0, cl_env);
+  if (rows == 0) {
+    // Autotuner over the launch shape: CTAs per unit (1, or a cluster of 2
+    // holding half the rows each) and rows per thread R0 (the fewest that
+    // fit 512 threads), R0 + 1 or 2 R0 (fewer warps: fewer instructions per
+    // basis vector, less latency hiding); timed on this batch once per
+    // (largest sector, units, precision), the solve then runs with the
+    // fastest.  A solve from a given start vector takes the tuned shape when
+    // there is one, else the smallest.
     std::unique_lock<std::mutex> lk(mu);
     auto it = cache.find(key);
     if (it != cache.end()) {
-      rows = it->second;
-    } else {
+      rows = it->second.first;
+      cl = it->second.second;
+    } else if (!prm.start_given) {
       const char* en = getenv("LGT_AUTOTUNE");
-      const int r0 = (maxN + 511) / 512;
-      rows = r0;
-      // candidates: the rows-per-thread cases R0, R0 + 1 and 2 R0 (rounded up
-      // to an instantiated case), each with at least 64 threads
+      // candidates: for each CTAs-per-unit count, the rows-per-thread cases
+      // R0, R0 + 1 and 2 R0 (rounded up to an instantiated case), each with
+      // at least 64 threads
       auto round_case = [](int r) { return r <= 3 ? r : (r <= 4 ? 4 : (r <= 8 ? 8 : 16)); };
-      std::vector<int> cand;
-      for (int r : {r0, r0 + 1, 2 * r0}) {
-        const int rc = round_case(r);
-        if (rc <= 16 && (maxN + rc - 1) / rc >= 64 &&
-            std::find(cand.begin(), cand.end(), rc) == cand.end())
-          cand.push_back(rc);
+      std::vector<std::pair<int, int>> cand;
+      for (int cc : {1, 2}) {
+        if (cl_env && cc != cl_env) continue;
+        const int rowsN = (cc == 2) ? (maxN + 1) / 2 : maxN;
+        const int r0 = (rowsN + 511) / 512;
+        for (int r : {r0, r0 + 1, 2 * r0}) {
+          const int rc = round_case(r);
+          const auto cp = std::make_pair(rc, cc);
+          if (rc <= 16 && (rowsN + rc - 1) / rc >= 64 &&
+              std::find(cand.begin(), cand.end(), cp) == cand.end())
+            cand.push_back(cp);
+        }
+        if (cand.empty() || cand.back().second != cc) cand.push_back({r0, cc});
       }
+      rows = cand[0].first;
+      cl = cand[0].second;
       if (!(en && en[0] == '0') && cand.size() > 1) {
         float best = 3e38f;
-        // each candidate twice, the faster run counts (a first run pays
+        // each candidate twice, the second run counts (a first run pays
         // the kernel's load and cold caches)
         for (int rep = 0; rep < 2; ++rep)
-          for (int rr : cand) {
+          for (auto& cc : cand) {
             cudaEventRecord(e0, s);
-            cudaError_t ce = launch(rr);
+            cudaError_t ce = launch(cc.first, cc.second);
             cudaEventRecord(e1, s);
+            if (ce != cudaSuccess && cc.second == 2) {  // no room for the cluster: skip it
+              cudaGetLastError();
+              SCK(cudaEventSynchronize(e1));
+              continue;
+            }
             if (ce != cudaSuccess) return std::string("k_lanczos_cta: ") + cudaGetErrorString(ce);
             SCK(cudaEventSynchronize(e1));
             float ms = 0.f;
             cudaEventElapsedTime(&ms, e0, e1);
             if (rep == 1 && ms < best) {
               best = ms;
-              rows = rr;
+              rows = cc.first;
+              cl = cc.second;
             }
           }
       }
-      cache[key] = rows;
+      cache[key] = std::make_pair(rows, cl);
     }
   }
   cudaEventRecord(e0, s);
-  cudaError_t e = launch(rows);
+  cudaError_t e = launch(rows, cl);
   cudaEventRecord(e1, s);
   if (e != cudaSuccess) return std::string("k_lanczos_cta: ") + cudaGetErrorString(e);
   std::vector<double> out(nunits * 8);

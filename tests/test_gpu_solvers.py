@@ -160,3 +160,60 @@ def test_mixed_with_fp64_refinement(oracle, lgt, solver, nx, ny, model):
         for key in ("E2_mean", "n_stag", "plaq_mean", "nf_even"):
             assert abs(obs[k][key] - mo[key]) <= 1e-10, (k, key, obs[k][key] - mo[key])
     H.close()
+
+
+@pytest.mark.parametrize("smem", ["0", "1"])
+@pytest.mark.parametrize("precision", ["fp32_mixed", "fp64"])
+@pytest.mark.parametrize("nx,ny,model", [(4, 2, "ref"), (3, 3, "pjw"), (2, 2, "ref")])
+def test_cta_cluster_split(oracle, lgt, monkeypatch, smem, precision, nx, ny, model):
+    """Each point on a cluster of two CTAs (LGT_CTA_CLUSTER=2: rows split,
+    dot and norm totals exchanged through distributed shared memory, the
+    basis kept whole in both CTAs or once in global memory with
+    LGT_CTA_BASIS_SMEM=0): energies and states against the FP64 oracle, and
+    against the one-CTA solve."""
+    monkeypatch.setenv("LGT_CTA_BASIS_SMEM", smem)
+    ob, gb = _basis(oracle, lgt, nx, ny)
+    gs = np.array([0.5, 0.9, 1.4, 2.0, 1.1])
+    H = lgt.build_hamiltonian(gb, g=gs, t=1.0, m=0.5, model=model)
+    monkeypatch.setenv("LGT_CTA_CLUSTER", "2")
+    E2, p2, info = lgt.find_ground_state(H, tol=1e-12, precision=precision, solver="cta",
+                                         as_complex=False, return_info=True)
+    monkeypatch.setenv("LGT_CTA_CLUSTER", "1")
+    E1, p1 = lgt.find_ground_state(H, tol=1e-12, precision=precision, solver="cta",
+                                   as_complex=False)
+    for k in range(len(gs)):
+        Ho = oracle.build_hamiltonian(ob, g=gs[k], t=1.0, m=0.5, model=model)
+        E0o, psio = oracle.ground_state(Ho)
+        assert abs(E2[k] - E0o) <= 1e-10 * abs(E0o), (k, E2[k], E0o)
+        assert abs(abs(np.dot(p2[:, k], psio)) - 1.0) <= 1e-8
+        assert abs(E2[k] - E1[k]) <= 1e-10 * abs(E0o)
+        assert info["residual"][k] <= (1e-11 if precision == "fp64" else 1e-3)
+    H.close()
+
+
+def test_cta_cluster_uneven_and_refined(oracle, lgt, monkeypatch):
+    """Split units in an uneven batch (the 4x2, 3x3 and 3x2 sectors in one
+    launch) and the FP64 refinement's second launch from a given start
+    vector, both on clusters of two CTAs."""
+    monkeypatch.setenv("LGT_CTA_CLUSTER", "2")
+    Hs, obs_b = [], []
+    for nx, ny in ((4, 2), (3, 3), (3, 2)):
+        ob, gb = _basis(oracle, lgt, nx, ny)
+        gs = np.array([0.7, 1.6])
+        Hs.append(lgt.build_hamiltonian(gb, g=gs, t=1.0, m=0.4))
+        obs_b.append((ob, gs))
+    res = lgt.find_ground_states(Hs, tol=1e-12, precision="fp32_mixed")
+    for (ob, gs), (E0, psi) in zip(obs_b, res):
+        for k in range(2):
+            Ho = oracle.build_hamiltonian(ob, g=gs[k], t=1.0, m=0.4)
+            E0o, _ = oracle.ground_state(Ho)
+            assert abs(E0[k] - E0o) <= 1e-10 * abs(E0o)
+    E0, psi = lgt.find_ground_state(Hs[0], tol=1e-12, precision="fp32_mixed", solver="cta",
+                                    refine_steps=20, as_complex=False)
+    ob, gs = obs_b[0]
+    for k in range(2):
+        Ho = oracle.build_hamiltonian(ob, g=gs[k], t=1.0, m=0.4)
+        E0o, _ = oracle.ground_state(Ho)
+        assert abs(E0[k] - E0o) <= 1e-12 * abs(E0o)
+    for H in Hs:
+        H.close()
