@@ -348,12 +348,18 @@ __global__ void __launch_bounds__(kT, 3) k_multidot_bulk(const float* __restrict
             }
           } else {
             const int q = sl - 1;
+            const bool full = vals == kBulkTile;
 #pragma unroll
             for (int qq = 0; qq < kIC; ++qq)
               if (qq == q) {
+                if (full) {
 #pragma unroll
-                for (int e = 0; e < kBulkElems; ++e)
-                  if (tid + kT * e < vals) df_fma(a[qq], buf[tid + kT * e], w[e]);
+                  for (int e = 0; e < kBulkElems; ++e) df_fma(a[qq], buf[tid + kT * e], w[e]);
+                } else {
+#pragma unroll
+                  for (int e = 0; e < kBulkElems; ++e)
+                    if (tid + kT * e < vals) df_fma(a[qq], buf[tid + kT * e], w[e]);
+                }
               }
           }
           // self slots of this group (W against itself) after its last vector
@@ -750,12 +756,14 @@ __global__ void __launch_bounds__(kT) k_update_bulk(const float* __restrict__ V,
   df nrm{0.f, 0.f};
   int n = 0;
   bool bad = false;
+  // chunk n = tile t, slot i (-1: W, then the basis vectors), advanced
+  // incrementally (no division per chunk)
+  int i = -1;
+  int64_t rs = r0;
+  int vals = int((r1 - rs < TR) ? (r1 - rs) : TR) * C;
   for (; n < nchunks; ++n) {
     const int st = n % kBulkStages;
     if (!mbar_wait_bounded(s_bar + st, uint32_t(n / kBulkStages) & 1u)) bad = true;
-    const int t = n / (J + 1), i = n - t * (J + 1) - 1;
-    const int64_t rs = r0 + int64_t(t) * TR;
-    const int vals = int((r1 - rs < TR) ? (r1 - rs) : TR) * C;
     const float* buf = s_buf + size_t(st) * kBulkTile;
     if (!bad) {
       if (i < 0) {
@@ -766,18 +774,17 @@ __global__ void __launch_bounds__(kT) k_update_bulk(const float* __restrict__ V,
           lo[e] = 0.f;
         }
       } else if (act) {
+        // values past the tile's rows (a partial last tile) are computed on
+        // whatever the stage holds and never stored
         const float hh = s_hh[i * C + c], hl = s_hl[i * C + c];
 #pragma unroll
         for (int e = 0; e < kBulkElems; ++e) {
-          const int idx = tid + kT * e;
-          if (idx < vals) {
-            const float xv = buf[idx];
-            float p, q, t2;
-            two_prod(hh, xv, p, q);
-            q = df_fma_rn(hl, xv, q);
-            two_sum(hi[e], -p, hi[e], t2);
-            lo[e] = df_add_rn(lo[e], df_sub_rn(t2, q));
-          }
+          const float xv = buf[tid + kT * e];
+          float p, q, t2;
+          two_prod(hh, xv, p, q);
+          q = df_fma_rn(hl, xv, q);
+          two_sum(hi[e], -p, hi[e], t2);
+          lo[e] = df_add_rn(lo[e], df_sub_rn(t2, q));
         }
       }
       if (i == J - 1 && act) {
@@ -792,6 +799,11 @@ __global__ void __launch_bounds__(kT) k_update_bulk(const float* __restrict__ V,
           }
         }
       }
+    }
+    if (++i == J) {
+      i = -1;
+      rs += TR;
+      vals = int((r1 - rs < TR) ? (r1 - rs) : TR) * C;
     }
     // the stage is free once every thread has read it
     if (__syncthreads_or(bad ? 1 : 0)) {
@@ -880,7 +892,20 @@ __global__ void k_scale(const SI* src, SO* dstbase, size_t vstride, const int* j
   const double b = bnorm[k];
   const double inv = (b > 0.0) ? 1.0 / b : 0.0;
   const float invf = float(inv);
-  for (int64_t row = int64_t(blockIdx.x) * RG + rg; row < N; row += int64_t(gridDim.x) * RG) {
+  const int64_t step = int64_t(gridDim.x) * RG;
+  int64_t row = int64_t(blockIdx.x) * RG + rg;
+  if (sizeof(SI) == 4 && sizeof(SO) == 4 && !gather) {
+    // FP32 to FP32 (the new Krylov vector): four rows' loads in flight
+    // before their stores
+    for (; row + 3 * step < N; row += 4 * step) {
+      float v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) v[u] = float(src[size_t(row + u * step) * C + c]);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) dst[size_t(row + u * step) * C + c] = SO(v[u] * invf);
+    }
+  }
+  for (; row < N; row += step) {
     const size_t i = size_t(row) * C + c;
     // gather: row `row` of the destination is row gather[row] of the source
     const size_t si = gather ? size_t(gather[row]) * C + c : i;
@@ -1143,6 +1168,64 @@ __global__ void k_combine_split(const S* __restrict__ V, size_t vstride, const d
       acc = fma(cf, widen(V[size_t(i) * vstride + off + cb]), acc);
     }
     out[(scatter ? size_t(scatter[row]) * C : off) + c] = acc;
+  }
+}
+
+// k_combine_split for an FP32 basis with double-float sums: one thread per
+// (row, point) forms both outputs from the float pair (v_i[re col],
+// v_i[im col]) of each basis vector, with the FP64 coefficients split once
+// per block into FP32 pairs (shared memory, [C][ldT][2] pairs) and the sums
+// carried as double-floats (TwoSum of the leading parts, trailing parts
+// summed apart): FP64-class results without FP64 FMAs per element.
+__global__ void __launch_bounds__(kT) k_combine_split_df(const float* __restrict__ V,
+                                                         size_t vstride, const double* coef,
+                                                         int ldT, const int* len, double* out,
+                                                         int64_t N, int K, const int* scatter) {
+  extern __shared__ float s_cf[];  // [C][ldT][2] hi, then [C][ldT][2] lo
+  const int C = 2 * K;
+  const int ncf = C * ldT * 2;
+  float* s_hi = s_cf;
+  float* s_lo = s_cf + ncf;
+  for (int i = threadIdx.x; i < ncf; i += blockDim.x) {
+    const double cv = coef[i];
+    const float h = narrow(cv);
+    s_hi[i] = h;
+    s_lo[i] = narrow(cv - widen(h));
+  }
+  __syncthreads();
+  const int64_t n = N * K;
+  for (int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; idx < n;
+       idx += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t row = idx / K;
+    const int k = int(idx - row * K);
+    const int ca = 2 * k, cb = ca + 1;
+    const size_t off = size_t(row) * C + ca;
+    df re{0.f, 0.f}, im{0.f, 0.f};
+    const int na = len[ca], nb = len[cb];
+    const int nmax = na > nb ? na : nb;
+    auto term = [](df& acc, float ch, float cl, float v) {
+      float p, e, t;
+      two_prod(ch, v, p, e);
+      e = df_fma_rn(cl, v, e);
+      two_sum(acc.hi, p, acc.hi, t);
+      acc.lo = df_add_rn(acc.lo, df_add_rn(t, e));
+    };
+    for (int i = 0; i < nmax; ++i) {
+      const float2 v = *reinterpret_cast<const float2*>(V + size_t(i) * vstride + off);
+      if (i < na) {  // the real column: (Re c) v to Re psi, (Im c) v to Im psi
+        const int q = (ca * ldT + i) * 2;
+        term(re, s_hi[q], s_lo[q], v.x);
+        term(im, s_hi[q + 1], s_lo[q + 1], v.x);
+      }
+      if (i < nb) {  // i (cr + i ci) v = -ci v + i cr v
+        const int q = (cb * ldT + i) * 2;
+        term(re, -s_hi[q + 1], -s_lo[q + 1], v.y);
+        term(im, s_hi[q], s_lo[q], v.y);
+      }
+    }
+    double* o = out + (scatter ? size_t(scatter[row]) * C : size_t(row) * C) + ca;
+    o[0] = widen(re.hi) + widen(re.lo);
+    o[1] = widen(im.hi) + widen(im.lo);
   }
 }
 
@@ -2187,8 +2270,20 @@ std::string expm_impl(const OpDev& op_in, const KrylovParams& p, Work<S>& w, dou
         if (++guard_sub > 4096) return std::string("NOCONV: exponential step could not be split");
       }
       KCK(cudaMemcpyAsync(errs.data(), w.resid, sizeof(double) * Kc, cudaMemcpyDeviceToHost, s));
-      k_combine_split<S><<<grid_for(N * C), kT, 0, s>>>(w.V, w.vstride, w.coef, w.ldT, w.len, X, N,
-                                                        K, perm), lgt::note_launch();
+      if constexpr (sizeof(S) == 4) {
+        const size_t shc = sizeof(float) * 4 * size_t(C) * w.ldT;
+        if (df_reductions_enabled() && shc <= 48 * 1024 && (w.vstride % 2) == 0) {
+          k_combine_split_df<<<grid_for(N * K), kT, shc, s>>>(
+              reinterpret_cast<const float*>(w.V), w.vstride, w.coef, w.ldT, w.len, X, N, K,
+              perm), lgt::note_launch();
+        } else {
+          k_combine_split<S><<<grid_for(N * C), kT, 0, s>>>(w.V, w.vstride, w.coef, w.ldT, w.len,
+                                                            X, N, K, perm), lgt::note_launch();
+        }
+      } else {
+        k_combine_split<S><<<grid_for(N * C), kT, 0, s>>>(w.V, w.vstride, w.coef, w.ldT, w.len, X,
+                                                          N, K, perm), lgt::note_launch();
+      }
       KCK(cudaGetLastError());
       KCK(cudaStreamSynchronize(s));
       for (int k = 0; k < K; ++k) maxerr = fmax(maxerr, hypot(errs[2 * k], errs[2 * k + 1]));
