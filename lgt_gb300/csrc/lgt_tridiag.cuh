@@ -240,42 +240,92 @@ __device__ inline double warp_lowest_eig_f32(const double* a64, const double* b6
     }
   }
   const float theta = 0.5f * (lo + hi);
-  if (lane == 0) {
-    // inverse iteration on T - (theta - delta) I, positive definite
-    const float shift = theta - 4e-7f * scale;
-    if (warm_z) {
-      for (int i = 0; i < n; ++i) zf[i] = float(z[i]);
-    } else {
-      for (int i = 0; i < n; ++i) zf[i] = 1.0f;
-    }
-    const int reps = warm_z ? 1 : 2;
-    for (int rep = 0; rep < reps; ++rep) {
-      float piv = a[0] - shift;
-      if (piv <= 0.0f) piv = 1e-30f;
-      d[0] = 1.0f / piv;
-      for (int i = 1; i < n; ++i) {
-        l[i - 1] = b[i - 1] * d[i - 1];
-        piv = (a[i] - shift) - l[i - 1] * b[i - 1];
-        if (piv <= 0.0f) piv = 1e-30f;
-        d[i] = 1.0f / piv;
+  // inverse iteration on T - (theta - delta) I, positive definite: the two
+  // triangular sweeps by lane 0 (the factorisation merged into the forward
+  // sweep, the diagonal scaling into the backward one), each reading its
+  // operands eight entries ahead so that the sweep waits on its arithmetic
+  // rather than on shared-memory loads; the scaling by the whole warp
+  const float shift = theta - 4e-7f * scale;
+  for (int i = lane; i < n; i += 32) zf[i] = warm_z ? float(z[i]) : 1.0f;
+  __syncwarp();
+  const int reps = warm_z ? 1 : 2;
+  for (int rep = 0; rep < reps; ++rep) {
+    if (lane == 0) {
+      float dprev = 0.0f, bprev = 0.0f, zprev = 0.0f;
+      for (int i0 = 0; i0 < n; i0 += 8) {
+        float ac[8], bc[8], zc[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int i = i0 + u;
+          ac[u] = (i < n) ? a[i] : 0.0f;
+          bc[u] = (i < n) ? b[i] : 0.0f;
+          zc[u] = (i < n) ? zf[i] : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int i = i0 + u;
+          if (i < n) {
+            float piv;
+            if (i == 0) {
+              piv = ac[u] - shift;
+            } else {
+              const float li = bprev * dprev;
+              l[i - 1] = li;
+              piv = (ac[u] - shift) - li * bprev;
+              zc[u] = fmaf(-li, zprev, zc[u]);
+            }
+            if (piv <= 0.0f) piv = 1e-30f;
+            const float di = 1.0f / piv;
+            d[i] = di;
+            zf[i] = zc[u];
+            dprev = di;
+            bprev = bc[u];
+            zprev = zc[u];
+          }
+        }
       }
-      for (int i = 1; i < n; ++i) zf[i] = fmaf(-l[i - 1], zf[i - 1], zf[i]);
-      for (int i = 0; i < n; ++i) zf[i] *= d[i];
-      for (int i = n - 2; i >= 0; --i) zf[i] = fmaf(-l[i], zf[i + 1], zf[i]);
-      float mx = 0.0f;
-      for (int i = 0; i < n; ++i) mx = fmaxf(mx, fabsf(zf[i]));
-      const float inv = 1.0f / mx;
-      float nn = 0.0f;
-      for (int i = 0; i < n; ++i) {
-        zf[i] *= inv;
-        nn = fmaf(zf[i], zf[i], nn);
+      float znext = 0.0f;
+      for (int i1 = n - 1; i1 >= 0; i1 -= 8) {
+        float zc[8], dc[8], lc[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int i = i1 - u;
+          zc[u] = (i >= 0) ? zf[i] : 0.0f;
+          dc[u] = (i >= 0) ? d[i] : 0.0f;
+          lc[u] = (i >= 0 && i < n - 1) ? l[i] : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int i = i1 - u;
+          if (i >= 0) {
+            float t = zc[u] * dc[u];
+            if (i < n - 1) t = fmaf(-lc[u], znext, t);
+            zf[i] = t;
+            znext = t;
+          }
+        }
       }
-      const float in2 = rsqrtf(nn);
-      for (int i = 0; i < n; ++i) zf[i] *= in2;
     }
-    const float sg = (zf[0] < 0.0f) ? -1.0f : 1.0f;
-    for (int i = 0; i < n; ++i) z[i] = double(sg * zf[i]);
+    __syncwarp();
+    float mx = 0.0f;
+    for (int i = lane; i < n; i += 32) mx = fmaxf(mx, fabsf(zf[i]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    const float inv = 1.0f / mx;
+    float nn = 0.0f;
+    for (int i = lane; i < n; i += 32) {
+      const float zi = zf[i] * inv;
+      zf[i] = zi;
+      nn = fmaf(zi, zi, nn);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nn += __shfl_xor_sync(0xffffffffu, nn, o);
+    const float in2 = rsqrtf(nn);
+    for (int i = lane; i < n; i += 32) zf[i] *= in2;
+    __syncwarp();
   }
+  const float sg = (zf[0] < 0.0f) ? -1.0f : 1.0f;
+  for (int i = lane; i < n; i += 32) z[i] = double(sg * zf[i]);
   __syncwarp();
   return double(theta);
 }
