@@ -268,6 +268,8 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
   __shared__ double s_work[3 * kMaxM];
   __shared__ double s_theta, s_resid;
   __shared__ int s_flag, s_zwarm;
+  __shared__ int s_next, s_pstep;  // the next check's step; the previous check's step
+  __shared__ double s_pres;        // and its residual
   __shared__ double s_xch[4];                 // unit_sum exchange (CL = 2)
   __shared__ double s_xh[2][2][kMaxM + 2];    // dot exchange [parity][rank][slot] (CL = 2)
   int par_sum = 0, par_dot = 0;
@@ -344,7 +346,12 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
   for (int cycle = 0;; ++cycle) {
     n = 0;
     bool exhausted = false;
-    if (tid == 0) s_zwarm = 0;
+    if (tid == 0) {
+      s_zwarm = 0;
+      s_next = 2 * prm.check_every;
+      s_pstep = 0;
+      s_pres = 0.0;
+    }
     __syncthreads();
     for (int j = 0; j < m; ++j) {
       const S* vj = V + size_t(j) * N;
@@ -567,9 +574,10 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
           }
         }
       }
-      // first check after 2 * check_every steps, then every check_every
-      const bool check = exhausted || (j + 1 == m) ||
-                         (j + 1 >= 2 * prm.check_every && (j + 1) % prm.check_every == 0);
+      // first check after 2 * check_every steps, then every check_every, or
+      // sooner where the residual's geometric decay between the last two
+      // checks predicts convergence (s_next)
+      const bool check = exhausted || (j + 1 == m) || (j + 1 >= s_next);
       if (check) {
         unit_sync();
         if (wid == 0) {
@@ -583,6 +591,20 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
             // FP32 panels resolve residuals to ~1e-6 |H|: relative floor
             const double tl = fp32 ? fmax(tol, 3e-6 * fmax(fabs(th), 1.0)) : tol;
             s_flag = (exhausted || rr <= tl) ? 1 : 0;
+            int nxt = n + prm.check_every;
+            if (s_pstep > 0 && rr > tl && s_pres > rr) {
+              const double rate = log(rr / s_pres) / double(n - s_pstep);  // < 0
+              // steps to the tolerance at that rate (a 25% margin measured
+              // slower: 121k vs 124.7k GS/s on the 4x2 batch)
+              const double need = log(tl / rr) / rate;                      // > 0 steps
+              if (need < double(prm.check_every)) {
+                const int p = n + ((need > 1.0) ? int(ceil(need)) : 1);
+                if (p < nxt) nxt = p;
+              }
+            }
+            s_next = nxt;
+            s_pstep = n;
+            s_pres = rr;
             s_theta = th;
             s_resid = rr;
             s_zwarm = 1;
