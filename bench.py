@@ -781,13 +781,12 @@ def main():
         "value": value, "unit": "GS/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "fp32-mixed (f32 H*psi and Krylov storage; f64-class dots/reorth, f64 "
-                 "tridiagonal/RQ)",
+        "dtype": "fp32-mixed (f32 H*psi, Krylov storage; f64-class reductions)",
         "data": "synthetic",
         "config": {"workload": workload, "l2": "flushed between steps (512 MB write, untimed)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "basis_build_ms": _r(r["basis_ms"])},
-        "roofline": {"kernel": "k_hpsi_%s (%s), 4x4 N=8563545 K=8 complex FP32, ref model"
+        "roofline": {"kernel": "k_hpsi_%s (%s), 4x4 K=8 complex FP32"
                                % ("table" if fam.startswith("table") else "fixed", dom["kernel"]),
                      "bound": "hbm", "achieved": _r(dom["gbs"]), "peak": rf["peak"],
                      "unit": "GB/s", "frac": _r(dom["frac"]), "traffic": traffic,
@@ -796,12 +795,11 @@ def main():
                      "frac_incl_table": _r(dom.get("frac_incl_table")),
                      "peak_source": rf["peak_src"]},
         "cpu_baseline": {"value": _r(cpu_val), "unit": "GS/s", "cores": ncores, "kind": "port",
-                         "sample": "one step (64 points), one point per host process: oracle "
-                                   "basis+H, scipy eigsh tol 1e-10 ncv 50, measure"},
+                         "sample": "one 64-point step, a point per process: oracle basis+H, "
+                                   "eigsh tol 1e-10, measure"},
         "e2e": {"value": e2e_val, "unit": "GS/s", "h2d_bytes_per_step": r["h2d"],
                 "d2h_bytes_per_step": r["d2h"],
-                "path": "build_basis+build_hamiltonian+find_ground_state+measure_ED each step, "
-                        "host numpy buffers",
+                "path": "basis+H+ground state+measure each step, host buffers",
                 "handles_kept_gs_per_s": _r(KPTS / statistics.mean(r["e2e_reuse"]))},
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],
@@ -809,7 +807,7 @@ def main():
             "c1_rel_dE": _r(extra["c1_3x2_fp64_tol1e-12"]["rel_dE"]),
             "c3_4x3": {k: [_r(v["rel_dE0"]), _r(v["abs_dE2"]), _r(v["abs_dn_stag"])]
                        for k, v in c3.items()},
-            "c3_cols": "rel dE0, abs dE2, abs dn_stag vs FP64 oracle; refined: 12 FP64 steps",
+            "c3_cols": "rel dE0, abs dE2, abs dn_stag vs FP64 oracle",
             "c4_gs_per_s": _r(c4["gs_per_s_incl_host_copies"]),
             "c4_min_max": [_r(v) for v in c4["gs_per_s_min_max"]],
             "c4_cpu_gs_per_s": _r(c4["cpu_baseline_gs_per_s"]),

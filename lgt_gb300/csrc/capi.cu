@@ -69,10 +69,10 @@ lgt_status set_device(const lgt_basis* b) {
 }
 
 // Reads and clears the basis' device error word.
-lgt_status check_device_errors(const lgt_basis* b) {
-  int err = 0;
-  CUDA_OR_FAIL(cudaMemcpyAsync(&err, b->B.err, sizeof(int), cudaMemcpyDeviceToHost, b->B.stream));
-  CUDA_OR_FAIL(cudaStreamSynchronize(b->B.stream));
+// The device error word: a fast path copies it into pinned memory next to
+// its results so that it rides on the same synchronisation; err_status
+// interprets a value (and resets the device word).
+lgt_status err_status(const lgt_basis* b, int err) {
   if (err) {
     cudaMemsetAsync(b->B.err, 0, sizeof(int), b->B.stream);
     std::string m = "device self-check failed:";
@@ -83,6 +83,13 @@ lgt_status check_device_errors(const lgt_basis* b) {
     return fail(LGT_ERR_DEVICE, m);
   }
   return LGT_OK;
+}
+
+lgt_status check_device_errors(const lgt_basis* b) {
+  int err = 0;
+  CUDA_OR_FAIL(cudaMemcpyAsync(&err, b->B.err, sizeof(int), cudaMemcpyDeviceToHost, b->B.stream));
+  CUDA_OR_FAIL(cudaStreamSynchronize(b->B.stream));
+  return err_status(b, err);
 }
 
 lgt_status upload_couplings(lgt_ham* h) {
@@ -569,8 +576,14 @@ lgt_status cta_solve(const std::vector<lgt_ham*>& hams, const KrylovParams& p,
   }
   lgt_ham* h0 = hams[0];
   double secs = 0.0;
+  // one basis for all jobs: its error word rides on the solve's own
+  // synchronisation
+  bool one_basis = true;
+  for (lgt_ham* hh : hams) one_basis = one_basis && hh->b == h0->b;
+  int dev_err = 0;
   std::string m = small_ground_states(jobs, small_params(p), p.mixed, &h0->small,
-                                      h0->b->B.stream, &secs);
+                                      h0->b->B.stream, &secs,
+                                      one_basis ? h0->b->B.err : nullptr, &dev_err);
   if (!m.empty()) return from_msg(m);
   if (p.mixed && p.refine > 0) {
     // FP64 correction: a short FP64 Lanczos per point (Krylov dimension
@@ -590,7 +603,8 @@ lgt_status cta_solve(const std::vector<lgt_ham*>& hams, const KrylovParams& p,
     q.start_given = 1;
     q.rows_per_thread = 0;
     double secs2 = 0.0;
-    m = small_ground_states(jobs, q, 0, &h0->small, h0->b->B.stream, &secs2);
+    m = small_ground_states(jobs, q, 0, &h0->small, h0->b->B.stream, &secs2,
+                            one_basis ? h0->b->B.err : nullptr, &dev_err);
     if (!m.empty()) return from_msg(m);
     secs += secs2;
     for (size_t i = 0; i < hams.size(); ++i)
@@ -617,9 +631,14 @@ lgt_status cta_solve(const std::vector<lgt_ham*>& hams, const KrylovParams& p,
     info->max_residual = maxr;
     info->seconds = secs;
   }
-  for (lgt_ham* h : hams) {
-    lgt_status de = check_device_errors(h->b);
+  if (one_basis) {
+    lgt_status de = err_status(h0->b, dev_err);
     if (de) return de;
+  } else {
+    for (lgt_ham* h : hams) {
+      lgt_status de = check_device_errors(h->b);
+      if (de) return de;
+    }
   }
   if (!all) return fail(LGT_ERR_NOCONV, "NOCONV: Lanczos did not converge within maxiter restarts");
   return LGT_OK;
@@ -804,11 +823,25 @@ lgt_status observe_dev(lgt_ham* h, const T* x, int ncomp, std::vector<double>* f
                                     static_cast<double*>(h->part.p), static_cast<double*>(h->out.p),
                                     h->b->B.err, s);
   if (e != cudaSuccess) return cuda_fail(e, "observe");
-  feat->resize(size_t(h->K) * nf);
-  CUDA_OR_FAIL(cudaMemcpyAsync(feat->data(), h->out.p, sizeof(double) * feat->size(),
-                               cudaMemcpyDeviceToHost, s));
+  // features and the device error word back through pinned memory, one
+  // synchronisation
+  const size_t n = size_t(h->K) * nf;
+  if (h->hfeat_n < n + 1) {  // the features, then the error word
+    if (h->hfeat) {
+      CUDA_OR_FAIL(cudaStreamSynchronize(s));
+      cudaFreeHost(h->hfeat);
+    }
+    h->hfeat = nullptr;
+    h->hfeat_n = 0;
+    CUDA_OR_FAIL(cudaMallocHost(&h->hfeat, sizeof(double) * (n + 1)));
+    h->hfeat_n = n + 1;
+  }
+  int* herr = reinterpret_cast<int*>(h->hfeat + n);
+  CUDA_OR_FAIL(cudaMemcpyAsync(h->hfeat, h->out.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  CUDA_OR_FAIL(cudaMemcpyAsync(herr, h->b->B.err, sizeof(int), cudaMemcpyDeviceToHost, s));
   CUDA_OR_FAIL(cudaStreamSynchronize(s));
-  return LGT_OK;
+  feat->assign(h->hfeat, h->hfeat + n);
+  return err_status(h->b, *herr);
 }
 
 // Observables after every step: the summaries and, where asked for, the
@@ -930,7 +963,7 @@ lgt_status lgt_observe(const lgt_ham* hc, const void* psi, int32_t ncomp, int32_
       std::memcpy(plaq_grid + size_t(k) * G.nP, f + 2 * G.ns, sizeof(double) * G.nP);
     if (summary) summarize_obs(G, f, t_now, summary + k);
   }
-  return check_device_errors(h->b);
+  return LGT_OK;  // observe_dev read the device error word
 }
 
 lgt_status lgt_energy(const lgt_ham* hc, const void* psi, int32_t ncomp, uint32_t flags,
@@ -995,7 +1028,11 @@ void lgt_ham_destroy(lgt_ham* h) {
   free_pattern(&h->pattern, s);
   free_nbr_table(&h->table);
   free_nbr_table(&h->table_ord);
-  dev_free(h->small.base, s);
+  free_small_work(&h->small, s);
+  if (h->hfeat) {
+    if (s) cudaStreamSynchronize(s);
+    cudaFreeHost(h->hfeat);
+  }
   dev_free(h->coef_d, s);
   dev_free(h->coef_f, s);
   lgt_basis* b = const_cast<lgt_basis*>(h->b);

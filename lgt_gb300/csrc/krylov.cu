@@ -97,6 +97,10 @@ __global__ void k_randn(S* out, int64_t N, int C, int ncomp, uint64_t seed) {
 #ifndef LGT_MD_MINB
 #define LGT_MD_MINB 4  // resident blocks per SM the dot kernel's registers must allow (FP64)
 #endif
+#ifndef LGT_MD_TRIP
+#define LGT_MD_TRIP 3  // rows per trip of the FP32 double-float dot pass (4x4 K = 8 quench:
+                       // 2 rows 17.70, 3 rows 18.21, 4 rows with 2 blocks/SM 17.96 steps/s)
+#endif
 #ifndef LGT_MD_MINB_F32
 #define LGT_MD_MINB_F32 3  // the same for FP32 panels (measured with chunks sized to the
                            // vectors left: 4 without spills beats 5 with them)
@@ -126,22 +130,27 @@ __device__ __forceinline__ void dots_chunk(const S* __restrict__ V, size_t vstri
       for (int q = 0; q < NQ; ++q)
         vq[q] = reinterpret_cast<const float*>(V) + size_t((i0 + q < Jv) ? i0 + q : ilast) * vstride + c;
       const float* wp = reinterpret_cast<const float*>(W) + c;
-      // two rows per trip: 2 (NQ + 1) loads in flight before the arithmetic
+      // LGT_MD_TRIP rows per trip: LGT_MD_TRIP (NQ + 1) loads in flight
+      // before the arithmetic
+      constexpr int kTrip = LGT_MD_TRIP;
       int64_t row = r0 + rg;
-      for (; row + RG < r1; row += 2 * int64_t(RG)) {
-        const size_t oa = size_t(row) * C, ob = oa + size_t(RG) * C;
-        const float wa = __ldg(wp + oa), wb = __ldg(wp + ob);
-        float va[NQ], vb[NQ];
+      for (; row + (kTrip - 1) * int64_t(RG) < r1; row += kTrip * int64_t(RG)) {
+        size_t o[kTrip];
+        float wv[kTrip], vv[kTrip][NQ];
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) {
-          va[q] = __ldg(vq[q] + oa);
-          vb[q] = __ldg(vq[q] + ob);
+        for (int u = 0; u < kTrip; ++u) {
+          o[u] = size_t(row + u * int64_t(RG)) * C;
+          wv[u] = __ldg(wp + o[u]);
         }
 #pragma unroll
         for (int q = 0; q < NQ; ++q)
+#pragma unroll
+          for (int u = 0; u < kTrip; ++u) vv[u][q] = __ldg(vq[q] + o[u]);
+#pragma unroll
+        for (int q = 0; q < NQ; ++q)
           if (i0 + q < J) {
-            df_fma(a[q], (i0 + q < Jv) ? va[q] : wa, wa);
-            df_fma(a[q], (i0 + q < Jv) ? vb[q] : wb, wb);
+#pragma unroll
+            for (int u = 0; u < kTrip; ++u) df_fma(a[q], (i0 + q < Jv) ? vv[u][q] : wv[u], wv[u]);
           }
       }
       for (; row < r1; row += RG) {

@@ -103,6 +103,8 @@ struct lgt_ham {
   int seg_smem = 0;
   KrylovCache* cache = nullptr;
   DevBuf x, y, part, out;
+  double* hfeat = nullptr;  // pinned staging of the observables' features and error word
+  size_t hfeat_n = 0;
   Pattern pattern;          // lookup pass of the per-CTA solver (built on demand)
   SmallWork small;
   // neighbour table of the panel H*psi (built on demand by the autotuner;

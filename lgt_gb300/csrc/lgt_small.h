@@ -68,16 +68,28 @@ struct SmallJob {
   bool* converged;                  // host [K] or null
 };
 
+// Per-Hamiltonian workspace of the per-CTA solver: device memory for the
+// unit tables, bases and outputs; a pinned host buffer that stages the
+// tables (kept as the copy last uploaded, so that an unchanged batch skips
+// the upload) and the outputs; and the timing events.
 struct SmallWork {
   void* base = nullptr;
   size_t bytes = 0;
+  void* host = nullptr;      // pinned: [uploaded tables][outputs]
+  size_t host_bytes = 0;
+  size_t up_bytes = 0;       // bytes of tables the device buffer holds (0: none)
+  cudaEvent_t ev[2] = {nullptr, nullptr};
 };
+void free_small_work(SmallWork* w, cudaStream_t s);
 
 std::string build_pattern(const BasisDev& B, uint32_t model, Pattern* P, cudaStream_t s);
 void free_pattern(Pattern* P, cudaStream_t s);
 
 // All (job, point) units in one launch, largest sectors first.
+// dev_err (may be null): a device error word copied back with the results
+// into *err_out (or'd into it).
 std::string small_ground_states(const std::vector<SmallJob>& jobs, const SmallParams& prm,
-                                int mixed, SmallWork* ws, cudaStream_t s, double* seconds);
+                                int mixed, SmallWork* ws, cudaStream_t s, double* seconds,
+                                const int* dev_err = nullptr, int* err_out = nullptr);
 
 }  // namespace lgt
