@@ -209,10 +209,10 @@ def gpu_workloads(args, rank, world):
             e1 = torch.cuda.Event(enable_timing=True)
             with torch.cuda.stream(stream):
                 e0.record(stream)
-                C.check(lib.lgt_ground_state(H.handle, o, E0.ctypes.data, psi_dev.data_ptr(),
-                                             None, C.LGT_DEVICE_PTRS, info))
-                C.check(lib.lgt_observe(H.handle, psi_dev.data_ptr(), 1, C.LGT_FP64,
-                                        C.LGT_DEVICE_PTRS, 0.0, None, None, None, summ))
+                # find_ground_state + measure_ED in one call (one synchronisation)
+                C.check(lib.lgt_ground_state_observe(H.handle, o, E0.ctypes.data,
+                                                     psi_dev.data_ptr(), None, C.LGT_DEVICE_PTRS,
+                                                     info, None, None, None, summ))
                 e1.record(stream)
             e1.synchronize()
             if it >= warmup:
@@ -336,10 +336,9 @@ def gs_only(args):
         e1 = torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(stream):
             e0.record(stream)
-            C.check(lib.lgt_ground_state(H.handle, o, E0.ctypes.data, psi.data_ptr(), None,
-                                         C.LGT_DEVICE_PTRS, info))
-            C.check(lib.lgt_observe(H.handle, psi.data_ptr(), 1, C.LGT_FP64, C.LGT_DEVICE_PTRS,
-                                    0.0, None, None, None, summ))
+            C.check(lib.lgt_ground_state_observe(H.handle, o, E0.ctypes.data, psi.data_ptr(),
+                                                 None, C.LGT_DEVICE_PTRS, info, None, None, None,
+                                                 summ))
             e1.record(stream)
         e1.synchronize()
         if it >= args.warmup:

@@ -228,6 +228,17 @@ LGT_API lgt_status lgt_ham_row_order(lgt_ham* h, int32_t* perm);
 LGT_API lgt_status lgt_ground_state(lgt_ham* h, const lgt_krylov_opts* opts, double* E0, void* psi,
                             double* residual, uint32_t flags, lgt_info* info);
 
+/* find_ground_state then measure_ED of the ground states in one call
+   (gs_benchmark.jl:116-125 runs the two per point): as lgt_ground_state
+   followed by lgt_observe(h, psi, 1, LGT_FP64, flags, 0, nf_grid, E2_grid,
+   plaq_grid, summary), with the observables launched on the device result
+   before the one synchronisation that returns both.  Replaces the pair
+   find_ground_state (finite_ed.jl:333-341) + measure_ED (:369-393). */
+LGT_API lgt_status lgt_ground_state_observe(lgt_ham* h, const lgt_krylov_opts* opts, double* E0,
+                                            void* psi, double* residual, uint32_t flags,
+                                            lgt_info* info, double* nf_grid, double* E2_grid,
+                                            double* plaq_grid, lgt_obs* summary);
+
 /* find_ground_state over several Hamiltonians at once (the GS benchmark
    grid, gs_benchmark.jl:36-52,86-175, and lattices / sectors of uneven
    dimension): every (Hamiltonian, point) pair of a sector up to 8192 states

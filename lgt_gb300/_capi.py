@@ -48,7 +48,8 @@ EXPORTS = (
     "lgt_launch_count",
     "lgt_ham_create", "lgt_ham_set_couplings", "lgt_ham_nnz", "lgt_ham_export_csr",
     "lgt_ham_row_order",
-    "lgt_matvec", "lgt_ground_state", "lgt_ground_state_batch", "lgt_expm_steps",
+    "lgt_matvec", "lgt_ground_state", "lgt_ground_state_observe", "lgt_ground_state_batch",
+    "lgt_expm_steps",
     "lgt_expm_steps_grids", "lgt_observe",
     "lgt_observe_noalloc", "lgt_energy", "lgt_autotune", "lgt_ham_destroy",
 )
@@ -158,6 +159,8 @@ def load(build_if_missing: bool = True):
         "lgt_matvec": (i32, [vp, vp, vp, i32, i32, u32]),
         "lgt_ground_state": (i32, [vp, ctypes.POINTER(KrylovOpts), vp, vp, vp, u32,
                                    ctypes.POINTER(Info)]),
+        "lgt_ground_state_observe": (i32, [vp, ctypes.POINTER(KrylovOpts), vp, vp, vp, u32,
+                                           ctypes.POINTER(Info), vp, vp, vp, vp]),
         "lgt_ground_state_batch": (i32, [i32, vp, ctypes.POINTER(KrylovOpts), vp, vp, vp, u32,
                                          ctypes.POINTER(Info)]),
         "lgt_expm_steps": (i32, [vp, ctypes.POINTER(KrylovOpts), dbl, i32, vp, vp, vp, u32,

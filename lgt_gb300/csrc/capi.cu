@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <new>
 #include <string>
 #include <thread>
@@ -90,6 +91,37 @@ lgt_status check_device_errors(const lgt_basis* b) {
   CUDA_OR_FAIL(cudaMemcpyAsync(&err, b->B.err, sizeof(int), cudaMemcpyDeviceToHost, b->B.stream));
   CUDA_OR_FAIL(cudaStreamSynchronize(b->B.stream));
   return err_status(b, err);
+}
+
+// measure_ED's outputs from the features [K][nfeat] of observe_dev.
+void fill_observables(const lgt_ham* h, const double* feat, double t_now, double* nf_grid,
+                      double* E2_grid, double* plaq_grid, lgt_obs* summary) {
+  const Geom& G = h->b->B.G;
+  const int nf = observe_nfeat(G);
+  for (int k = 0; k < h->K; ++k) {
+    const double* f = feat + size_t(k) * nf;
+    if (nf_grid) std::memcpy(nf_grid + size_t(k) * G.ns, f, sizeof(double) * G.ns);
+    if (E2_grid) std::memcpy(E2_grid + size_t(k) * G.ns, f + G.ns, sizeof(double) * G.ns);
+    if (plaq_grid && G.nP)
+      std::memcpy(plaq_grid + size_t(k) * G.nP, f + 2 * G.ns, sizeof(double) * G.nP);
+    if (summary) summarize_obs(G, f, t_now, summary + k);
+  }
+}
+
+// The pinned staging of K feature rows and an error word (observe_dev and
+// the fused ground state + observables call).
+lgt_status ensure_hfeat(lgt_ham* h, size_t n) {
+  if (h->hfeat_n >= n + 1) return LGT_OK;
+  cudaStream_t s = h->b->B.stream;
+  if (h->hfeat) {
+    CUDA_OR_FAIL(cudaStreamSynchronize(s));
+    cudaFreeHost(h->hfeat);
+  }
+  h->hfeat = nullptr;
+  h->hfeat_n = 0;
+  CUDA_OR_FAIL(cudaMallocHost(&h->hfeat, sizeof(double) * (n + 1)));
+  h->hfeat_n = n + 1;
+  return LGT_OK;
 }
 
 lgt_status upload_couplings(lgt_ham* h) {
@@ -538,7 +570,7 @@ SmallParams small_params(const KrylovParams& p) {
 // Per-CTA solves of several Hamiltonians (device panels X[i]).
 lgt_status cta_solve(const std::vector<lgt_ham*>& hams, const KrylovParams& p,
                      const std::vector<double*>& X, double* const* E0, double* const* residual,
-                     lgt_info* info) {
+                     lgt_info* info, const std::function<cudaError_t()>& before_sync = {}) {
   std::vector<SmallJob> jobs;
   std::vector<std::vector<double>> coef(hams.size());
   std::vector<std::vector<int>> steps(hams.size()), rest(hams.size());
@@ -581,9 +613,11 @@ lgt_status cta_solve(const std::vector<lgt_ham*>& hams, const KrylovParams& p,
   bool one_basis = true;
   for (lgt_ham* hh : hams) one_basis = one_basis && hh->b == h0->b;
   int dev_err = 0;
+  const bool refine = p.mixed && p.refine > 0;
   std::string m = small_ground_states(jobs, small_params(p), p.mixed, &h0->small,
                                       h0->b->B.stream, &secs,
-                                      one_basis ? h0->b->B.err : nullptr, &dev_err);
+                                      one_basis ? h0->b->B.err : nullptr, &dev_err,
+                                      refine ? std::function<cudaError_t()>() : before_sync);
   if (!m.empty()) return from_msg(m);
   if (p.mixed && p.refine > 0) {
     // FP64 correction: a short FP64 Lanczos per point (Krylov dimension
@@ -604,7 +638,7 @@ lgt_status cta_solve(const std::vector<lgt_ham*>& hams, const KrylovParams& p,
     q.rows_per_thread = 0;
     double secs2 = 0.0;
     m = small_ground_states(jobs, q, 0, &h0->small, h0->b->B.stream, &secs2,
-                            one_basis ? h0->b->B.err : nullptr, &dev_err);
+                            one_basis ? h0->b->B.err : nullptr, &dev_err, before_sync);
     if (!m.empty()) return from_msg(m);
     secs += secs2;
     for (size_t i = 0; i < hams.size(); ++i)
@@ -698,6 +732,75 @@ lgt_status lgt_ground_state(lgt_ham* h, const lgt_krylov_opts* opts, double* E0,
   if (de) return de;
   if (rc == LGT_ERR_NOCONV) return fail(LGT_ERR_NOCONV, m);
   return LGT_OK;
+}
+
+lgt_status lgt_ground_state_observe(lgt_ham* h, const lgt_krylov_opts* opts, double* E0,
+                                    void* psi, double* residual, uint32_t flags, lgt_info* info,
+                                    double* nf_grid, double* E2_grid, double* plaq_grid,
+                                    lgt_obs* summary) {
+  if (!h || !E0) return fail(LGT_ERR_ARG, "null argument");
+  KrylovParams p = to_params(opts, 0);
+  if (p.check_every > p.krylovdim) p.check_every = p.krylovdim;
+  if (p.start_given && !psi) return fail(LGT_ERR_ARG, "start_given needs psi");
+  lgt_status st = set_device(h->b);
+  if (st) return st;
+  if (!use_cta(h, opts, p)) {
+    // the panel solver: the two calls in turn (the state stays where it is)
+    lgt_status rc = lgt_ground_state(h, opts, E0, psi, residual, flags, info);
+    if (rc != LGT_OK && rc != LGT_ERR_NOCONV) return rc;
+    if (!psi) return rc;
+    lgt_status ro = lgt_observe(h, psi, 1, LGT_FP64, flags, 0.0, nf_grid, E2_grid, plaq_grid,
+                                summary);
+    return ro ? ro : rc;
+  }
+  const int64_t N = h->b->B.dim;
+  if (N == 0) return fail(LGT_ERR_ARG, "empty basis");
+  const size_t bytes = size_t(N) * h->K * sizeof(double);
+  cudaStream_t s = h->b->B.stream;
+  double* X = nullptr;
+  if (psi && on_device(flags)) {
+    X = static_cast<double*>(psi);
+  } else {
+    CUDA_OR_FAIL(h->x.need(bytes, h->b->B.stream));
+    X = static_cast<double*>(h->x.p);
+    if (p.start_given) CUDA_OR_FAIL(cudaMemcpyAsync(X, psi, bytes, cudaMemcpyHostToDevice, s));
+  }
+  const Geom& G = h->b->B.G;
+  const int nf = observe_nfeat(G);
+  int nblk;
+  int64_t rpb;
+  observe_plan(N, &nblk, &rpb);
+  CUDA_OR_FAIL(h->part.need(sizeof(double) * size_t(nblk) * h->K * nf, s));
+  CUDA_OR_FAIL(h->out.need(sizeof(double) * size_t(h->K) * nf, s));
+  const size_t n = size_t(h->K) * nf;
+  st = ensure_hfeat(h, n);
+  if (st) return st;
+  int* herr = reinterpret_cast<int*>(h->hfeat + n);
+  // the observables of the solution, launched before the solve's one
+  // synchronisation
+  auto observe = [&]() -> cudaError_t {
+    cudaError_t e = launch_observe_planned<double>(G, h->b->B.view(), X, h->K, 1, nblk, rpb,
+                                                   static_cast<double*>(h->part.p),
+                                                   static_cast<double*>(h->out.p), h->b->B.err, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(h->hfeat, h->out.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(herr, h->b->B.err, sizeof(int), cudaMemcpyDeviceToHost, s);
+    return e;
+  };
+  std::vector<double> res(h->K);
+  double* r = res.data();
+  lgt_status rc = cta_solve({h}, p, {X}, &E0, &r, info, observe);
+  if (residual) std::memcpy(residual, res.data(), sizeof(double) * h->K);
+  if (rc != LGT_OK && rc != LGT_ERR_NOCONV) return rc;
+  lgt_status de = err_status(h->b, *herr);
+  if (de) return de;
+  fill_observables(h, h->hfeat, 0.0, nf_grid, E2_grid, plaq_grid, summary);
+  if (psi && !on_device(flags)) {
+    CUDA_OR_FAIL(cudaMemcpyAsync(psi, X, bytes, cudaMemcpyDeviceToHost, s));
+    CUDA_OR_FAIL(cudaStreamSynchronize(s));
+  }
+  return rc;
 }
 
 lgt_status lgt_ground_state_batch(int32_t nham, lgt_ham* const* hams, const lgt_krylov_opts* opts,
@@ -826,15 +929,9 @@ lgt_status observe_dev(lgt_ham* h, const T* x, int ncomp, std::vector<double>* f
   // features and the device error word back through pinned memory, one
   // synchronisation
   const size_t n = size_t(h->K) * nf;
-  if (h->hfeat_n < n + 1) {  // the features, then the error word
-    if (h->hfeat) {
-      CUDA_OR_FAIL(cudaStreamSynchronize(s));
-      cudaFreeHost(h->hfeat);
-    }
-    h->hfeat = nullptr;
-    h->hfeat_n = 0;
-    CUDA_OR_FAIL(cudaMallocHost(&h->hfeat, sizeof(double) * (n + 1)));
-    h->hfeat_n = n + 1;
+  {
+    lgt_status hs = ensure_hfeat(h, n);  // the features, then the error word
+    if (hs) return hs;
   }
   int* herr = reinterpret_cast<int*>(h->hfeat + n);
   CUDA_OR_FAIL(cudaMemcpyAsync(h->hfeat, h->out.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
@@ -954,15 +1051,7 @@ lgt_status lgt_observe(const lgt_ham* hc, const void* psi, int32_t ncomp, int32_
   st = (precision == LGT_FP64) ? observe_dev<double>(h, static_cast<const double*>(dx), ncomp, &feat)
                                : observe_dev<float>(h, static_cast<const float*>(dx), ncomp, &feat);
   if (st) return st;
-  const int nf = observe_nfeat(G);
-  for (int k = 0; k < h->K; ++k) {
-    const double* f = feat.data() + size_t(k) * nf;
-    if (nf_grid) std::memcpy(nf_grid + size_t(k) * G.ns, f, sizeof(double) * G.ns);
-    if (E2_grid) std::memcpy(E2_grid + size_t(k) * G.ns, f + G.ns, sizeof(double) * G.ns);
-    if (plaq_grid && G.nP)
-      std::memcpy(plaq_grid + size_t(k) * G.nP, f + 2 * G.ns, sizeof(double) * G.nP);
-    if (summary) summarize_obs(G, f, t_now, summary + k);
-  }
+  fill_observables(h, feat.data(), t_now, nf_grid, E2_grid, plaq_grid, summary);
   return LGT_OK;  // observe_dev read the device error word
 }
 

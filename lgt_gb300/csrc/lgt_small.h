@@ -1,6 +1,7 @@
 // lgt_small.h -- persistent per-CTA Lanczos for small sectors.
 #pragma once
 
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -88,8 +89,12 @@ void free_pattern(Pattern* P, cudaStream_t s);
 // All (job, point) units in one launch, largest sectors first.
 // dev_err (may be null): a device error word copied back with the results
 // into *err_out (or'd into it).
+// before_sync (may be empty): enqueued work of the caller's (e.g. the
+// observables of the solution) run after the solve's output copies and
+// before the one synchronisation.
 std::string small_ground_states(const std::vector<SmallJob>& jobs, const SmallParams& prm,
                                 int mixed, SmallWork* ws, cudaStream_t s, double* seconds,
-                                const int* dev_err = nullptr, int* err_out = nullptr);
+                                const int* dev_err = nullptr, int* err_out = nullptr,
+                                const std::function<cudaError_t()>& before_sync = {});
 
 }  // namespace lgt

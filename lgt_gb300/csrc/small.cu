@@ -847,7 +847,8 @@ void free_pattern(Pattern* P, cudaStream_t s) {
 
 std::string small_ground_states(const std::vector<SmallJob>& jobs, const SmallParams& prm,
                                 int mixed, SmallWork* ws, cudaStream_t s, double* seconds,
-                                const int* dev_err, int* err_out) {
+                                const int* dev_err, int* err_out,
+                                const std::function<cudaError_t()>& before_sync) {
   // problems and units, the largest sectors first
   std::vector<SmallProblem> probs;
   std::vector<SmallUnit> units;
@@ -1033,6 +1034,7 @@ std::string small_ground_states(const std::vector<SmallJob>& jobs, const SmallPa
   SCK(cudaMemcpyAsync(h_out, d_out, sizeof(double) * nunits * 8, cudaMemcpyDeviceToHost, s));
   int* h_err = reinterpret_cast<int*>(h_out + nunits * 8);
   if (dev_err) SCK(cudaMemcpyAsync(h_err, dev_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (before_sync) SCK(before_sync());
   SCK(cudaStreamSynchronize(s));
   if (dev_err && err_out) *err_out |= *h_err;
   const double* out = h_out;
