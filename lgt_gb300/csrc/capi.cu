@@ -115,12 +115,15 @@ lgt_status ensure_hfeat(lgt_ham* h, size_t n) {
   cudaStream_t s = h->b->B.stream;
   if (h->hfeat) {
     CUDA_OR_FAIL(cudaStreamSynchronize(s));
-    cudaFreeHost(h->hfeat);
+    pinned_put(h->hfeat, h->hfeat_n * sizeof(double));
   }
   h->hfeat = nullptr;
   h->hfeat_n = 0;
-  CUDA_OR_FAIL(cudaMallocHost(&h->hfeat, sizeof(double) * (n + 1)));
-  h->hfeat_n = n + 1;
+  void* p = nullptr;
+  size_t cap = 0;
+  CUDA_OR_FAIL(pinned_get(sizeof(double) * (n + 1), &p, &cap));
+  h->hfeat = static_cast<double*>(p);
+  h->hfeat_n = cap / sizeof(double);
   return LGT_OK;
 }
 
@@ -1120,7 +1123,7 @@ void lgt_ham_destroy(lgt_ham* h) {
   free_small_work(&h->small, s);
   if (h->hfeat) {
     if (s) cudaStreamSynchronize(s);
-    cudaFreeHost(h->hfeat);
+    pinned_put(h->hfeat, h->hfeat_n * sizeof(double));
   }
   dev_free(h->coef_d, s);
   dev_free(h->coef_f, s);

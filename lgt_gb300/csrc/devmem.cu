@@ -11,7 +11,14 @@
 // of the panel drivers (allocated once per shape and kept), the stored
 // neighbour tables and the allocation-free observables entry point do not
 // use it.
+//
+// Pinned host staging buffers (the per-CTA solver's tables and outputs, the
+// observables' read-back) come from a process-wide cache by size class:
+// page-locking and unlocking host memory costs far more than a small solve,
+// and a sweep creates and destroys handles per batch.
+#include <map>
 #include <mutex>
+#include <vector>
 
 #include "lgt_internal.h"
 
@@ -49,7 +56,48 @@ cudaError_t pool_of(int dev, cudaMemPool_t* out) {
   return cudaSuccess;
 }
 
+constexpr size_t kPinnedMinBytes = 4096;
+constexpr size_t kPinnedKeepPerClass = 16;
+std::mutex g_pinned_mu;
+std::map<size_t, std::vector<void*>> g_pinned;  // free buffers by capacity
+
 }  // namespace
+
+cudaError_t pinned_get(size_t bytes, void** p, size_t* cap) {
+  size_t c = kPinnedMinBytes;
+  while (c < bytes) c <<= 1;
+  {
+    std::lock_guard<std::mutex> lock(g_pinned_mu);
+    auto it = g_pinned.find(c);
+    if (it != g_pinned.end() && !it->second.empty()) {
+      *p = it->second.back();
+      it->second.pop_back();
+      *cap = c;
+      return cudaSuccess;
+    }
+  }
+  cudaError_t e = cudaMallocHost(p, c);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    *cap = 0;
+    return e;
+  }
+  *cap = c;
+  return cudaSuccess;
+}
+
+void pinned_put(void* p, size_t cap) {
+  if (!p) return;
+  {
+    std::lock_guard<std::mutex> lock(g_pinned_mu);
+    std::vector<void*>& v = g_pinned[cap];
+    if (v.size() < kPinnedKeepPerClass) {
+      v.push_back(p);
+      return;
+    }
+  }
+  cudaFreeHost(p);
+}
 
 cudaError_t dev_alloc(void** p, size_t bytes, cudaStream_t s) {
   *p = nullptr;

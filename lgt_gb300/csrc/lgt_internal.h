@@ -51,6 +51,11 @@ inline bool df_reductions_enabled() {
 // call; a free takes effect after the work enqueued on `s` before it.
 cudaError_t dev_alloc(void** p, size_t bytes, cudaStream_t s);
 cudaError_t dev_free(void* p, cudaStream_t s);
+// Pinned host memory from the library's cache (capacity rounded up to a
+// power of two, at least 4 KB); pinned_put returns it (no copy may still be
+// in flight from or to it).
+cudaError_t pinned_get(size_t bytes, void** p, size_t* cap);
+void pinned_put(void* p, size_t cap);
 template <typename T>
 cudaError_t dev_alloc_n(T** p, size_t n, cudaStream_t s) {
   return dev_alloc(reinterpret_cast<void**>(p), n * sizeof(T), s);

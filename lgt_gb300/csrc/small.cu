@@ -830,7 +830,7 @@ void free_small_work(SmallWork* w, cudaStream_t s) {
   dev_free(w->base, s);
   if (w->host) {
     cudaStreamSynchronize(s);  // a copy staged through it may still be in flight
-    cudaFreeHost(w->host);
+    pinned_put(w->host, w->host_bytes);
   }
   if (w->ev[0]) cudaEventDestroy(w->ev[0]);
   if (w->ev[1]) cudaEventDestroy(w->ev[1]);
@@ -930,13 +930,12 @@ std::string small_ground_states(const std::vector<SmallJob>& jobs, const SmallPa
   if (ws->host_bytes < tb + ob) {
     if (ws->host) {
       SCK(cudaStreamSynchronize(s));
-      cudaFreeHost(ws->host);
+      pinned_put(ws->host, ws->host_bytes);
     }
     ws->host = nullptr;
     ws->host_bytes = 0;
     ws->up_bytes = 0;
-    SCK(cudaMallocHost(&ws->host, tb + ob));
-    ws->host_bytes = tb + ob;
+    SCK(pinned_get(tb + ob, &ws->host, &ws->host_bytes));
   }
   char* hst = static_cast<char*>(ws->host);
   const bool same = ws->up_bytes == pb + ub && memcmp(hst, probs.data(), pb) == 0 &&

@@ -25,6 +25,7 @@ matrices are indexed [ix-1, iy-1].
 from __future__ import annotations
 
 import ctypes
+import weakref
 from collections.abc import Mapping
 
 import numpy as np
@@ -118,6 +119,7 @@ class Basis:
         C.check(L.lgt_basis_dim(self._h, ctypes.byref(d)))
         self.dim = int(d.value)
         self._observers = {}
+        self._hams = weakref.WeakSet()  # Hamiltonians made from this basis
 
     @property
     def handle(self):
@@ -193,8 +195,13 @@ class Basis:
         return int(self.lookup([encode(n_f, e_R, e_U)])[0])
 
     def observer(self, K: int) -> "Hamiltonian":
-        """A K-point operator on this basis used for measurements."""
+        """A K-point operator on this basis used for measurements: any open
+        Hamiltonian of K points made from it (the observables depend on the
+        basis alone), else one of its own."""
         if K not in self._observers:
+            for h in list(self._hams):
+                if h.K == K and h.is_open():
+                    return h
             one = np.ones(K)
             self._observers[K] = Hamiltonian(self, g=one, t=one, m=one, model="pjw")
         return self._observers[K]
@@ -263,6 +270,7 @@ class Hamiltonian:
         h = ctypes.c_void_p()
         C.check(L.lgt_ham_create(basis.handle, self.K, _p(self.g), _p(self.t), _p(self.m),
                                  self.model, ctypes.byref(h)))
+        basis._hams.add(self)
         self._h = h
 
     @property
@@ -272,6 +280,9 @@ class Hamiltonian:
     @property
     def shape(self):
         return (self.basis.dim, self.basis.dim)
+
+    def is_open(self) -> bool:
+        return bool(getattr(self, "_h", None) and self._h.value)
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
