@@ -570,8 +570,10 @@ def roofline(L, C, lib, torch, stream, dev, reps=10, only=None):
     gs = np.random.default_rng(0).uniform(0.5, 1.5, RF_K)
     out = {"N": N, "basis_build_s": basis_s}
     # variants: the autotuner's choice, and each kernel family forced
-    # (LGT_HPSI_VARIANT: 3 fixed shape, 6 stored table; two vectors per lane)
-    forced = {"": None, "_generic": None, "_fixed": "3", "_table": "6", "_table_ordered": "6"}
+    # (LGT_HPSI_VARIANT: 3 fixed shape, 6 stored table, two vectors per lane;
+    # 8 stored table with the neighbour rows gathered by the copy engine)
+    forced = {"": None, "_generic": None, "_fixed": "3", "_table": "6", "_table_ordered": "6",
+              "_gather": "8", "_gather_ordered": "8"}
     models, precs = ("ref", "pjw"), (("fp64", torch.float64, 16), ("fp32", torch.float32, 8))
     if only is not None:
         sfx = "" if only == "auto" else "_" + only
@@ -589,7 +591,7 @@ def roofline(L, C, lib, torch, stream, dev, reps=10, only=None):
         for prec, dtype, s in precs:
             for suffix, var in forced.items():
                 generic = suffix == "_generic"
-                ordered = suffix == "_table_ordered"
+                ordered = suffix.endswith("_ordered")
                 if var is None:
                     os.environ.pop("LGT_HPSI_VARIANT", None)
                 else:
@@ -619,6 +621,8 @@ def roofline(L, C, lib, torch, stream, dev, reps=10, only=None):
                 t = statistics.mean(ts)
                 if generic:
                     kernel = "generic"
+                elif var == "8":
+                    kernel = "table_gather_ordered" if ordered else "table_gather"
                 elif ordered:
                     kernel = "table_ordered_vpl2"
                 elif var is not None:
@@ -666,7 +670,8 @@ def main():
                     help="also write every measured figure (roofline variants, per-config "
                          "detail, quench trajectories' summaries) to this JSON file")
     ap.add_argument("--hpsi-only", default=None,
-                    choices=["auto", "generic", "fixed", "table", "table_ordered"],
+                    choices=["auto", "generic", "fixed", "table", "table_ordered", "gather",
+                             "gather_ordered"],
                     help="--part hpsi: time one kernel family on the reference FP32 panel")
     ap.add_argument("--part", default="all", choices=["all", "hpsi", "gs", "quench"],
                     help="hpsi: only the 4x4 H*psi roofline loop; gs: only the headline "
@@ -768,7 +773,9 @@ def main():
     # autotuner's choice, in the table's row order when that is the table
     dom = rf["ref_fp32"]
     fam = "table" if dom["kernel"].startswith("table") else "fixed"
-    if fam == "table" and "ref_fp32_table_ordered" in rf:
+    if dom["kernel"] == "table_gather" and "ref_fp32_gather_ordered" in rf:
+        dom, fam = rf["ref_fp32_gather_ordered"], "gather_ordered"
+    elif fam == "table" and "ref_fp32_table_ordered" in rf:
         dom, fam = rf["ref_fp32_table_ordered"], "table_ordered"
     traffic = RF_TRAFFIC_BYTES.get(fam) if dom["kernel"] != "generic" else None
     e2e_val = KPTS / statistics.mean(r["e2e_times"])
@@ -786,7 +793,8 @@ def main():
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "basis_build_ms": _r(r["basis_ms"])},
         "roofline": {"kernel": "k_hpsi_%s (%s), 4x4 K=8 complex FP32"
-                               % ("table" if fam.startswith("table") else "fixed", dom["kernel"]),
+                               % ({"fixed": "fixed", "gather_ordered": "table_bulk"}.get(fam, "table"),
+                                  dom["kernel"]),
                      "bound": "hbm", "achieved": _r(dom["gbs"]), "peak": rf["peak"],
                      "unit": "GB/s", "frac": _r(dom["frac"]), "traffic": traffic,
                      "algo_bytes_per_launch": dom["algo_bytes"], "ms_per_launch": _r(dom["ms"]),

@@ -314,14 +314,16 @@ LGT_API lgt_status lgt_energy(const lgt_ham* h, const void* psi, int32_t ncomp, 
    Hamiltonian (4 bytes per off-diagonal entry and per row; no matrix values)
    when its size bound fits min(free device memory / 4, LGT_NBR_TABLE_MB,
    default 16384 MB); LGT_NBR_TABLE=0 disables it.  LGT_AUTOTUNE=0 in the
-   environment keeps the built-in rules; LGT_HPSI_VARIANT=1..7 forces one
+   environment keeps the built-in rules; LGT_HPSI_VARIANT=1..8 forces one
    H*psi kernel (the hpsi_kernel codes below) for cross-checks. */
 typedef struct lgt_tuning {
   int32_t hpsi_kernel;    /* 0 built-in rule, 1 run-time geometry, fixed
                              shape with 2 one / 3 two 16-byte vectors per
                              lane, 4 two vectors as one 32-byte access;
                              5, 6, 7 the same load modes from the stored
-                             neighbour table                                */
+                             neighbour table; 8 the stored table with the
+                             neighbour rows gathered by the copy engine
+                             (FP32 panels of 16 columns)                    */
   int32_t reduce_blocks;  /* block-count cap of the panel reductions         */
   double hpsi_ms;         /* one H*psi with the chosen kernel                */
   double reduce_ms;       /* one 8-vector Gram-Schmidt pass, chosen blocks   */

@@ -1421,7 +1421,7 @@ struct Work {
 
 template <typename S>
 cudaError_t apply_h(const OpDev& op, const S* x, const int* xsel, size_t xstride, S* y, int ncomp,
-                    cudaStream_t s);
+                    cudaStream_t s, int nslots = 1);
 
 template <typename S>
 void set_table(const OpDev& op, HpsiArgs<S>* a) {
@@ -1438,7 +1438,7 @@ void set_table(const OpDev& op, HpsiArgs<S>* a) {
 
 template <>
 cudaError_t apply_h<double>(const OpDev& op, const double* x, const int* xsel, size_t xstride,
-                            double* y, int ncomp, cudaStream_t s) {
+                            double* y, int ncomp, cudaStream_t s, int) {
   HpsiArgs<double> a;
   a.G = op.G;
   a.R = op.R;
@@ -1464,7 +1464,7 @@ cudaError_t apply_h<double>(const OpDev& op, const double* x, const int* xsel, s
 
 template <>
 cudaError_t apply_h<float>(const OpDev& op, const float* x, const int* xsel, size_t xstride,
-                           float* y, int ncomp, cudaStream_t s) {
+                           float* y, int ncomp, cudaStream_t s, int nslots) {
   HpsiArgs<float> a;
   a.G = op.G;
   a.R = op.R;
@@ -1484,6 +1484,8 @@ cudaError_t apply_h<float>(const OpDev& op, const float* x, const int* xsel, siz
   a.xstride = xstride;
   a.force_generic = op.force_generic;
   a.vpl = op.vpl;
+  // rows behind x: every Krylov slot when x + xsel * xstride picks one
+  a.x_rows = xsel ? int64_t(xstride / size_t(a.C)) * nslots : a.N;
   set_table(op, &a);
   return launch_hpsi<float>(a, op.model, s);
 }
@@ -1594,7 +1596,7 @@ cudaError_t launch_update(Work<S>& w, S* Wp, cudaStream_t s, const int* need = n
 template <typename S>
 cudaError_t lanczos_step(const OpDev& op, Work<S>& w, int reorth, double tiny_rel,
                          cudaStream_t s) {
-  cudaError_t e = apply_h<S>(op, w.V, w.jstate, w.vstride, w.W, w.hcomp, s);
+  cudaError_t e = apply_h<S>(op, w.V, w.jstate, w.vstride, w.W, w.hcomp, s, w.m + 1);
   if (e != cudaSuccess) return e;
   const unsigned fdb = finish_blocks(w.ldT * w.K);
   // Classical Gram-Schmidt against the whole basis (this also performs the
@@ -1684,14 +1686,15 @@ bool autotune_enabled() {
 
 void apply_variant(OpDev* op, int v) {
   op->force_generic = (v == kHpsiGeneric) ? 1 : 0;
-  op->use_table = (v >= kHpsiTable1 && v <= kHpsiTable2w) ? 1 : 0;
+  op->use_table = (v >= kHpsiTable1 && v <= kHpsiTableBulk) ? 1 : 0;
   op->vpl = (v == kHpsiFixed1 || v == kHpsiTable1)    ? 1
             : (v == kHpsiFixed2 || v == kHpsiTable2)  ? 2
             : (v == kHpsiFixed2w || v == kHpsiTable2w) ? 3
+            : (v == kHpsiTableBulk)                    ? 4
                                                        : 0;
 }
 
-bool is_table_variant(int v) { return v >= kHpsiTable1 && v <= kHpsiTable2w; }
+bool is_table_variant(int v) { return v >= kHpsiTable1 && v <= kHpsiTableBulk; }
 
 bool stream_capturing(cudaStream_t s) {
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
@@ -1755,11 +1758,11 @@ bool use_krylov_order(const OpDev& op) {
   return op.use_table && op.table_ord && op.table_ord->state == 1 && op.table_ord->perm;
 }
 
-// The H*psi variant forced by LGT_HPSI_VARIANT (1..7), or 0.
+// The H*psi variant forced by LGT_HPSI_VARIANT (1..8), or 0.
 int hpsi_forced() {
   const char* fv = getenv("LGT_HPSI_VARIANT");
   const int v = fv ? atoi(fv) : 0;
-  return (v >= kHpsiGeneric && v <= kHpsiTable2w) ? v : 0;
+  return (v >= kHpsiGeneric && v <= kHpsiTableBulk) ? v : 0;
 }
 
 // Applies variant v, or the built-in rule when v needs a table that cannot
@@ -1830,6 +1833,8 @@ std::string tune_hpsi(OpDev* op, const S* x, S* y, int C, int hcomp, cudaStream_
       cand.push_back(kHpsiTable1);
       if (mode >= 2) cand.push_back(kHpsiTable2);
       if (mode >= 3) cand.push_back(kHpsiTable2w);
+      // (the copy-engine gather, kHpsiTableBulk, is not a candidate: 3.3x
+      // slower on the 4x4 K = 8 panel; LGT_HPSI_VARIANT=8 forces it)
     }
   }
   EventPair evp;

@@ -40,7 +40,16 @@ struct HpsiArgs {
   // the panels are in the table's own row order (a renumbered table): only
   // the table kernel may run; anything else is an error, not a fallback
   int table_order = 0;
+  // rows addressable from x (all the Krylov slots behind x + xsel * xstride;
+  // 0: N): the extent of the tensor map of the gathered variant (vpl 4)
+  int64_t x_rows = 0;
 };
+
+// The stored-table kernel with the neighbour rows gathered by the copy
+// engine (nbr_table_bulk.cu): FP32 panels of 16 columns.
+bool table_bulk_applies(const HpsiArgs<float>& a, int64_t x_rows);
+cudaError_t launch_table_bulk(const HpsiArgs<float>& a, uint32_t model, int64_t x_rows,
+                              cudaStream_t s);
 
 // The neighbour ranks of every row of a basis for one model, kept in HBM
 // (nbr_table.cu): meta[N], tile_off[ceil(N/32) + 1], nbr[nnz].

@@ -55,6 +55,7 @@ enum HpsiVariant : int {
   kHpsiTable1 = 5,    // stored neighbour table, one 16-byte vector per lane
   kHpsiTable2 = 6,    // stored neighbour table, two 16-byte vectors per lane
   kHpsiTable2w = 7,   // stored neighbour table, one 32-byte access per lane
+  kHpsiTableBulk = 8, // stored neighbour table, rows gathered by the copy engine
 };
 struct TuneChoice {
   int hpsi_variant = kHpsiDefault;

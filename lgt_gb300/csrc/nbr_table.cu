@@ -215,6 +215,12 @@ cudaError_t launch_table_v(const HpsiArgs<T>& a, cudaStream_t s) {
 
 template <typename T, bool PLAQ, bool JW>
 cudaError_t launch_table_m(const HpsiArgs<T>& a, cudaStream_t s) {
+  if constexpr (sizeof(T) == 4) {
+    // the gathered variant where it applies, else the widest load mode
+    const int64_t rows = a.x_rows > 0 ? a.x_rows : a.N;
+    if (a.vpl == 4 && table_bulk_applies(a, rows))
+      return launch_table_bulk(a, (PLAQ ? kModelPlaq : 0u) | (JW ? kModelJW : 0u), rows, s);
+  }
   int mode = 0;
   table_load_mode(a, &mode);
   const int want = a.vpl == 0 ? 2 : a.vpl;

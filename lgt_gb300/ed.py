@@ -38,7 +38,7 @@ _PREC = {"fp64": C.LGT_FP64, "fp32": C.LGT_FP32, "fp32_mixed": C.LGT_FP32_MIXED,
          "mixed": C.LGT_FP32_MIXED}
 # lgt_tuning.hpsi_kernel codes (include/lgt_ed.h)
 HPSI_KERNELS = {0: "rule", 1: "generic", 2: "fixed_vpl1", 3: "fixed_vpl2", 4: "fixed_wide",
-                5: "table_vpl1", 6: "table_vpl2", 7: "table_wide"}
+                5: "table_vpl1", 6: "table_vpl2", 7: "table_wide", 8: "table_gather"}
 
 
 def _p(a):

@@ -159,7 +159,7 @@ end
 
 "Names of the `hpsi_kernel` codes of `Tuning` (index = code + 1; include/lgt_ed.h)."
 const HPSI_KERNELS = ("rule", "generic", "fixed_vpl1", "fixed_vpl2", "fixed_wide",
-                      "table_vpl1", "table_vpl2", "table_wide")
+                      "table_vpl1", "table_vpl2", "table_wide", "table_gather")
 
 function autotune(H::Hamiltonian; ncomp::Integer=1, precision::Int32=LGT_FP64)
     t = Ref{Tuning}()

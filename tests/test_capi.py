@@ -22,16 +22,16 @@ def test_header_lists_the_python_binding():
 
 
 def test_hpsi_kernel_names_agree_across_bindings():
-    """lgt_tuning.hpsi_kernel codes 0..7: the Python and Julia name lists
+    """lgt_tuning.hpsi_kernel codes 0..8: the Python and Julia name lists
     cover the codes the header documents, in the same order."""
     import lgt_gb300 as lgt
     hdr = open(os.path.join(ROOT, "include", "lgt_ed.h")).read()
     doc = hdr[hdr.index("int32_t hpsi_kernel;"):hdr.index("int32_t reduce_blocks;")]
-    assert "0 built-in rule" in doc and "5, 6, 7" in doc
-    assert sorted(lgt.HPSI_KERNELS) == list(range(8))
+    assert "0 built-in rule" in doc and "5, 6, 7" in doc and "8 the stored table" in doc
+    assert sorted(lgt.HPSI_KERNELS) == list(range(9))
     jl = open(os.path.join(ROOT, "lgt_gb300", "julia", "LGTED.jl")).read()
     names = re.search(r"HPSI_KERNELS = \(([^)]*)\)", jl, re.S).group(1)
-    assert re.findall(r'"([a-z_0-9]+)"', names) == [lgt.HPSI_KERNELS[i] for i in range(8)]
+    assert re.findall(r'"([a-z_0-9]+)"', names) == [lgt.HPSI_KERNELS[i] for i in range(9)]
 
 
 def test_library_exports_every_declared_symbol():

@@ -60,3 +60,24 @@ def test_bulk_update_ground_state_bitwise(oracle, lgt, monkeypatch, K):
     Ho = oracle.build_hamiltonian(ob, g=gs[0], t=1.0, m=0.5, model="pjw")
     E0o, _ = oracle.ground_state(Ho)
     assert abs(ea[0] - E0o) <= 1e-10 * abs(E0o)
+
+
+def test_gathered_hpsi_quench(lgt, monkeypatch):
+    """The stored-table H*psi with the copy engine gathering the neighbour
+    rows (LGT_HPSI_VARIANT=8) inside the FP32-mixed Krylov drivers (the
+    panel picked by a device-resident slot index, the table in its
+    renumbered row order) against the lane-gathering table kernel (7): the
+    same sums in the same order."""
+    b = lgt.build_basis(4, 3, 1, lgt.staggered_charges(4, 3))[0]
+    gs = np.linspace(0.6, 1.5, 8)
+    v0 = lgt.staggered_product_state(b)
+    p0 = np.repeat(v0[:, None], 8, axis=1)
+    out = {}
+    for var in ("8", "7"):
+        monkeypatch.setenv("LGT_HPSI_VARIANT", var)
+        H = lgt.build_hamiltonian(b, g=gs, t=1.0, m=0.5)
+        data, psi, drift = lgt.evolve_ED(p0, H, dt=0.05, n_steps=3, tol=1e-12,
+                                         precision="fp32_mixed", return_state=True)
+        H.close()
+        out[var] = psi
+    assert np.max(np.abs(out["8"] - out["7"])) <= 1e-12

@@ -3,7 +3,8 @@
 The table is built once per Hamiltonian by the run-time-geometry move
 enumeration (any shape, any dg); its kernel gathers with the fixed-shape
 kernel's load modes (LGT_HPSI_VARIANT=5, 6, 7: one or two 16-byte vectors
-per lane, two as one 32-byte access).  Bars: 1e-12 relative to max |y|
+per lane, two as one 32-byte access), or has the copy engine gather the
+neighbour rows (8: FP32 panels of 16 columns; other panels fall back to 7).  Bars: 1e-12 relative to max |y|
 (FP64) and 2e-6 (FP32) against the FP64 oracle's CSR matrix (reference and
 plaquette+JW models), against the run-time-geometry kernel for the JW-only
 and plaquette-only models and on the 4x4 lattice; ground states within
@@ -21,7 +22,8 @@ COUPLINGS = [(1.0, 1.0, 0.5), (0.8, 1.3, 0.3), (2.0, 0.7, -1.1), (0.55, 1.0, 0.9
 CASES = [(3, 2, 1, "stag"), (2, 3, 1, "zero"), (4, 2, 1, "string"), (3, 3, 1, "stag"),
          (4, 3, 1, "stag"), (3, 4, 1, "string"), (2, 2, 2, "stag"), (3, 2, 2, "stag"),
          (1, 4, 1, "stag"), (4, 1, 1, "stag")]
-WIDTHS = {"fp64": [(1, True), (2, True), (4, False)], "fp32": [(2, True), (4, True), (8, False)]}
+WIDTHS = {"fp64": [(1, True), (2, True), (4, False)],
+          "fp32": [(2, True), (4, True), (8, False), (8, True), (16, False)]}
 
 _cache = {}
 
@@ -53,7 +55,7 @@ def _tol(prec):
     return 1e-12 if prec == "fp64" else 2e-6
 
 
-@pytest.mark.parametrize("variant", ["5", "6", "7"])
+@pytest.mark.parametrize("variant", ["5", "6", "7", "8"])
 @pytest.mark.parametrize("model", ["ref", "jw", "plaq", "pjw"])
 @pytest.mark.parametrize("nx,ny,dg,kind", CASES)
 def test_table_vs_oracle(oracle, lgt, nx, ny, dg, kind, model, variant, monkeypatch):
@@ -63,7 +65,8 @@ def test_table_vs_oracle(oracle, lgt, nx, ny, dg, kind, model, variant, monkeypa
     Hos = {}
     for prec in ("fp64", "fp32"):
         for K, cplx in WIDTHS[prec]:
-            gs, ts, ms = (np.array(v) for v in zip(*COUPLINGS[:K]))
+            cpl = (COUPLINGS * 2)[:K]  # 16 real columns: the couplings twice
+            gs, ts, ms = (np.array(v) for v in zip(*cpl))
             H = lgt.build_hamiltonian(gb, g=gs, t=ts, m=ms, model=model)
             x = _panel(rng, ob.dim, K, cplx, prec)
             y = H.matvec(x, precision=prec)
@@ -74,26 +77,28 @@ def test_table_vs_oracle(oracle, lgt, nx, ny, dg, kind, model, variant, monkeypa
                 H.close()
                 continue
             for k in range(K):
-                if k not in Hos:
-                    g, t, m = COUPLINGS[k]
-                    Hos[k] = oracle.build_hamiltonian(ob, g=g, t=t, m=m, model=model)
-                yo = Hos[k] @ x[:, k].astype(np.complex128 if cplx else np.float64)
+                kc = k % len(COUPLINGS)
+                if kc not in Hos:
+                    g, t, m = COUPLINGS[kc]
+                    Hos[kc] = oracle.build_hamiltonian(ob, g=g, t=t, m=m, model=model)
+                yo = Hos[kc] @ x[:, k].astype(np.complex128 if cplx else np.float64)
                 err = np.max(np.abs(y[:, k] - yo))
                 assert err <= _tol(prec) * max(1.0, np.max(np.abs(yo))), (prec, K, cplx, k, err)
             H.close()
 
 
-@pytest.mark.parametrize("variant", ["6", "7"])
+@pytest.mark.parametrize("variant,K", [("6", 4), ("7", 4), ("8", 8)])
 @pytest.mark.parametrize("model", ["ref", "pjw"])
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
-def test_table_4x4_vs_generic(lgt, model, prec, variant, monkeypatch):
-    """4x4 staggered sector (N = 8,563,545), K = 4 complex."""
+def test_table_4x4_vs_generic(lgt, model, prec, variant, K, monkeypatch):
+    """4x4 staggered sector (N = 8,563,545), K = 4 or 8 complex (8: the
+    gathered kernel's panel width)."""
     monkeypatch.setenv("LGT_HPSI_VARIANT", variant)
     st, _ = lgt.build_basis(4, 4, 1, lgt.staggered_charges(4, 4))
     rng = np.random.default_rng(45)
-    gs, ts, ms = (np.array(v) for v in zip(*COUPLINGS[:4]))
+    gs, ts, ms = (np.array(v) for v in zip(*COUPLINGS[:K]))
     H = lgt.build_hamiltonian(st, g=gs, t=ts, m=ms, model=model)
-    x = _panel(rng, len(st), 4, True, prec)
+    x = _panel(rng, len(st), K, True, prec)
     y = H.matvec(x, precision=prec)
     yg = H.matvec(x, precision=prec, generic=True)
     assert np.max(np.abs(y - yg)) <= _tol(prec) * max(1.0, float(np.max(np.abs(yg))))
