@@ -925,6 +925,46 @@ __global__ void k_scale(const SI* src, SO* dstbase, size_t vstride, const int* j
   }
 }
 
+// k_scale for FP32 panels whose width is a multiple of 4 (no gather): a
+// thread keeps four consecutive columns (the grid's thread count is a
+// multiple of C / 4, so the columns stay put) and moves 16 bytes per access;
+// columns of points not in state `sel` keep their values.
+__global__ void __launch_bounds__(kT) k_scale_f4(const float* __restrict__ src, float* dstbase,
+                                                 size_t vstride, const int* jstate, int dst_off,
+                                                 int64_t N, int C, int ncomp,
+                                                 const double* bnorm, const int* status, int sel) {
+  float* dst = dstbase + size_t((jstate ? *jstate : 0) + dst_off) * vstride;
+  const int C4 = C / 4;
+  const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t nthr = int64_t(gridDim.x) * blockDim.x;
+  const int c0 = int(tid % C4) * 4;
+  float inv[4];
+  bool on[4];
+  bool all = true;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const int k = (c0 + e) / ncomp;
+    on[e] = !status || status[k] == sel;
+    const double b = bnorm[k];
+    inv[e] = float((b > 0.0) ? 1.0 / b : 0.0);
+    all = all && on[e];
+  }
+  const int64_t n4 = N * C4;
+  for (int64_t i = tid; i < n4; i += nthr) {
+    const float4 v = reinterpret_cast<const float4*>(src)[i];
+    const float4 o = make_float4(v.x * inv[0], v.y * inv[1], v.z * inv[2], v.w * inv[3]);
+    if (all) {
+      reinterpret_cast<float4*>(dst)[i] = o;
+    } else {
+      float* d = dst + 4 * i;
+      if (on[0]) d[0] = o.x;
+      if (on[1]) d[1] = o.y;
+      if (on[2]) d[2] = o.z;
+      if (on[3]) d[3] = o.w;
+    }
+  }
+}
+
 __global__ void k_advance(int* jstate) { jstate[0] += 1; }
 
 __global__ void k_set_int(int* p, int n, int v, const int* status, int only_status) {
@@ -1621,9 +1661,22 @@ cudaError_t lanczos_step(const OpDev& op, Work<S>& w, int reorth, double tiny_re
   k_finish_norm<<<finish_blocks(w.K), 128, 0, s>>>(w.npart, w.red.nblk, w.K, w.C, w.ncomp, w.jstate,
                                                w.beta, w.alpha, w.ldT, w.status, w.len, w.bnorm,
                                                tiny_rel, 1), lgt::note_launch();
-  k_scale<S, S><<<grid_for(int64_t(w.vstride)), kT, 0, s>>>(w.W, w.V, w.vstride, w.jstate, 1, w.N,
-                                                            w.C, w.ncomp, w.bnorm, w.status,
-                                                            kActive, nullptr), lgt::note_launch();
+  bool f4 = false;
+  if constexpr (sizeof(S) == 4) {
+    // 16-byte accesses when the panel allows (the grid a multiple of C / 4
+    // threads, so that every thread keeps its columns)
+    f4 = w.C % 4 == 0 && (kT % (w.C / 4)) == 0 && (w.vstride % 4) == 0 &&
+         (reinterpret_cast<uintptr_t>(w.V) & 15) == 0 && (reinterpret_cast<uintptr_t>(w.W) & 15) == 0;
+    if (f4)
+      k_scale_f4<<<grid_for(int64_t(w.vstride) / 4), kT, 0, s>>>(
+          reinterpret_cast<const float*>(w.W), reinterpret_cast<float*>(w.V), w.vstride, w.jstate,
+          1, w.N, w.C, w.ncomp, w.bnorm, w.status, kActive), lgt::note_launch();
+  }
+  if (!f4)
+    k_scale<S, S><<<grid_for(int64_t(w.vstride)), kT, 0, s>>>(w.W, w.V, w.vstride, w.jstate, 1,
+                                                              w.N, w.C, w.ncomp, w.bnorm,
+                                                              w.status, kActive, nullptr),
+        lgt::note_launch();
   k_advance<<<1, 1, 0, s>>>(w.jstate), lgt::note_launch();
   return cudaGetLastError();
 }

@@ -108,40 +108,96 @@ __device__ inline double warp_lowest_eig(const double* a, const double* b, int n
     }
   }
   const double theta = 0.5 * (lo + hi);
-  if (lane == 0) {
-    const double shift = theta - 4.0 * 2.2e-16 * scale;
-    double* d = work;  // reciprocal pivots
-    double* l = work + kTriMax;
-    if (!warm_z)
-      for (int i = 0; i < n; ++i) z[i] = 1.0;
-    const int reps = warm_z ? 1 : 2;
-    for (int rep = 0; rep < reps; ++rep) {
-      double piv = a[0] - shift;
-      if (piv <= 0.0) piv = 1e-300;
-      d[0] = 1.0 / piv;
-      for (int i = 1; i < n; ++i) {
-        l[i - 1] = b[i - 1] * d[i - 1];
-        piv = (a[i] - shift) - l[i - 1] * b[i - 1];
-        if (piv <= 0.0) piv = 1e-300;
-        d[i] = 1.0 / piv;
+  // inverse iteration on the positive-definite T - (theta - delta) I: the
+  // two triangular sweeps by lane 0 (factorisation merged into the forward
+  // sweep, diagonal scaling into the backward one), operands read eight
+  // entries ahead; the scaling by the whole warp
+  const double shift = theta - 4.0 * 2.2e-16 * scale;
+  double* d = work;  // reciprocal pivots
+  double* l = work + kTriMax;
+  if (!warm_z)
+    for (int i = lane; i < n; i += 32) z[i] = 1.0;
+  __syncwarp();
+  const int reps = warm_z ? 1 : 2;
+  for (int rep = 0; rep < reps; ++rep) {
+    if (lane == 0) {
+      double dprev = 0.0, bprev = 0.0, zprev = 0.0;
+      for (int i0 = 0; i0 < n; i0 += 8) {
+        double ac[8], bc[8], zc[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int i = i0 + u;
+          ac[u] = (i < n) ? a[i] : 0.0;
+          bc[u] = (i < n - 1) ? b[i] : 0.0;
+          zc[u] = (i < n) ? z[i] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int i = i0 + u;
+          if (i < n) {
+            double piv;
+            if (i == 0) {
+              piv = ac[u] - shift;
+            } else {
+              const double li = bprev * dprev;
+              l[i - 1] = li;
+              piv = (ac[u] - shift) - li * bprev;
+              zc[u] = fma(-li, zprev, zc[u]);
+            }
+            if (piv <= 0.0) piv = 1e-300;
+            const double di = 1.0 / piv;
+            d[i] = di;
+            z[i] = zc[u];
+            dprev = di;
+            bprev = bc[u];
+            zprev = zc[u];
+          }
+        }
       }
-      for (int i = 1; i < n; ++i) z[i] = fma(-l[i - 1], z[i - 1], z[i]);
-      for (int i = 0; i < n; ++i) z[i] *= d[i];
-      for (int i = n - 2; i >= 0; --i) z[i] = fma(-l[i], z[i + 1], z[i]);
-      double mx = 0.0;
-      for (int i = 0; i < n; ++i) mx = fmax(mx, fabs(z[i]));
-      const double inv = 1.0 / mx;
-      double nn = 0.0;
-      for (int i = 0; i < n; ++i) {
-        z[i] *= inv;
-        nn = fma(z[i], z[i], nn);
+      double znext = 0.0;
+      for (int i1 = n - 1; i1 >= 0; i1 -= 8) {
+        double zc[8], dc[8], lc[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int i = i1 - u;
+          zc[u] = (i >= 0) ? z[i] : 0.0;
+          dc[u] = (i >= 0) ? d[i] : 0.0;
+          lc[u] = (i >= 0 && i < n - 1) ? l[i] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int i = i1 - u;
+          if (i >= 0) {
+            double t = zc[u] * dc[u];
+            if (i < n - 1) t = fma(-lc[u], znext, t);
+            z[i] = t;
+            znext = t;
+          }
+        }
       }
-      const double in2 = 1.0 / sqrt(nn);
-      for (int i = 0; i < n; ++i) z[i] *= in2;
     }
-    if (z[0] < 0.0)
-      for (int i = 0; i < n; ++i) z[i] = -z[i];
+    __syncwarp();
+    double mx = 0.0;
+    for (int i = lane; i < n; i += 32) mx = fmax(mx, fabs(z[i]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    const double inv = 1.0 / mx;
+    double nn = 0.0;
+    for (int i = lane; i < n; i += 32) {
+      const double zi = z[i] * inv;
+      z[i] = zi;
+      nn = fma(zi, zi, nn);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nn += __shfl_xor_sync(0xffffffffu, nn, o);
+    const double in2 = 1.0 / sqrt(nn);
+    for (int i = lane; i < n; i += 32) z[i] *= in2;
+    __syncwarp();
   }
+  const bool neg = z[0] < 0.0;
+  __syncwarp();
+  if (neg)
+    for (int i = lane; i < n; i += 32) z[i] = -z[i];
   __syncwarp();
   return theta;
 }
