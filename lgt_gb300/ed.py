@@ -42,7 +42,9 @@ HPSI_KERNELS = {0: "rule", 1: "generic", 2: "fixed_vpl1", 3: "fixed_vpl2", 4: "f
 
 
 def _p(a):
-    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+    """Data address of a host array for a ``c_void_p`` argument (the caller
+    holds the array across the call)."""
+    return a.ctypes.data if a is not None else None
 
 
 # ---------------------------------------------------------------------------
@@ -452,7 +454,7 @@ def find_ground_state(H: Hamiltonian, *, tol=1e-10, krylovdim=50, maxiter=300, p
     N, K = H.basis.dim, H.K
     o = _opts(False, tol, krylovdim, maxiter, precision, seed, check_every, refine_steps,
               use_graph, v0 is not None, solver=solver)
-    psi = np.zeros((N, K), np.float64)
+    psi = np.empty((N, K), np.float64)  # written whole by the solver
     if v0 is not None:
         v = np.asarray(v0)
         psi[:] = np.real(v).reshape(N, K) if v.ndim == 1 else np.real(v)
@@ -537,10 +539,9 @@ def _obs_dicts(basis, K, nf, e2, pl, summ):
     pnx, pny = max(nx - 1, 0), max(ny - 1, 0)
     pl_g = list(pl[:K * pnx * pny].reshape(K, pny, pnx).transpose(0, 2, 1).copy())
     sm = np.frombuffer(summ, dtype=np.float64).reshape(K, len(_OBS_FIELDS)).tolist()
-    return [{"t": r[0], "nf_mean": r[1], "nf_even": r[2], "nf_odd": r[3], "E2_mean": r[4],
-             "plaq_mean": r[5], "n_stag": r[6], "norm2": r[7],
-             "nf_grid": a, "E2_grid": b, "plaq_grid": c}
-            for r, a, b, c in zip(sm, nf_g, e2_g, pl_g)]
+    return [{"t": t, "nf_mean": n0, "nf_even": n1, "nf_odd": n2, "E2_mean": e, "plaq_mean": w,
+             "n_stag": ns, "norm2": nn, "nf_grid": a, "E2_grid": b, "plaq_grid": c}
+            for (t, n0, n1, n2, e, w, ns, nn), a, b, c in zip(sm, nf_g, e2_g, pl_g)]
 
 
 def measure_ED(psi, states: Basis, nx=None, ny=None, dg=None, t_now: float = 0.0):
