@@ -15,6 +15,7 @@
 // warps, device-wide exclusive scan over blocks) emits the order keys already
 // sorted.  No sort and no hash table are needed.
 #include <cstdio>
+#include <cstdlib>
 #include <string>
 
 #include "lgt_internal.h"
@@ -179,22 +180,26 @@ __global__ void __launch_bounds__(1024) k_scan_counts(const uint32_t* counts, in
   if (threadIdx.x == 0) offsets[n] = carry;
 }
 
-// segc[r] = first index of the segment of mask r (lower bound of mask<<ushift)
-__global__ void k_segments(const uint64_t* keys, int64_t dim, const uint32_t* masks, int nmasks,
-                           int ushift, uint32_t* segc) {
-  int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r > nmasks) return;
-  if (r == nmasks) {
-    segc[r] = uint32_t(dim);
-    return;
-  }
+// segc[r] = first index of the segment of mask r (lower bound of mask<<ushift);
+// segc[nmasks] = dim
+__device__ __forceinline__ uint32_t segment_start(const uint64_t* keys, int64_t dim,
+                                                  const uint32_t* masks, int nmasks, int ushift,
+                                                  int r) {
+  if (r == nmasks) return uint32_t(dim);
   const uint64_t t = uint64_t(masks[r]) << ushift;
   int64_t lo = 0, hi = dim;
   while (lo < hi) {
     int64_t mid = (lo + hi) >> 1;
     if (keys[mid] < t) lo = mid + 1; else hi = mid;
   }
-  segc[r] = uint32_t(lo);
+  return uint32_t(lo);
+}
+
+__global__ void k_segments(const uint64_t* keys, int64_t dim, const uint32_t* masks, int nmasks,
+                           int ushift, uint32_t* segc) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r > nmasks) return;
+  segc[r] = segment_start(keys, dim, masks, nmasks, ushift, r);
 }
 
 __global__ void k_low_parts(const uint64_t* keys, int64_t dim, int ushift, uint32_t* low) {
@@ -202,16 +207,18 @@ __global__ void k_low_parts(const uint64_t* keys, int64_t dim, int ushift, uint3
   if (i < dim) low[i] = uint32_t(keys[i] & ((1ull << ushift) - 1));
 }
 
-__global__ void k_binom(uint32_t* binom) {
-  int p = threadIdx.x;  // 0..31
-  if (p >= 32) return;
-  // C(p, j) for j = 0..32
+// C(p, j) for j = 0..32 into binom[p * 33 + j] (p < 32)
+__device__ __forceinline__ void binom_column(uint32_t* binom, int p) {
   uint64_t c = 1;
   for (int j = 0; j <= 32; ++j) {
     binom[p * 33 + j] = (j <= p) ? uint32_t(c) : 0u;
     if (j < p) c = c * uint64_t(p - j) / uint64_t(j + 1);
     else c = 0;
   }
+}
+
+__global__ void k_binom(uint32_t* binom) {
+  if (threadIdx.x < 32) binom_column(binom, threadIdx.x);
 }
 
 __global__ void k_decode_states(Geom G, const uint64_t* keys, int64_t i0, int64_t n, int8_t* nf,
@@ -310,9 +317,7 @@ __device__ __forceinline__ bool eR_row_ok(int nx, int dg, uint32_t rowbits, cons
 
 // Cnt_{ny-1}(u_{ny-2}): the last e_R row, for every bit pattern m of the last
 // site row and every free index fp of u_{ny-2}.
-__global__ void k_tab_last(Geom G, int F, uint32_t* L) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (1 << G.nx) * F) return;
+__device__ __forceinline__ void tab_last_at(const Geom& G, int F, uint32_t* L, int idx) {
   const uint32_t m = uint32_t(idx / F), fp = uint32_t(idx % F);
   const int r = G.ny - 1;
   const int Rl = __popc(m) + G.grow[r];
@@ -321,13 +326,16 @@ __global__ void k_tab_last(Geom G, int F, uint32_t* L) {
   L[idx] = (okp && eR_row_ok(G.nx, G.dg, m, G.gq + r * G.nx, nullptr, up)) ? 1u : 0u;
 }
 
+__global__ void k_tab_last(Geom G, int F, uint32_t* L) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < (1 << G.nx) * F) tab_last_at(G, F, L, idx);
+}
+
 // T_r for e_U row r (0 <= r <= ny-2): m = site rows >= r (nx*(ny-r) bits),
 // fp = free index of u_{r-1} (Fp = 1 for r = 0).  `next` is Cnt_{r+1}:
 // L when r = ny-2, else T_{r+1} (its entry [F]).
-__global__ void k_tab_row(Geom G, int F, int r, const uint32_t* next, int next_is_last,
-                          uint32_t* T, int Fp, int64_t nm) {
-  const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (idx >= nm * Fp) return;
+__device__ __forceinline__ void tab_row_at(const Geom& G, int F, int r, const uint32_t* next,
+                                           int next_is_last, uint32_t* T, int Fp, int64_t idx) {
   const uint32_t m = uint32_t(idx / Fp), fp = uint32_t(idx % Fp);
   const int B = 2 * G.dg + 1;
   const uint32_t rowmask = (1u << G.nx) - 1u;
@@ -348,6 +356,12 @@ __global__ void k_tab_row(Geom G, int F, int r, const uint32_t* next, int next_i
   out[F] = run;
 }
 
+__global__ void k_tab_row(Geom G, int F, int r, const uint32_t* next, int next_is_last,
+                          uint32_t* T, int Fp, int64_t nm) {
+  const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx < nm * Fp) tab_row_at(G, F, r, next, next_is_last, T, Fp, idx);
+}
+
 // T_0 += segc of the mask's segment (masks with the sector's particle number)
 __global__ void k_tab_seg(Geom G, const uint32_t* masks, const uint32_t* segc, int nmasks, int F,
                           uint32_t* T0) {
@@ -358,15 +372,126 @@ __global__ void k_tab_seg(Geom G, const uint32_t* masks, const uint32_t* segc, i
 }
 
 // every basis key must rank to its own index through the tables
-__global__ void k_tab_check(RankView R, int* bad) {
-  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= R.dim) return;
+__device__ __forceinline__ bool tab_ranks_own_index(const RankView& R, int64_t i) {
   const uint64_t key = R.keys[i];
   const uint64_t digits = key & ((1ull << R.ushift) - 1);
   uint32_t f[kMaxTabRows];
 #pragma unroll
   for (int r = 0; r < kMaxTabRows; ++r) f[r] = (r < R.nrows) ? row_index(R, digits, r) : 0u;
-  if (rank_rows(R, uint32_t(key >> R.ushift), f, -1, 0) != i) atomicOr(bad, 1);
+  return rank_rows(R, uint32_t(key >> R.ushift), f, -1, 0) == i;
+}
+
+__global__ void k_tab_check(RankView R, int* bad) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < R.dim && !tab_ranks_own_index(R, i)) atomicOr(bad, 1);
+}
+
+// ---- small sectors in one launch -------------------------------------------
+//
+// For a candidate space of at most kFusedMaxCandidates and tables of at most
+// kFusedMaxTable entries, one block builds the whole basis: binomials, the
+// masks and the order keys by the same ordered compaction (tile by tile of
+// the block, warp ballots and a prefix over the warps), the segment starts
+// and low parts, the rank tables row by row and their self-check, with block
+// barriers between the phases.  The host then waits once, for the sector
+// dimension and the check, instead of a dozen launches and two read-backs.
+constexpr int kFusedThreads = 1024;
+constexpr uint64_t kFusedMaxCandidates = uint64_t(1) << 15;
+constexpr int64_t kFusedMaxTable = int64_t(1) << 16;
+
+struct FusedBasisArgs {
+  Geom G;
+  RankView R;        // tables and geometry (its dim is an upper bound)
+  uint32_t* binom;
+  uint32_t* masks;
+  uint64_t* keys;
+  uint32_t* low;     // null when the e_U part exceeds 32 bits
+  uint32_t* segc;
+  uint32_t* tab;     // null: no tables
+  uint32_t* L;       // the last e_U row's counts (tables only)
+  int64_t* out;      // [0] sector dimension, [1] tables failed their check
+  int* err;
+  int nmasks;        // C(ns, N_f)
+  uint64_t nfree;    // free e_U strings per mask
+  uint64_t cap;      // nmasks * nfree: room for every candidate
+  int F;
+  int64_t nlast;
+};
+
+// In-order compaction of p's candidates by one block; returns the count.
+template <class Pred, class Out>
+__device__ uint64_t block_compact(const Pred& p, Out* out, uint64_t cap, int* err,
+                                  uint32_t* warp_cnt) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  uint64_t running = 0;
+  for (uint64_t base = 0; base < p.total; base += blockDim.x) {
+    const uint64_t idx = base + threadIdx.x;
+    uint64_t v = 0;
+    const bool ok = idx < p.total && p(idx, &v);
+    const uint32_t bal = __ballot_sync(0xffffffffu, ok);
+    if (lane == 0) warp_cnt[wid] = __popc(bal);
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+    for (int w = 0; w < nw; ++w) {
+      const uint32_t c = warp_cnt[w];
+      before += (w < wid) ? c : 0u;
+      total += c;
+    }
+    if (ok) {
+      const uint64_t at = running + before + __popc(bal & ((1u << lane) - 1u));
+      if (at < cap) out[at] = Out(v);
+      else raise_err(err, kDevErrBounds);
+    }
+    running += total;
+    __syncthreads();  // warp_cnt reused; this tile's writes visible to the block
+  }
+  return running;
+}
+
+template <int DG>
+__global__ void __launch_bounds__(kFusedThreads) k_basis_fused(FusedBasisArgs a) {
+  __shared__ uint32_t warp_cnt[kFusedThreads / 32];
+  __shared__ int s_bad;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  if (tid < 32) binom_column(a.binom, tid);
+  if (tid == 0) s_bad = 0;
+  const int nmasks = a.nmasks;
+  block_compact(MaskPred{a.G.nf_target, uint64_t(1) << a.G.ns}, a.masks, uint64_t(nmasks), a.err,
+                warp_cnt);
+  const CandPred<DG> cp{a.G, a.masks, a.nfree, uint64_t(nmasks) * a.nfree};
+  const int64_t dim = int64_t(block_compact(cp, a.keys, a.cap, a.err, warp_cnt));
+  for (int r = tid; r <= nmasks; r += nt)
+    a.segc[r] = segment_start(a.keys, dim, a.masks, nmasks, a.G.ushift, r);
+  if (a.low)
+    for (int64_t i = tid; i < dim; i += nt)
+      a.low[i] = uint32_t(a.keys[i] & ((1ull << a.G.ushift) - 1));
+  if (a.tab) {
+    const int F = a.F, nrows = a.G.ny - 1;
+    for (int64_t idx = tid; idx < a.nlast * F; idx += nt) tab_last_at(a.G, F, a.L, int(idx));
+    __syncthreads();
+    for (int r = nrows - 1; r >= 0; --r) {
+      const int64_t nm = int64_t(1) << (a.G.nx * (a.G.ny - r));
+      const int Fp = (r == 0) ? 1 : F;
+      const uint32_t* next = (r == nrows - 1) ? a.L : a.tab + a.R.tab_off[r + 1];
+      for (int64_t idx = tid; idx < nm * Fp; idx += nt)
+        tab_row_at(a.G, F, r, next, r == nrows - 1, a.tab + a.R.tab_off[r], Fp, idx);
+      __syncthreads();
+    }
+    // T_0 += segc of the mask's segment (segc was written before the
+    // barriers above)
+    for (int64_t idx = tid; idx < int64_t(nmasks) * (F + 1); idx += nt) {
+      const int cr = int(idx / (F + 1)), v = int(idx % (F + 1));
+      a.tab[uint64_t(a.masks[cr]) * (F + 1) + v] += a.segc[cr];
+    }
+    __syncthreads();
+    for (int64_t i = tid; i < dim; i += nt)
+      if (!tab_ranks_own_index(a.R, i)) s_bad = 1;
+    __syncthreads();
+  }
+  if (tid == 0) {
+    a.out[0] = dim;
+    a.out[1] = s_bad;
+  }
 }
 
 #define CK(call)                                                                 \
@@ -486,26 +611,40 @@ std::string make_geom(int nx, int ny, int dg, const int32_t* g, Geom* Gp) {
   return std::string();
 }
 
-// Builds the row-count rank tables when they fit (at most 2^25 entries) and
-// keeps them only if every basis key ranks to its own index through them.
-std::string build_rank_tables(BasisDev* B) {
-  const Geom& G = B->G;
-  cudaStream_t s = B->stream;
+// Layout of the row-count rank tables: F strings per row, the start of each
+// row's table, the entries of all of them and of the last row's counts.
+// False when the tables do not apply or exceed 2^25 entries.
+bool tab_plan(const Geom& G, int* Fo, int64_t* off, int64_t* toto, int64_t* nlasto) {
   const int nrows = G.ny - 1;
-  if (B->dim == 0 || nrows < 1 || nrows > kMaxTabRows || G.nx < 2) return std::string();
+  if (nrows < 1 || nrows > kMaxTabRows || G.nx < 2) return false;
   const int Bd = 2 * G.dg + 1;
   long double Fl = 1;
   for (int i = 0; i < G.nx - 1; ++i) Fl *= Bd;
-  if (Fl > 4096) return std::string();
+  if (Fl > 4096) return false;
   const int F = int(Fl);
-  int64_t off[kMaxTabRows] = {};
+  for (int r = 0; r < kMaxTabRows; ++r) off[r] = 0;
   long double tot = (long double)(1ull << G.ns) * (F + 1);
   for (int r = 1; r < nrows; ++r) {
     off[r] = int64_t(tot);
     tot += (long double)(1ull << (G.nx * (G.ny - r))) * F * (F + 1);
   }
   const int64_t nlast = int64_t(1) << G.nx;
-  if (tot + nlast * F > (long double)(int64_t(1) << 25)) return std::string();
+  if (tot + nlast * F > (long double)(int64_t(1) << 25)) return false;
+  *Fo = F;
+  *toto = int64_t(tot);
+  *nlasto = nlast;
+  return true;
+}
+
+// Builds the row-count rank tables when they fit (at most 2^25 entries) and
+// keeps them only if every basis key ranks to its own index through them.
+std::string build_rank_tables(BasisDev* B) {
+  const Geom& G = B->G;
+  cudaStream_t s = B->stream;
+  const int nrows = G.ny - 1;
+  int F = 0;
+  int64_t off[kMaxTabRows], tot = 0, nlast = 0;
+  if (B->dim == 0 || !tab_plan(G, &F, off, &tot, &nlast)) return std::string();
   uint32_t* tab = nullptr;
   uint32_t* L = nullptr;
   int* bad = nullptr;
@@ -542,9 +681,112 @@ std::string build_rank_tables(BasisDev* B) {
   return std::string();
 }
 
+// The whole basis of a small sector from one launch of k_basis_fused, its
+// buffers carved from one pool allocation (BasisDev::block).
+std::string build_basis_fused(BasisDev* B, int nmasks, uint64_t nfree) {
+  const Geom& G = B->G;
+  cudaStream_t s = B->stream;
+  const uint64_t cap = uint64_t(nmasks) * nfree;
+  int F = 0;
+  int64_t off[kMaxTabRows] = {}, tot = 0, nlast = 0;
+  const bool tabs = tab_plan(G, &F, off, &tot, &nlast) && tot + nlast * F <= kFusedMaxTable;
+  size_t at = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = at;
+    at += (bytes + 255) & ~size_t(255);
+    return o;
+  };
+  const size_t o_hdr = take(64);  // error word at 0, dimension and check flag at 16
+  const size_t o_binom = take(32 * 33 * sizeof(uint32_t));
+  const size_t o_masks = take(size_t(nmasks) * sizeof(uint32_t));
+  const size_t o_keys = take(cap * sizeof(uint64_t));
+  const size_t o_low = (G.ushift <= 32) ? take(cap * sizeof(uint32_t)) : 0;
+  const size_t o_segc = take((size_t(nmasks) + 1) * sizeof(uint32_t));
+  const size_t o_tab = tabs ? take(size_t(tot) * sizeof(uint32_t)) : 0;
+  const size_t o_L = tabs ? take(size_t(nlast) * F * sizeof(uint32_t)) : 0;
+  void* blk = nullptr;
+  CK(dev_alloc(&blk, at, s));
+  B->block = blk;
+  char* base = static_cast<char*>(blk);
+  CK(cudaMemsetAsync(base + o_hdr, 0, 64, s));
+  B->err = reinterpret_cast<int*>(base + o_hdr);
+  int64_t* out = reinterpret_cast<int64_t*>(base + o_hdr + 16);
+  B->binom = reinterpret_cast<uint32_t*>(base + o_binom);
+  B->masks = reinterpret_cast<uint32_t*>(base + o_masks);
+  B->keys = reinterpret_cast<uint64_t*>(base + o_keys);
+  B->low = (G.ushift <= 32) ? reinterpret_cast<uint32_t*>(base + o_low) : nullptr;
+  B->segc = reinterpret_cast<uint32_t*>(base + o_segc);
+  B->nmasks = nmasks;
+  B->dim = int64_t(cap);  // room for every candidate until the count is read
+  if (tabs) {
+    B->tab = reinterpret_cast<uint32_t*>(base + o_tab);
+    B->tab_F = F;
+    for (int r = 0; r < kMaxTabRows; ++r) B->tab_off[r] = off[r];
+  }
+  FusedBasisArgs a;
+  a.G = G;
+  a.R = B->view();
+  a.binom = B->binom;
+  a.masks = B->masks;
+  a.keys = B->keys;
+  a.low = B->low;
+  a.segc = B->segc;
+  a.tab = B->tab;
+  a.L = tabs ? reinterpret_cast<uint32_t*>(base + o_L) : nullptr;
+  a.out = out;
+  a.err = B->err;
+  a.nmasks = nmasks;
+  a.nfree = nfree;
+  a.cap = cap;
+  a.F = F;
+  a.nlast = nlast;
+  switch (G.dg) {
+#define LGT_FUSED_CASE(D)                                        \
+  case D:                                                        \
+    k_basis_fused<D><<<1, kFusedThreads, 0, s>>>(a);             \
+    break;
+    LGT_FUSED_CASE(1)
+    LGT_FUSED_CASE(2)
+    LGT_FUSED_CASE(3)
+    LGT_FUSED_CASE(4)
+    LGT_FUSED_CASE(5)
+    LGT_FUSED_CASE(6)
+    LGT_FUSED_CASE(7)
+#undef LGT_FUSED_CASE
+    default:
+      return "unsupported dg";
+  }
+  lgt::note_launch();
+  CK(cudaGetLastError());
+  int64_t hout[2] = {0, 0};
+  CK(cudaMemcpyAsync(hout, out, sizeof(hout), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  B->dim = hout[0];
+  if (tabs && hout[1]) {  // the block keeps the memory; ranking by search
+    B->tab = nullptr;
+    B->tab_F = 0;
+    return "rank tables failed their self-check";
+  }
+  return std::string();
+}
+
 std::string build_basis_device(BasisDev* B) {
   const Geom& G = B->G;
   cudaStream_t s = B->stream;
+  int64_t expect = 1;  // masks with N_f set bits: C(ns, N_f)
+  for (int j = 0; j < G.nf_target; ++j) expect = expect * (G.ns - j) / (j + 1);
+  const int nfd = (G.ny - 1) * (G.nx - 1);
+  const uint64_t base = uint64_t(2 * G.dg + 1);
+  long double space = 1;
+  for (int i = 0; i < nfd; ++i) space *= (long double)base;
+  if (space * (long double)(expect ? expect : 1) > 1.8e19L)
+    return "candidate space exceeds 64-bit indexing";
+  const uint64_t nfree = ipow(base, nfd);
+  const char* fz = std::getenv("LGT_BASIS_FUSED");  // "0": the multi-launch build
+  if (expect > 0 && space * (long double)expect <= (long double)kFusedMaxCandidates &&
+      !(fz && fz[0] == '0'))
+    return build_basis_fused(B, int(expect), nfree);
+
   CK(dev_alloc_n(&B->err, 1, s));
   CK(cudaMemsetAsync(B->err, 0, sizeof(int), s));
   CK(dev_alloc_n(&B->binom, 32 * 33, s));
@@ -554,21 +796,12 @@ std::string build_basis_device(BasisDev* B) {
   // 1. masks with N_f set bits, ascending: C(ns, N_f) of them (the write is
   //    bounds-checked into the error word against that count)
   MaskPred mp{G.nf_target, 1ull << G.ns};
-  int64_t expect = 1;
-  for (int j = 0; j < G.nf_target; ++j) expect = expect * (G.ns - j) / (j + 1);
   int64_t nmasks = 0;
   std::string err = compact(mp, &B->masks, &nmasks, B->err, s, expect);
   if (!err.empty()) return err;
   B->nmasks = int(nmasks);
 
   // 2. candidates (mask, free e_U digits) -> sorted order keys
-  const int nfd = (G.ny - 1) * (G.nx - 1);
-  const uint64_t base = uint64_t(2 * G.dg + 1);
-  long double space = 1;
-  for (int i = 0; i < nfd; ++i) space *= (long double)base;
-  if (space * (long double)(nmasks ? nmasks : 1) > 1.8e19L)
-    return "candidate space exceeds 64-bit indexing";
-  const uint64_t nfree = ipow(base, nfd);
   int64_t dim = 0;
   if (nmasks > 0) {
     switch (G.dg) {
@@ -611,6 +844,15 @@ std::string build_basis_device(BasisDev* B) {
 
 void free_basis_device(BasisDev* B) {
   cudaStream_t s = B->stream;
+  if (B->block) {  // one allocation holds every buffer
+    dev_free(B->block, s);
+    const Geom G = B->G;
+    const cudaStream_t st = B->stream;
+    *B = BasisDev();
+    B->G = G;
+    B->stream = st;
+    return;
+  }
   dev_free(B->tab, s);
   B->tab = nullptr;
   dev_free(B->keys, s);

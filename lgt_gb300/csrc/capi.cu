@@ -200,7 +200,7 @@ lgt_status lgt_basis_create(int32_t nx, int32_t ny, int32_t dg, const int32_t* g
     b->device = device;
   }
   cudaError_t e = cudaSetDevice(b->device);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->B.stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = stream_get(b->device, &b->B.stream);
   b->own_stream = b->B.stream;
   if (e != cudaSuccess) {
     delete b;
@@ -210,7 +210,7 @@ lgt_status lgt_basis_create(int32_t nx, int32_t ny, int32_t dg, const int32_t* g
   m = build_basis_device(&b->B);
   if (!m.empty()) {
     free_basis_device(&b->B);
-    cudaStreamDestroy(b->B.stream);
+    stream_put(b->device, b->own_stream);
     delete b;
     if (m.find("memory") != std::string::npos) return fail(LGT_ERR_MEMORY, m);
     return fail(LGT_ERR_CUDA, m);
@@ -313,10 +313,10 @@ namespace {
 void release_basis(lgt_basis* b) {
   if (!b || b->refs.fetch_sub(1) != 1) return;
   cudaSetDevice(b->device);
-  // stream-ordered frees; the basis' own stream is released once its work
-  // has completed
+  // stream-ordered frees; the basis' own stream goes back to the device's
+  // list with them queued
   free_basis_device(&b->B);
-  cudaStreamDestroy(b->own_stream);
+  stream_put(b->device, b->own_stream);
   delete b;
 }
 }  // namespace

@@ -12,6 +12,8 @@
 // neighbour tables and the allocation-free observables entry point do not
 // use it.
 //
+// Bases take their streams from a per-device list of released ones.
+//
 // Pinned host staging buffers (the per-CTA solver's tables and outputs, the
 // observables' read-back) come from a process-wide cache by size class:
 // page-locking and unlocking host memory costs far more than a small solve,
@@ -97,6 +99,42 @@ void pinned_put(void* p, size_t cap) {
     }
   }
   cudaFreeHost(p);
+}
+
+// Basis streams: a sweep creates and drops a basis per batch, and creating
+// and destroying a stream each time costs more than a small sector's build.
+// A released stream goes back to its device's list (work still queued on it
+// runs in order before the next user's); beyond kStreamsKept it is destroyed.
+namespace {
+constexpr size_t kStreamsKept = 32;
+std::mutex g_stream_mu;
+std::map<int, std::vector<cudaStream_t>> g_streams;
+}  // namespace
+
+cudaError_t stream_get(int dev, cudaStream_t* s) {
+  {
+    std::lock_guard<std::mutex> lock(g_stream_mu);
+    std::vector<cudaStream_t>& v = g_streams[dev];
+    if (!v.empty()) {
+      *s = v.back();
+      v.pop_back();
+      return cudaSuccess;
+    }
+  }
+  return cudaStreamCreateWithFlags(s, cudaStreamNonBlocking);
+}
+
+void stream_put(int dev, cudaStream_t s) {
+  if (!s) return;
+  {
+    std::lock_guard<std::mutex> lock(g_stream_mu);
+    std::vector<cudaStream_t>& v = g_streams[dev];
+    if (v.size() < kStreamsKept) {
+      v.push_back(s);
+      return;
+    }
+  }
+  cudaStreamDestroy(s);
 }
 
 cudaError_t dev_alloc(void** p, size_t bytes, cudaStream_t s) {

@@ -51,6 +51,9 @@ inline bool df_reductions_enabled() {
 // call; a free takes effect after the work enqueued on `s` before it.
 cudaError_t dev_alloc(void** p, size_t bytes, cudaStream_t s);
 cudaError_t dev_free(void* p, cudaStream_t s);
+// non-blocking streams reused across bases (devmem.cu)
+cudaError_t stream_get(int dev, cudaStream_t* s);
+void stream_put(int dev, cudaStream_t s);
 // Pinned host memory from the library's cache (capacity rounded up to a
 // power of two, at least 4 KB); pinned_put returns it (no copy may still be
 // in flight from or to it).
@@ -123,6 +126,7 @@ struct BasisDev {
   int tab_F = 0;
   int* err = nullptr;           // device error word (DevErr bits)
   cudaStream_t stream = nullptr;
+  void* block = nullptr;        // the one allocation of a small sector's buffers
   RankView view() const {
     RankView v;
     v.keys = keys;
