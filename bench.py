@@ -185,7 +185,14 @@ def gpu_workloads(args, rank, world):
     t0 = time.perf_counter()
     states, key_dict = L.build_basis(NX, NY, DG, g_ch, device=dev)
     torch.cuda.synchronize()
-    basis_ms = (time.perf_counter() - t0) * 1e3
+    basis_ms_first = (time.perf_counter() - t0) * 1e3  # includes loading the kernels
+    warm = []
+    for _ in range(20):
+        t0 = time.perf_counter()
+        b_, _ = L.build_basis(NX, NY, DG, g_ch, device=dev)
+        warm.append((time.perf_counter() - t0) * 1e3)
+        b_.close()
+    basis_ms = statistics.median(warm)
     N = len(states)
     C.check(lib.lgt_basis_set_stream(states.handle, ctypes_ptr(stream.cuda_stream)))
 
@@ -312,7 +319,8 @@ def gpu_workloads(args, rank, world):
                 t_b64=t_b64, dE_b64=dE_b64, plain_times=plain_times, dE_plain=dE_plain,
                 t_pjw=t_pjw, dE_pjw=dE_pjw, e2e_times=e2e_times, e2e_reuse=e2e_reuse,
                 h2d=h2d, d2h=d2h,
-                dE_e2e=dE_e2e, basis_ms=basis_ms, N=N, rf=rf, quench=qn,
+                dE_e2e=dE_e2e, basis_ms=basis_ms, basis_ms_first=basis_ms_first, N=N, rf=rf,
+                quench=qn,
                 t_mref=t_mref, dE_mref=dE_mref, dobs_mix=dobs_mix, dobs_mref=dobs_mref,
                 matvecs_mix=info_mix.matvecs, restarts_mix=info_mix.restarts)
 
@@ -796,7 +804,8 @@ def main():
         "data": "synthetic",
         "config": {"workload": workload, "l2": "flushed between steps (512 MB write, untimed)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
-                   "basis_build_ms": _r(r["basis_ms"])},
+                   "basis_build_ms": _r(r["basis_ms"]),
+                   "basis_build_ms_first_call": _r(r["basis_ms_first"])},
         "roofline": {"kernel": "k_hpsi_%s (%s), 4x4 K=8 complex FP32"
                                % ({"fixed": "fixed", "gather_ordered": "table_bulk"}.get(fam, "table"),
                                   dom["kernel"]),
