@@ -129,8 +129,10 @@ lgt_status ensure_hfeat(lgt_ham* h, size_t n) {
 
 lgt_status upload_couplings(lgt_ham* h) {
   const int K = h->K;
-  std::vector<double> cd(4 * size_t(K));
-  std::vector<float> cf(4 * size_t(K));
+  // [4][K] FP64 coefficients followed by their FP32 copies, as on the device
+  std::vector<double> stage(4 * size_t(K) + 2 * size_t(K));
+  double* cd = stage.data();
+  float* cf = reinterpret_cast<float*>(stage.data() + 4 * size_t(K));
   for (int k = 0; k < K; ++k) {
     const double g = h->g[k], t = h->t[k], m = h->m[k];
     if (!std::isfinite(g) || !std::isfinite(t) || !std::isfinite(m))
@@ -144,13 +146,11 @@ lgt_status upload_couplings(lgt_ham* h) {
     cd[2 * K + k] = -t;              // finite_ed.jl:293-294,312-313
     cd[3 * K + k] = plaq ? -(1.0 / (2.0 * (g * g))) : 0.0;  // matter_gauge_entanglement_pjw.jl:131,142-143
   }
-  for (size_t i = 0; i < cd.size(); ++i) cf[i] = float(cd[i]);
-  // Copies from pageable memory stage the host data before they return, and
+  for (size_t i = 0; i < 4 * size_t(K); ++i) cf[i] = float(cd[i]);
+  // A copy from pageable memory stages the host data before it returns, and
   // every kernel that reads the coefficients runs later on the same stream:
   // no synchronisation needed here.
-  CUDA_OR_FAIL(cudaMemcpyAsync(h->coef_d, cd.data(), sizeof(double) * cd.size(),
-                               cudaMemcpyHostToDevice, h->b->B.stream));
-  CUDA_OR_FAIL(cudaMemcpyAsync(h->coef_f, cf.data(), sizeof(float) * cf.size(),
+  CUDA_OR_FAIL(cudaMemcpyAsync(h->coef_d, stage.data(), sizeof(double) * stage.size(),
                                cudaMemcpyHostToDevice, h->b->B.stream));
   return LGT_OK;
 }
@@ -360,8 +360,9 @@ lgt_status lgt_ham_create(const lgt_basis* b, int32_t K, const double* g, const 
   h->t.assign(t, t + K);
   h->m.assign(m, m + K);
   h->seg_smem = hpsi_seg_smem_default(b->B.nmasks);
-  cudaError_t e = dev_alloc_n(&h->coef_d, 4 * size_t(K), b->B.stream);
-  if (e == cudaSuccess) e = dev_alloc_n(&h->coef_f, 4 * size_t(K), b->B.stream);
+  // the FP64 coefficients and their FP32 copies in one allocation
+  cudaError_t e = dev_alloc_n(&h->coef_d, 6 * size_t(K), b->B.stream);
+  if (e == cudaSuccess) h->coef_f = reinterpret_cast<float*>(h->coef_d + 4 * size_t(K));
   if (e != cudaSuccess) {
     lgt_ham_destroy(h);
     return cuda_fail(e, "lgt_ham_create");
@@ -708,12 +709,14 @@ lgt_status lgt_ground_state(lgt_ham* h, const lgt_krylov_opts* opts, double* E0,
   std::vector<double> res(h->K);
   if (use_cta(h, opts, p)) {
     double* r = res.data();
-    lgt_status rc = cta_solve({h}, p, {X}, &E0, &r, info);
+    // a host psi is copied back behind the solve, before its one
+    // synchronisation (on an error status its contents are unspecified)
+    const bool host_psi = psi && !on_device(flags);
+    auto copy_back = [&]() -> cudaError_t {
+      return host_psi ? cudaMemcpyAsync(psi, X, bytes, cudaMemcpyDeviceToHost, s) : cudaSuccess;
+    };
+    lgt_status rc = cta_solve({h}, p, {X}, &E0, &r, info, copy_back);
     if (residual) std::memcpy(residual, res.data(), sizeof(double) * h->K);
-    if (rc != LGT_OK && rc != LGT_ERR_NOCONV) return rc;
-    if (psi && !on_device(flags))
-      CUDA_OR_FAIL(cudaMemcpyAsync(psi, X, bytes, cudaMemcpyDeviceToHost, s));
-    CUDA_OR_FAIL(cudaStreamSynchronize(s));
     return rc;
   }
   KrylovReport rep;
@@ -1125,8 +1128,7 @@ void lgt_ham_destroy(lgt_ham* h) {
     if (s) cudaStreamSynchronize(s);
     pinned_put(h->hfeat, h->hfeat_n * sizeof(double));
   }
-  dev_free(h->coef_d, s);
-  dev_free(h->coef_f, s);
+  dev_free(h->coef_d, s);  // coef_f lives in the same allocation
   lgt_basis* b = const_cast<lgt_basis*>(h->b);
   delete h;
   release_basis(b);

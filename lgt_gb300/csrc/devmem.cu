@@ -137,6 +137,43 @@ void stream_put(int dev, cudaStream_t s) {
   cudaStreamDestroy(s);
 }
 
+// Timing events of the per-CTA solver's workspaces, reused the same way.
+namespace {
+constexpr size_t kEventsKept = 64;
+std::mutex g_event_mu;
+std::map<int, std::vector<cudaEvent_t>> g_events;
+}  // namespace
+
+cudaError_t event_get(cudaEvent_t* e) {
+  int dev = 0;
+  cudaError_t r = cudaGetDevice(&dev);
+  if (r != cudaSuccess) return r;
+  {
+    std::lock_guard<std::mutex> lock(g_event_mu);
+    std::vector<cudaEvent_t>& v = g_events[dev];
+    if (!v.empty()) {
+      *e = v.back();
+      v.pop_back();
+      return cudaSuccess;
+    }
+  }
+  return cudaEventCreate(e);
+}
+
+void event_put(cudaEvent_t e) {
+  if (!e) return;
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess) {
+    std::lock_guard<std::mutex> lock(g_event_mu);
+    std::vector<cudaEvent_t>& v = g_events[dev];
+    if (v.size() < kEventsKept) {
+      v.push_back(e);
+      return;
+    }
+  }
+  cudaEventDestroy(e);
+}
+
 cudaError_t dev_alloc(void** p, size_t bytes, cudaStream_t s) {
   *p = nullptr;
   int dev = 0;

@@ -54,6 +54,9 @@ cudaError_t dev_free(void* p, cudaStream_t s);
 // non-blocking streams reused across bases (devmem.cu)
 cudaError_t stream_get(int dev, cudaStream_t* s);
 void stream_put(int dev, cudaStream_t s);
+// events reused across workspaces of the current device (devmem.cu)
+cudaError_t event_get(cudaEvent_t* e);
+void event_put(cudaEvent_t e);
 // Pinned host memory from the library's cache (capacity rounded up to a
 // power of two, at least 4 KB); pinned_put returns it (no copy may still be
 // in flight from or to it).

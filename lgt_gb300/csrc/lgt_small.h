@@ -23,6 +23,7 @@ struct Pattern {
   uint32_t* nbr = nullptr;
   int16_t* e2 = nullptr;
   int16_t* stag = nullptr;
+  void* block = nullptr;  // the one allocation the arrays above are carved from
 };
 
 struct SmallProblem {

@@ -817,12 +817,26 @@ std::string build_pattern(const BasisDev& B, uint32_t model, Pattern* P, cudaStr
   // the exact count back; the fill kernel checks its bounds.
   const Geom& G = B.G;
   const size_t cap = size_t(N) * size_t(G.max_moves > 0 ? G.max_moves : 1);
-  SCK(dev_alloc_n(&P->rowptr, size_t(N) + 1, s));
-  SCK(dev_alloc_n(&P->e2, size_t(N) + 1, s));
-  SCK(dev_alloc_n(&P->stag, size_t(N) + 1, s));
-  SCK(dev_alloc_n(&P->nbr, cap + 1, s));
-  int* counts = nullptr;
-  SCK(dev_alloc_n(&counts, size_t(N) + 1, s));
+  // one pool allocation for the row pointers, the diagonal features, the
+  // neighbour entries and the scan's counts (256-byte aligned pieces)
+  size_t at = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = at;
+    at += (bytes + 255) & ~size_t(255);
+    return o;
+  };
+  const size_t o_rowptr = take((size_t(N) + 1) * sizeof(int));
+  const size_t o_e2 = take((size_t(N) + 1) * sizeof(int16_t));
+  const size_t o_stag = take((size_t(N) + 1) * sizeof(int16_t));
+  const size_t o_nbr = take((cap + 1) * sizeof(uint32_t));
+  const size_t o_counts = take((size_t(N) + 1) * sizeof(int));
+  SCK(dev_alloc(&P->block, at, s));
+  char* base = static_cast<char*>(P->block);
+  P->rowptr = reinterpret_cast<int*>(base + o_rowptr);
+  P->e2 = reinterpret_cast<int16_t*>(base + o_e2);
+  P->stag = reinterpret_cast<int16_t*>(base + o_stag);
+  P->nbr = reinterpret_cast<uint32_t*>(base + o_nbr);
+  int* counts = reinterpret_cast<int*>(base + o_counts);
   const unsigned blocks = unsigned((N + 255) / 256);
   const RankView R = B.view();
   const bool plaq = model & kModelPlaq, jw = model & kModelJW;
@@ -841,7 +855,6 @@ std::string build_pattern(const BasisDev& B, uint32_t model, Pattern* P, cudaStr
   else
     k_pattern_fill<false, false><<<blocks, 256, 0, s>>>(G, R, N, P->rowptr, P->nbr, P->e2, P->stag, B.err), lgt::note_launch();
   SCK(cudaGetLastError());
-  SCK(dev_free(counts, s));
   return std::string();
 }
 
@@ -851,16 +864,13 @@ void free_small_work(SmallWork* w, cudaStream_t s) {
     cudaStreamSynchronize(s);  // a copy staged through it may still be in flight
     pinned_put(w->host, w->host_bytes);
   }
-  if (w->ev[0]) cudaEventDestroy(w->ev[0]);
-  if (w->ev[1]) cudaEventDestroy(w->ev[1]);
+  event_put(w->ev[0]);
+  event_put(w->ev[1]);
   *w = SmallWork();
 }
 
 void free_pattern(Pattern* P, cudaStream_t s) {
-  dev_free(P->rowptr, s);
-  dev_free(P->nbr, s);
-  dev_free(P->e2, s);
-  dev_free(P->stag, s);
+  dev_free(P->block, s);
   *P = Pattern();
 }
 
@@ -967,8 +977,8 @@ std::string small_ground_states(const std::vector<SmallJob>& jobs, const SmallPa
     ws->up_bytes = pb + ub;
   }
   double* h_out = reinterpret_cast<double*>(hst + tb);
-  if (!ws->ev[0]) SCK(cudaEventCreate(&ws->ev[0]));
-  if (!ws->ev[1]) SCK(cudaEventCreate(&ws->ev[1]));
+  if (!ws->ev[0]) SCK(event_get(&ws->ev[0]));
+  if (!ws->ev[1]) SCK(event_get(&ws->ev[1]));
   cudaEvent_t e0 = ws->ev[0], e1 = ws->ev[1];
   auto launch = [&](int rows, int cl) {
     return mixed ? launch_cta<float>(d_probs, d_units, int(nunits), maxN, prm, s, rows, cl)
