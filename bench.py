@@ -63,17 +63,20 @@ def _cpu_point(args):
     """basis + H + Lanczos ground state + measure for one coupling point,
     the span gs_benchmark.jl:116-125 times (eigsolve settings of
     finite_ed.jl:336-338: krylovdim 50, tol 1e-10, lowest).  args: (g, seed)
-    on the headline lattice, or (nx, ny, g, m, seed)."""
+    on the headline lattice, or (nx, ny, g, m, seed[, model])."""
+    model = "ref"
     if len(args) == 2:
         (g, seed), (nx, ny, m) = args, (NX, NY, MASS)
-    else:
+    elif len(args) == 5:
         nx, ny, g, m, seed = args
+    else:
+        nx, ny, g, m, seed, model = args
     from scipy.sparse.linalg import eigsh
 
     from oracle import oracle as O
     t0 = time.perf_counter()
     b = O.build_basis(nx, ny, DG, O.staggered_charges(nx, ny))
-    H = O.build_hamiltonian(b, g=g, t=T_HOP, m=m, model="ref")
+    H = O.build_hamiltonian(b, g=g, t=T_HOP, m=m, model=model)
     v0 = np.random.default_rng(seed).standard_normal(b.dim)
     w, v = eigsh(H, k=1, which="SA", tol=1e-10, ncv=min(50, b.dim), v0=v0)
     O.measure(v[:, 0], b)
@@ -314,6 +317,7 @@ def gpu_workloads(args, rank, world):
     # ---- roofline: H*psi on the 4x4 lattice (working set > L2) ---------------
     rf = roofline(L, C, lib, torch, stream, dev)
     qn = quench(L, C, lib, torch, stream, dev, n_steps=args.quench_steps)
+    qn["pjw"] = quench(L, C, lib, torch, stream, dev, n_steps=args.quench_steps, model="pjw")
     states.close()
     return dict(t_mix=t_mix, dE_mix=dE_mix, launches=launches, clocks=clocks, info_mix=info_mix,
                 t_b64=t_b64, dE_b64=dE_b64, plain_times=plain_times, dE_plain=dE_plain,
@@ -361,9 +365,10 @@ def gs_only(args):
     return {"gs_per_s": KPTS / statistics.mean(ts), "ms_per_step": 1e3 * statistics.mean(ts)}
 
 
-def quench(L, C, lib, torch, stream, dev, n_steps=100, K=None):
+def quench(L, C, lib, torch, stream, dev, n_steps=100, K=None, model="ref"):
     """4x4 real-time quench panel: K points (8 unless given) g ~ U[0.5, 1.5]
-    (seed 0), m = 0.5, t = 1, from the staggered product state, dt = 0.05;
+    (seed 0), m = 0.5, t = 1, from the staggered product state, dt = 0.05,
+    under the model flags `model` ("ref" or "pjw");
     n_steps Krylov exp(-iH dt) steps (100: t = 5) with observables every step, FP64 and
     FP32-mixed.  Reports steps/s, the norm drift (max |1 - ||psi||| before
     each renormalisation), the energy drift at the end, and the largest
@@ -375,10 +380,11 @@ def quench(L, C, lib, torch, stream, dev, n_steps=100, K=None):
     ns = RF_NX * RF_NY
     K = RF_K if K is None else K
     gs = np.random.default_rng(0).uniform(0.5, 1.5, K)
-    H = L.build_hamiltonian(b, g=gs, t=1.0, m=0.5, model="ref")
+    H = L.build_hamiltonian(b, g=gs, t=1.0, m=0.5, model=model)
     v0 = L.staggered_product_state(b)
     i0 = int(np.argmax(np.abs(v0)))
-    out = {"N": N, "K": K, "dt": 0.05, "steps_timed": n_steps, "t_end": 0.05 * n_steps}
+    out = {"N": N, "K": K, "model": model, "dt": 0.05, "steps_timed": n_steps,
+           "t_end": 0.05 * n_steps}
     traj = {}
     for prec, code in (("fp64", C.LGT_FP64), ("fp32_mixed", C.LGT_FP32_MIXED)):
         psi = torch.zeros((N, K, 2), dtype=torch.float64, device="cuda")
@@ -460,22 +466,27 @@ def extra_configs(L, pool, dev, reps=3):
     3x2 plain FP64 at tol 1e-12; 4x3 (g = 0.8, m = 0.3) FP32-mixed against
     FP64, errors of E0, <E^2>, <n_stag> against the FP64 oracle, both model
     flags; the uneven batch 3x2 + 4x2 + 3x3 + 4x3 x 16 points in one call."""
-    jobs = [(3, 2, 1.0, 0.5, "ref", False)]
-    jobs += [(4, 3, 0.8, 0.3, model, True) for model in ("ref", "pjw")]
+    MODELS = ("ref", "pjw")
+    jobs = [(3, 2, 1.0, 0.5, model, False) for model in MODELS]
+    jobs += [(4, 3, 0.8, 0.3, model, True) for model in MODELS]
     pts = c4_points()
-    for (nx, ny), (g, m) in zip(C4_LATTICES, pts):
-        jobs += [(nx, ny, float(g[i]), float(m[i]), "ref", False) for i in range(16)]
+    for model in MODELS:
+        for (nx, ny), (g, m) in zip(C4_LATTICES, pts):
+            jobs += [(nx, ny, float(g[i]), float(m[i]), model, False) for i in range(16)]
     out = {}
-    # C1: 3x2, FP64, tol 1e-12, start normal(seed 0)
+    # C1: 3x2, FP64, tol 1e-12, start normal(seed 0), both models
     b, kd = L.build_basis(3, 2, 1, L.staggered_charges(3, 2), device=dev)
-    H = L.build_hamiltonian(b, kd, 3, 2, 1, g=1.0, t=1.0, m=0.5)
-    ts = []
-    for it in range(2 + reps):
-        t0 = time.perf_counter()
-        E1, _ = L.find_ground_state(H, tol=1e-12, seed=0)
-        if it >= 2:
-            ts.append(time.perf_counter() - t0)
-    H.close()
+    c1 = {}
+    for model in MODELS:
+        H = L.build_hamiltonian(b, kd, 3, 2, 1, g=1.0, t=1.0, m=0.5, model=model)
+        ts = []
+        for it in range(2 + reps):
+            t0 = time.perf_counter()
+            E1, _ = L.find_ground_state(H, tol=1e-12, seed=0)
+            if it >= 2:
+                ts.append(time.perf_counter() - t0)
+        c1[model] = (E1, min(ts))
+        H.close()
     b.close()
     # C3: 4x3, g = 0.8, m = 0.3, FP32-mixed vs FP64, both models
     b, kd = L.build_basis(4, 3, 1, L.staggered_charges(4, 3), device=dev)
@@ -493,37 +504,44 @@ def extra_configs(L, pool, dev, reps=3):
                                            "s_incl_host_copies": time.perf_counter() - t0}
         H.close()
     b.close()
-    # C4: uneven batch, FP32-mixed, one call
-    bases, Hs = [], []
-    for (nx, ny), (g, m) in zip(C4_LATTICES, pts):
-        bb, kk = L.build_basis(nx, ny, 1, L.staggered_charges(nx, ny), device=dev)
-        bases.append(bb)
-        Hs.append(L.build_hamiltonian(bb, kk, nx, ny, 1, g=g, t=1.0, m=m))
-    ts4 = []
-    for it in range(1 + 2 * reps):
-        t0 = time.perf_counter()
-        res4 = L.find_ground_states(Hs, precision="fp32_mixed")
-        if it >= 1:
-            ts4.append(time.perf_counter() - t0)
-    for H in Hs:
-        H.close()
-    for bb in bases:
+    # C4: uneven batch, FP32-mixed, one call, both models
+    bases = []
+    for (nx, ny), _ in zip(C4_LATTICES, pts):
+        bases.append(L.build_basis(nx, ny, 1, L.staggered_charges(nx, ny), device=dev))
+    ts4, res4 = {}, {}
+    for model in MODELS:
+        Hs = [L.build_hamiltonian(bb, kk, nx, ny, 1, g=g, t=1.0, m=m, model=model)
+              for (bb, kk), (nx, ny), (g, m) in zip(bases, C4_LATTICES, pts)]
+        ts4[model] = []
+        for it in range(1 + 2 * reps):
+            t0 = time.perf_counter()
+            res4[model] = L.find_ground_states(Hs, precision="fp32_mixed")
+            if it >= 1:
+                ts4[model].append(time.perf_counter() - t0)
+        for H in Hs:
+            H.close()
+    for bb, _ in bases:
         bb.close()
     # C4 on the host cores: the oracle port of the per-point span, one point
     # per process (after the GPU timing, so the host cores are idle then)
-    c4_jobs = [(nx, ny, float(g[i]), float(m[i]), i)
-               for (nx, ny), (g, m) in zip(C4_LATTICES, pts) for i in range(16)]
-    t0 = time.perf_counter()
-    pool.map(_cpu_point, c4_jobs)
-    c4_cpu_s = time.perf_counter() - t0
+    c4_cpu_s = {}
+    for model in MODELS:
+        c4_jobs = [(nx, ny, float(g[i]), float(m[i]), i, model)
+                   for (nx, ny), (g, m) in zip(C4_LATTICES, pts) for i in range(16)]
+        t0 = time.perf_counter()
+        pool.map(_cpu_point, c4_jobs)
+        c4_cpu_s[model] = time.perf_counter() - t0
     # the oracle's reference values, computed after the timed sections so that
     # the host cores are idle while those run
     ref = pool.map(_oracle_point, jobs)
-    out["c1_3x2_fp64_tol1e-12"] = {"N": 90, "E0": E1, "rel_dE": abs(E1 - ref[0][0]) / abs(ref[0][0]),
-                                   "ms_per_solve_incl_host_copies": 1e3 * min(ts)}
+    for q, model in enumerate(MODELS):
+        E1, t1 = c1[model]
+        out["c1_3x2_fp64_tol1e-12" + ("" if model == "ref" else "_pjw")] = {
+            "N": 90, "model": model, "E0": E1, "rel_dE": abs(E1 - ref[q][0]) / abs(ref[q][0]),
+            "ms_per_solve_incl_host_copies": 1e3 * t1}
     c3e = {}
-    for q, model in enumerate(("ref", "pjw")):
-        E0o, E2o, nso = ref[1 + q]
+    for q, model in enumerate(MODELS):
+        E0o, E2o, nso = ref[2 + q]
         for prec in ("fp64", "fp32_mixed", "fp32_mixed_refined"):
             r = c3["%s_%s" % (model, prec)]
             c3e["%s_%s" % (model, prec)] = {
@@ -531,15 +549,18 @@ def extra_configs(L, pool, dev, reps=3):
                 "abs_dn_stag": abs(r["n_stag"] - nso),
                 "s_incl_host_copies": r["s_incl_host_copies"]}
     out["c3_4x3_mixed_vs_fp64"] = {"N": 72211, "g": 0.8, "m": 0.3, "errors_vs_fp64_oracle": c3e}
-    e4 = np.array([r[0] for r in ref[3:]])
-    got = np.concatenate([E for E, _ in res4])
-    out["c4_uneven_batch"] = {
-        "lattices": ["%dx%d" % l for l in C4_LATTICES], "points_per_lattice": 16,
-        "rows_total": int(sum(16 * bb for bb in (90, 645, 2443, 72211))),
-        "gs_per_s_incl_host_copies": 64 / statistics.median(ts4),
-        "gs_per_s_min_max": [64 / max(ts4), 64 / min(ts4)], "repeats": len(ts4),
-        "cpu_baseline_gs_per_s": 64 / c4_cpu_s,
-        "max_rel_dE_fp32_mixed": float(np.max(np.abs(got - e4) / np.abs(e4)))}
+    for q, model in enumerate(MODELS):
+        e4 = np.array([r[0] for r in ref[4 + 64 * q:4 + 64 * (q + 1)]])
+        got = np.concatenate([E for E, _ in res4[model]])
+        t4 = ts4[model]
+        out["c4_uneven_batch" + ("" if model == "ref" else "_pjw")] = {
+            "model": model,
+            "lattices": ["%dx%d" % l for l in C4_LATTICES], "points_per_lattice": 16,
+            "rows_total": int(sum(16 * bb for bb in (90, 645, 2443, 72211))),
+            "gs_per_s_incl_host_copies": 64 / statistics.median(t4),
+            "gs_per_s_min_max": [64 / max(t4), 64 / min(t4)], "repeats": len(t4),
+            "cpu_baseline_gs_per_s": 64 / c4_cpu_s[model],
+            "max_rel_dE_fp32_mixed": float(np.max(np.abs(got - e4) / np.abs(e4)))}
     return out
 
 
@@ -677,6 +698,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quench-steps", type=int, default=100,
                     help="timed 4x4 quench steps (dt = 0.05; 100 reach t = 5)")
+    ap.add_argument("--quench-model", default="ref", choices=["ref", "pjw"],
+                    help="model flags of --part quench")
     ap.add_argument("--quench-points", type=int, default=None,
                     help="--part quench: coupling points in the panel (8 unless given)")
     ap.add_argument("--detail", default=None,
@@ -735,7 +758,7 @@ def main():
         from lgt_gb300 import _capi as C
         torch.cuda.set_device(0)
         q = quench(L, C, C.load(), torch, torch.cuda.Stream(), 0, n_steps=args.quench_steps,
-                   K=args.quench_points)
+                   K=args.quench_points, model=args.quench_model)
         print(json.dumps({"part": "quench", "quench": q}))
         return
 
@@ -795,6 +818,8 @@ def main():
     qn = r["quench"]
     c3 = extra["c3_4x3_mixed_vs_fp64"]["errors_vs_fp64_oracle"]
     c4 = extra["c4_uneven_batch"]
+    c4p = extra["c4_uneven_batch_pjw"]
+    qp = qn["pjw"]
     line = {
         "metric": METRIC,
         "value": value, "unit": "GS/s", "n_gpus": args.gpus, "steps": args.steps,
@@ -832,14 +857,25 @@ def main():
             "c4_gs_per_s": _r(c4["gs_per_s_incl_host_copies"]),
             "c4_min_max": [_r(v) for v in c4["gs_per_s_min_max"]],
             "c4_cpu_gs_per_s": _r(c4["cpu_baseline_gs_per_s"]),
-            "c4_max_rel_dE": _r(c4["max_rel_dE_fp32_mixed"])},
+            "c4_max_rel_dE": _r(c4["max_rel_dE_fp32_mixed"]),
+            "pjw": {"c1_rel_dE": _r(extra["c1_3x2_fp64_tol1e-12_pjw"]["rel_dE"]),
+                    "c4_gs_per_s": _r(c4p["gs_per_s_incl_host_copies"]),
+                    "c4_cpu_gs_per_s": _r(c4p["cpu_baseline_gs_per_s"]),
+                    "c4_max_rel_dE": _r(c4p["max_rel_dE_fp32_mixed"])}},
         "quench_4x4": {"K": RF_K, "t_end": qn["t_end"],
                        "steps_per_s": {p: _r(qn[p]["quench_steps_per_s"])
                                        for p in ("fp64", "fp32_mixed")},
                        "norm_drift": {p: _r(qn[p]["max_norm_drift"]) for p in ("fp64", "fp32_mixed")},
                        "energy_drift": {p: _r(qn[p]["max_rel_energy_drift"])
                                         for p in ("fp64", "fp32_mixed")},
-                       "mixed_vs_fp64": {k: _r(v) for k, v in qn["mixed_vs_fp64_max_abs"].items()}},
+                       "mixed_vs_fp64": {k: _r(v) for k, v in qn["mixed_vs_fp64_max_abs"].items()},
+                       "pjw": {"steps_per_s": {p: _r(qp[p]["quench_steps_per_s"])
+                                               for p in ("fp64", "fp32_mixed")},
+                               "norm_drift": {p: _r(qp[p]["max_norm_drift"])
+                                              for p in ("fp64", "fp32_mixed")},
+                               "energy_drift": {p: _r(qp[p]["max_rel_energy_drift"])
+                                                for p in ("fp64", "fp32_mixed")},
+                               "mixed_vs_fp64_E2": _r(qp["mixed_vs_fp64_max_abs"]["E2_mean"])}},
         "accuracy": {"max_rel_dE_fp32_mixed": _r(r["dE_mix"]),
                      "max_abs_dobs_mixed_16pts": _r(r["dobs_mix"]),
                      "max_rel_dE_mixed_refined": _r(r["dE_mref"]),

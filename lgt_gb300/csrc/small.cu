@@ -390,15 +390,11 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
       // prm.reorth) runs only when a pass cancels more than two digits,
       // ||w_after|| < 1e-2 ||w_before||: the rounding error it leaves along the
       // basis is then above eps * 100 relative to w.
-      // ||w||^2 comes with each pass's dots (w against itself in slot j + 1),
-      // and ||w_after||^2 = ||w||^2 - sum_i h_i^2 over the orthonormal basis:
-      // beta without a reduction of its own.  Relative to ||w_after||^2 that
-      // difference is accurate to eps * ||w||^2 / ||w_after||^2 <= 1e4 eps
-      // whenever it is accepted; a last pass that still cancels more than two
-      // digits takes the norm of the updated rows instead.
-      double ss = 0.0;
+      // ||w||^2 before the first pass comes with that pass's dots: w against
+      // itself in slot j + 1 (no separate block reduction)
+      double nb = 0.0, ss = 0.0;
       for (int pass = 0; pass < prm.reorth; ++pass) {
-        const int jd = j + 1;
+        const int jd = (pass == 0) ? j + 1 : j;
         for (int b0 = 0; b0 <= jd; b0 += 4) {
           if constexpr (kDF) {
             df pd[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
@@ -488,33 +484,7 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
         }
         par_dot ^= 1;
         __syncthreads();
-        const double self = s_h[j + 1];
-        // beta = ||w_after||, 1 / beta and the exhaustion test of this step
-        // (alpha_j is final: the pass's reduction synchronised), by thread 0
-        auto beta_root = [&](double sv) {
-          const double rs = (sv > 0.0) ? rsqrt(sv) : 0.0;
-          const double b = sv * rs;
-          s_sum[0] = sv;
-          s_sum[1] = b;
-          s_sum[2] = rs;
-          if (kDF) {
-            const float rh = narrow(rs);
-            s_rb[0] = rh;
-            s_rb[1] = narrow(rs - widen(rh));
-          }
-          double scl = fabs(s_alpha[j]);
-          if (j > 0) scl = fmax(scl, s_beta[j - 1]);
-          s_exh = (b > tiny_rel * fmax(scl, 1.0)) ? 0 : 1;
-        };
-        // the difference of squares by warp 0 ahead of its update rows, the
-        // other warps updating meanwhile; both CTAs of a split unit hold the
-        // same dots and take the same sum
-        if (wid == 0) {
-          double q = 0.0;
-          for (int i = lane; i <= j; i += 32) q = fma(s_h[i], s_h[i], q);
-          q = warp_sum(q);
-          if (lane == 0) beta_root(self - q);
-        }
+        if (pass == 0) nb = ss = s_h[j + 1];
         if constexpr (kDF) {
           for (int b0 = 0; b0 <= j; b0 += 4) {
             float hh[4], hl[4];
@@ -551,12 +521,6 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
             }
           }
         }
-        __syncthreads();  // beta_root's results
-        ss = s_sum[0];
-        if (!(ss < 1e-4 * self)) break;
-        if (pass + 1 < prm.reorth) continue;
-        // the last pass cancelled more than two digits (an exhausted Krylov
-        // space among them): the norm of the updated rows themselves
         double s1 = 0.0;
         if constexpr (kDF) {
           df n2{0.f, 0.f};
@@ -567,9 +531,26 @@ __global__ void __launch_bounds__(kCta, 1) k_lanczos_cta(const SmallProblem* pro
 #pragma unroll
           for (int i = 0; i < R; ++i) s1 = fma(w[i], w[i], s1);
         }
-        ss = unit_sum<CL>(s1, s_red, s_sum, s_xch, par_sum, beta_root);
+        // beta = ||w||, 1 / beta and the exhaustion test of this step, by
+        // thread 0 (alpha_j is final: the pass's reduction synchronised)
+        ss = unit_sum<CL>(s1, s_red, s_sum, s_xch, par_sum, [&](double sv) {
+          const double rs = (sv > 0.0) ? rsqrt(sv) : 0.0;
+          const double b = sv * rs;
+          s_sum[1] = b;
+          s_sum[2] = rs;
+          if (kDF) {
+            const float rh = narrow(rs);
+            s_rb[0] = rh;
+            s_rb[1] = narrow(rs - widen(rh));
+          }
+          double scl = fabs(s_alpha[j]);
+          if (j > 0) scl = fmax(scl, s_beta[j - 1]);
+          s_exh = (b > tiny_rel * fmax(scl, 1.0)) ? 0 : 1;
+        });
+        if (!(ss < 1e-4 * nb)) break;
+        nb = ss;
       }
-      // beta = sqrt(ss) and the exhaustion flag from the last pass
+      // beta = sqrt(ss) and the exhaustion flag from the last pass's block_sum
       // (reorth_passes >= 1: at least one pass ran)
       const double beta = s_sum[1];
       const double rbeta = s_sum[2];

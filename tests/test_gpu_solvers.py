@@ -217,3 +217,33 @@ def test_cta_cluster_uneven_and_refined(oracle, lgt, monkeypatch):
         assert abs(E0[k] - E0o) <= 1e-12 * abs(E0o)
     for H in Hs:
         H.close()
+
+
+def _wide_points(n, seed):
+    """Couplings of the uneven-batch benchmark: g log-uniform on [0.3, 3]
+    (electric or plaquette terms dominating), m uniform on [0, 1]."""
+    rng = np.random.default_rng(seed)
+    return np.exp(rng.uniform(np.log(0.3), np.log(3.0), n)), rng.uniform(0.0, 1.0, n)
+
+
+@pytest.mark.parametrize("model", ["ref", "pjw"])
+@pytest.mark.parametrize("nx,ny", [(3, 2), (4, 2)])
+def test_cta_wide_couplings(oracle, lgt, nx, ny, model):
+    """The per-point solver over couplings far from the headline's range
+    (electric or plaquette terms dominating) against the oracle's dense
+    ground states.  A 3x2 PJW point at g = 2.58 once converged to a wrong
+    Ritz pair when beta was taken from the dots (||w||^2 - sum h^2) instead
+    of the updated rows' own norm."""
+    g, m = _wide_points(16, 0)
+    g = np.concatenate([g, [2.583, 0.302, 1.952]])
+    m = np.concatenate([m, [0.384, 0.981, 0.028]])
+    b = lgt.build_basis(nx, ny, 1, lgt.staggered_charges(nx, ny))[0]
+    H = lgt.build_hamiltonian(b, g=g, t=1.0, m=m, model=model)
+    ob = oracle.build_basis(nx, ny, 1, oracle.staggered_charges(nx, ny))
+    Eo = np.array([oracle.ground_state(oracle.build_hamiltonian(ob, g=gk, t=1.0, m=mk,
+                                                                model=model))[0]
+                   for gk, mk in zip(g, m)])
+    for precision, tol in (("fp32_mixed", 1e-10), ("fp64", 1e-12)):
+        E, _ = lgt.find_ground_state(H, precision=precision, solver="cta", as_complex=False)
+        assert np.max(np.abs(E - Eo) / np.abs(Eo)) <= tol, precision
+    H.close()
