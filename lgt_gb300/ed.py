@@ -475,6 +475,37 @@ def find_ground_state(H: Hamiltonian, *, tol=1e-10, krylovdim=50, maxiter=300, p
     return E, P
 
 
+def find_ground_state_measured(H: Hamiltonian, *, tol=1e-10, krylovdim=50, maxiter=300,
+                               precision="fp64", seed=0, check_every=None, refine_steps=0,
+                               use_graph=True, solver="auto", as_complex=True):
+    """find_ground_state then measure_ED of its state, the pair
+    gs_benchmark.jl:116-125 runs per point, in one call
+    (lgt_ground_state_observe: the observables are taken from the device
+    copy of the state before the solve's one synchronisation).  Returns
+    (E0, psi, obs), E0 and psi as find_ground_state returns them and obs as
+    measure_ED(psi, ...) does: one dict for K = 1, else a list of K."""
+    b = H.basis
+    N, K = b.dim, H.K
+    o = _opts(False, tol, krylovdim, maxiter, precision, seed, check_every, refine_steps,
+              use_graph, False, solver=solver)
+    psi = np.empty((N, K), np.float64)  # written whole by the solver
+    E0 = np.zeros(K)
+    info = C.Info()
+    ns, npl = b.nx * b.ny, max((b.nx - 1) * (b.ny - 1), 0)
+    nf = np.zeros(K * ns)
+    e2 = np.zeros(K * ns)
+    pl = np.zeros(max(K * npl, 1))
+    summ = (C.Obs * K)()
+    C.check(C.load().lgt_ground_state_observe(H.handle, ctypes.byref(o), _p(E0), _p(psi), None,
+                                              0, ctypes.byref(info), _p(nf), _p(e2), _p(pl),
+                                              summ))
+    obs = _obs_dicts(b, K, nf, e2, pl, summ)
+    out_psi = psi.astype(np.complex128) if as_complex else psi
+    if K == 1:
+        return float(E0[0]), out_psi[:, 0], obs[0]
+    return E0, out_psi, obs
+
+
 def find_ground_states(Hs, *, tol=1e-10, krylovdim=50, maxiter=300, precision="fp64", seed=0,
                        check_every=None, solver="auto", device_psi=None, return_info=False):
     """Ground states of several Hamiltonians (lattices, sectors, coupling

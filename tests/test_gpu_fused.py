@@ -59,3 +59,26 @@ def test_fused_equals_two_calls(oracle, lgt, nx, ny, K, device, prec):
     ob = oracle.build_basis(nx, ny, 1, oracle.staggered_charges(nx, ny))
     E0o = oracle.ground_state(oracle.build_hamiltonian(ob, g=gs[0], t=1.0, m=0.5))[0]
     assert abs(a[0][0] - E0o) <= 1e-10 * abs(E0o)
+
+
+@pytest.mark.parametrize("precision", ["fp32_mixed", "fp64"])
+@pytest.mark.parametrize("K", [1, 16])
+def test_python_measured_wrapper(lgt, precision, K):
+    """find_ground_state_measured against find_ground_state + measure_ED
+    through the Python API: bitwise the same energies, states and dicts."""
+    b = lgt.build_basis(4, 2, 1, lgt.staggered_charges(4, 2))[0]
+    gs = np.linspace(0.6, 1.9, K)
+    H = lgt.build_hamiltonian(b, g=gs, t=1.0, m=0.5, model="pjw")
+    E1, P1, O1 = lgt.find_ground_state_measured(H, precision=precision, as_complex=False)
+    E2, P2 = lgt.find_ground_state(H, precision=precision, as_complex=False)
+    O2 = lgt.measure_ED(P2, b, 4, 2, 1, 0.0)
+    assert np.array_equal(np.atleast_1d(E1), np.atleast_1d(E2))
+    assert np.array_equal(P1, P2)
+    recs1 = [O1] if K == 1 else O1
+    recs2 = [O2] if K == 1 else O2
+    assert len(recs1) == len(recs2) == K
+    for a, c in zip(recs1, recs2):
+        assert set(a) == set(c)
+        for key in a:
+            assert np.array_equal(np.asarray(a[key]), np.asarray(c[key])), key
+    H.close()
