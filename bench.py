@@ -279,9 +279,10 @@ def gpu_workloads(args, rank, world):
 
     # ---- end to end through the public API, host buffers ----------------------
     # (a) span-matched: every step builds the basis and the Hamiltonian, then
-    # solves and measures, the span gs_benchmark.jl:116-125 times per point
-    # and the CPU arm times here; (b) the same with the basis and Hamiltonian
-    # handles kept across steps (a sweep that only changes couplings).
+    # solves and measures (find_ground_state_measured: the pair in one call),
+    # the span gs_benchmark.jl:116-125 times per point and the CPU arm times
+    # here; (b) the same with the basis and Hamiltonian handles kept across
+    # steps (a sweep that only changes couplings).
     e2e_times, e2e_reuse = [], []
     C.check(lib.lgt_basis_set_stream(states.handle, None))
     for it in range(args.warmup + args.steps):
@@ -290,8 +291,8 @@ def gpu_workloads(args, rank, world):
         t0 = time.perf_counter()
         st, kd = L.build_basis(NX, NY, DG, g_ch, device=dev)               # H2D: charges
         Hs = L.build_hamiltonian(st, kd, NX, NY, DG, g=gs, t=T_HOP, m=MASS)  # H2D: couplings
-        E0, P = L.find_ground_state(Hs, precision="fp32_mixed", as_complex=False)  # D2H: E0, psi
-        obs = L.measure_ED(P, st, NX, NY, DG, 0.0)                          # H2D psi, D2H grids
+        # find_ground_state + measure_ED in one call; D2H: E0, psi, grids
+        E0, P, obs = L.find_ground_state_measured(Hs, precision="fp32_mixed", as_complex=False)
         Hs.close()
         st.close()
         dt_ = time.perf_counter() - t0
@@ -303,13 +304,12 @@ def gpu_workloads(args, rank, world):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         H.set_couplings(g=gs, t=T_HOP, m=MASS)
-        E0, P = L.find_ground_state(H, precision="fp32_mixed", as_complex=False)
-        obs = L.measure_ED(P, states, NX, NY, DG, 0.0)
+        E0, P, obs = L.find_ground_state_measured(H, precision="fp32_mixed", as_complex=False)
         dt_ = time.perf_counter() - t0
         if it >= args.warmup:
             e2e_reuse.append(dt_)
     dE_e2e = max(dE_e2e, float(np.max(np.abs(E0 - E_ref) / np.abs(E_ref))))
-    h2d = NX * NY * 4 + 3 * KPTS * 8 + N * KPTS * 8
+    h2d = NX * NY * 4 + 3 * KPTS * 8
     d2h = KPTS * 8 * 2 + N * KPTS * 8 + KPTS * (2 * NX * NY + (NX - 1) * (NY - 1)) * 8 + KPTS * 64
     _ = obs
     H.close()
