@@ -190,6 +190,32 @@ function ite_ground_state_ED(states, key_dict, nx, ny, dg; g, t, m)
     return find_ground_state(H)
 end
 
+# ── find_ground_state then measure_ED of its state, as gs_benchmark.jl:116-125
+#    runs them per point, in one call (lgt_ground_state_observe) ─────────────
+function find_ground_state_measured(H::Hamiltonian; tol=1e-10, krylovdim=50, maxiter=300,
+                                    precision::Int32=LGT_FP64, seed::Integer=0)
+    o = defaults(false)
+    o = KrylovOpts(krylovdim, maxiter, tol, precision, o.reorth_passes, o.check_every,
+                   o.refine_steps, UInt64(seed), o.use_graph, 0, 0)
+    N, K = H.basis.dim, H.K
+    nx, ny = H.basis.nx, H.basis.ny
+    E0 = zeros(Float64, K)
+    ψ = zeros(Float64, K, N)                      # [k, row]: row-major panel [N][K]
+    nf = zeros(Float64, nx * ny, K)
+    e2 = zeros(Float64, nx * ny, K)
+    obs = Vector{Obs}(undef, K)
+    info = Ref{Info}()
+    check(ccall((:lgt_ground_state_observe, libpath), Int32,
+                (Ptr{Cvoid}, Ref{KrylovOpts}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, UInt32,
+                 Ref{Info}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Obs}),
+                H.ptr, Ref(o), E0, ψ, C_NULL, 0, info, nf, e2, C_NULL, obs))
+    vecs = [ComplexF64.(ψ[k, :]) for k in 1:K]
+    recs = [(t=0.0, nf_mean=obs[k].nf_mean, nf_even=obs[k].nf_even, nf_odd=obs[k].nf_odd,
+             E2_mean=obs[k].E2_mean, nf_grid=reshape(nf[:, k], nx, ny),
+             E2_grid=reshape(e2[:, k], nx, ny)) for k in 1:K]
+    return K == 1 ? (E0[1], vecs[1], recs[1]) : (E0, vecs, recs)
+end
+
 # ── measure_ED (finite_ed.jl:369-393) ───────────────────────────────────────
 function measure_ED(ψ::Vector{ComplexF64}, states::Basis, nx::Int, ny::Int, dg::Int,
                     t_now::Float64; H::Union{Nothing,Hamiltonian}=nothing)

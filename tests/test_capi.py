@@ -118,3 +118,60 @@ def test_basis_outlives_its_hamiltonians_any_destroy_order():
     from lgt_gb300 import _capi as C
     lib = C.load(build_if_missing=False)
     assert hasattr(lib, "lgt_basis_destroy") and hasattr(lib, "lgt_ham_destroy")
+
+
+def _split_top(s):
+    """Split at commas outside (), {} and []."""
+    out, depth, cur = [], 0, ""
+    for ch in s:
+        if ch in "({[":
+            depth += 1
+        elif ch in ")}]":
+            depth -= 1
+        if ch == "," and depth == 0:
+            out.append(cur.strip())
+            cur = ""
+        else:
+            cur += ch
+    if cur.strip():
+        out.append(cur.strip())
+    return out
+
+
+def _header_arity():
+    src = open(os.path.join(ROOT, "include", "lgt_ed.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    ar = {}
+    for m in re.finditer(r"LGT_API[^;{]*?\b(lgt_[a-z_0-9]+)\s*\(([^;]*?)\)\s*;", src, re.S):
+        params = m.group(2).strip()
+        ar[m.group(1)] = 0 if params in ("", "void") else len(_split_top(params))
+    return ar
+
+
+def test_julia_shim_calls_match_the_header():
+    """Every ccall of the Julia shim names a declared entry point and passes
+    as many arguments as the header's prototype takes (the shim cannot run
+    here: no Julia)."""
+    jl = open(os.path.join(ROOT, "lgt_gb300", "julia", "LGTED.jl")).read()
+    ar = _header_arity()
+    calls = []
+    for m in re.finditer(r"ccall\(\(:(lgt_[a-z_0-9]+), libpath\),", jl):
+        # return type, then the argument-type tuple up to its matching paren
+        rest = jl[m.end():]
+        i = rest.index(",") + 1
+        while rest[i] in " \n":
+            i += 1
+        assert rest[i] == "(", m.group(1)
+        depth, j = 0, i
+        while True:
+            depth += {"(": 1, ")": -1}.get(rest[j], 0)
+            if depth == 0:
+                break
+            j += 1
+        calls.append((m.group(1), rest[i + 1:j]))
+    assert len(calls) >= 10
+    for name, types in calls:
+        assert name in ar, name
+        t = types.replace("\n", " ").strip()
+        n = 0 if t == "" else len(_split_top(t))
+        assert n == ar[name], (name, n, ar[name])
