@@ -12,7 +12,8 @@
 // neighbour tables and the allocation-free observables entry point do not
 // use it.
 //
-// Bases take their streams from a per-device list of released ones.
+// Bases take their streams, and the per-CTA solver's workspaces their timing
+// events, from per-device lists of released ones.
 //
 // Pinned host staging buffers (the per-CTA solver's tables and outputs, the
 // observables' read-back) come from a process-wide cache by size class:
